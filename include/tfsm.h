@@ -1,0 +1,123 @@
+/*
+ * tfsm.h — C ABI of the GB300 T-FSM engine (frequent subgraph mining with MNI support).
+ *
+ * Plain C, no exceptions across the boundary, caller-owned buffers, status-code returns.
+ * Every entry point returns TFSM_OK (0) or a TFSM_ERR_* code; tfsm_last_error() then gives a
+ * message for the calling thread.  A graph handle is immutable after loading and owns its device
+ * copy on the GPU that was current when it was loaded; calls on one handle are serialised
+ * internally, so a handle may be shared by host threads.
+ *
+ * The reference (lyuheng/T-FSM) has no plugin or FFI layer: its hot path is in-process C++.
+ * Each entry point below names the reference interface it replaces.
+ */
+#ifndef TFSM_H
+#define TFSM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TFSM_OK 0
+#define TFSM_ERR_ARG 1        /* invalid argument (null pointer, bad size, malformed pattern) */
+#define TFSM_ERR_IO 2         /* graph file cannot be opened */
+#define TFSM_ERR_FORMAT 3     /* malformed .lg input */
+#define TFSM_ERR_PATTERN 4    /* pattern larger than TFSM_MAX_PATTERN_VERTICES */
+#define TFSM_ERR_LIMIT 5      /* graph beyond the device layout's limits */
+#define TFSM_ERR_NO_DEVICE 9  /* no CUDA device */
+#define TFSM_ERR_CUDA 10      /* CUDA runtime error */
+#define TFSM_ERR_INTERNAL 11
+
+#define TFSM_MAX_PATTERN_VERTICES 16
+
+/* flags */
+#define TFSM_FLAG_EXACT 1u    /* exact MNI per vertex: no early exit at tau */
+#define TFSM_FLAG_PLAIN 2u    /* tfsm_mine: one engine call per candidate pattern (unbatched) */
+#define TFSM_FLAG_NO_SPLIT 4u /* disable splitting of long searches (hub tasks) */
+
+typedef struct tfsm_graph tfsm_graph;
+
+/* One DFS-code edge, as in the reference's dfs_code_t (parallel/graph.h:225-312). */
+typedef struct {
+    int32_t from, to, from_label, edge_label, to_label;
+} tfsm_dfs_code;
+
+/* A connected pattern given by its DFS code (forward edges introduce vertex `to`). */
+typedef struct {
+    int32_t n_codes;
+    const tfsm_dfs_code *codes;
+} tfsm_pattern;
+
+typedef struct {
+    int32_t status;        /* TFSM_OK or an error for this pattern */
+    int32_t frequent;      /* 1 when MNI support >= tau */
+    int32_t n_vertices;
+    int32_t decided_by_filter; /* 1 when domain filtering alone decided the result */
+    uint32_t support;      /* min over vertices of mni[] (exact with TFSM_FLAG_EXACT) */
+    uint32_t mni[TFSM_MAX_PATTERN_VERTICES]; /* per-vertex MNI domain sizes found */
+    uint64_t searches;     /* candidate checks (backtracking searches) started */
+    uint64_t steps;        /* 32-candidate chunks evaluated by the searches */
+} tfsm_result;
+
+typedef struct {
+    uint32_t n_vertices;   /* after label pruning */
+    uint64_t n_edges;      /* undirected, after label pruning */
+    uint32_t n_frequent_vertex_labels;
+    uint32_t n_frequent_edge_labels;
+    uint32_t n_frequent_edge_patterns; /* frequent 1-edge patterns */
+    uint32_t max_degree;
+    uint64_t device_bytes; /* device copy of the graph */
+    double load_ms;        /* parse + prune + device upload */
+} tfsm_graph_info_t;
+
+typedef struct {
+    double load_ms, mine_ms, extend_ms;
+    double init_ms, refine_ms, search_ms;   /* device time per kernel family (CUDA events) */
+    uint64_t init_launches, refine_launches, search_launches;
+    uint64_t init_words, refine_words;      /* bitmap words processed */
+    uint64_t evaluations;  /* candidate patterns evaluated (support evaluations) */
+    uint64_t frequent;     /* frequent patterns, 1-edge patterns included */
+    uint64_t searches, steps, by_filter, engine_calls;
+    int32_t levels;
+} tfsm_mine_stats;
+
+/* Load a .lg graph and prune it for threshold `tau` (label frequency, edge-label frequency and
+ * the frequent 1-edge pattern table), then upload it to the current CUDA device.
+ * Replaces Graph::load_graph (parallel/graph.h:557-570, serial/graph.h:485-494). */
+int tfsm_graph_load(const char *path, int32_t tau, tfsm_graph **out);
+
+/* Same from host arrays: vertex labels [n_vertices], and n_edges undirected edges
+ * (src[i], dst[i], elabels[i]), as the `v` / `e` lines of a .lg file in that order. */
+int tfsm_graph_from_edges(uint32_t n_vertices, const int32_t *vlabels, uint64_t n_edges, const uint32_t *src,
+                          const uint32_t *dst, const int32_t *elabels, int32_t tau, tfsm_graph **out);
+
+void tfsm_graph_free(tfsm_graph *g);
+
+int tfsm_graph_info(const tfsm_graph *g, tfsm_graph_info_t *info);
+
+/* MNI support evaluation of one pattern: is MNI(P) >= tau?  With TFSM_FLAG_EXACT, mni[] holds
+ * the exact per-vertex MNI domain sizes.  Replaces GraMi::frequency (serial/grami.h:261-328) and
+ * the task_container life cycle of the parallel miner (parallel/comper.h:1552-1700, 1069-1152).
+ * `tau` should equal the graph's load threshold (the pruned graph depends on it). */
+int tfsm_evaluate_support(tfsm_graph *g, const tfsm_pattern *pattern, int32_t tau, uint32_t flags,
+                          tfsm_result *out);
+
+/* Batched form: all `n` patterns are evaluated by one launch sequence. */
+int tfsm_evaluate_batch(tfsm_graph *g, const tfsm_pattern *patterns, int32_t n, int32_t tau, uint32_t flags,
+                        tfsm_result *results);
+
+/* Whole mining run: frequent patterns with at most max_nodes vertices (-1: unbounded), written
+ * to `results_path` (may be NULL) in the serial reference's grami_results.txt format.
+ * Replaces GraMi::project (serial/grami.h:224-234) and Worker::run (parallel/worker.h:226-284). */
+int tfsm_mine(tfsm_graph *g, int32_t tau, int32_t max_nodes, uint32_t flags, const char *results_path,
+              tfsm_mine_stats *stats);
+
+/* Message of the last failing call on this thread ("" when none). */
+const char *tfsm_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TFSM_H */

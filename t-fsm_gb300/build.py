@@ -1,0 +1,101 @@
+"""Build recipe of the GB300 T-FSM engine (no cmake; a handful of translation units in parallel).
+
+Produces, inside this package directory:
+  libtfsm_gb300.so   C-ABI library (include/tfsm.h): CUDA kernels for sm_103a + host engine
+  bin/run            command-line drop-in for the reference miners
+  bin/gen_lg         seeded synthetic .lg generator
+Objects go to _build/.  Run `python t-fsm_gb300/build.py` or call build().
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+BIN = PKG / "bin"
+LIB = PKG / "libtfsm_gb300.so"
+ROOT = PKG.parent
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CXXFLAGS = ["-std=c++17", "-O3", "-fPIC", "-Wall", "-Wno-unused-function"]
+
+
+def _cuda_home() -> Path:
+    for c in (os.environ.get("CUDA_HOME"), os.environ.get("CUDA_PATH"), "/usr/local/cuda"):
+        if c and (Path(c) / "bin" / "nvcc").exists():
+            return Path(c)
+    nvcc = shutil.which("nvcc")
+    if nvcc:
+        return Path(nvcc).resolve().parent.parent
+    raise RuntimeError("nvcc not found: set CUDA_HOME")
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + r.stdout)
+
+
+def _stale(target: Path, deps: list[Path]) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(d.stat().st_mtime > t for d in deps)
+
+
+def build(verbose: bool = False) -> Path:
+    cuda = _cuda_home()
+    nvcc = str(cuda / "bin" / "nvcc")
+    BUILD.mkdir(exist_ok=True)
+    BIN.mkdir(exist_ok=True)
+    headers = list(CSRC.rglob("*.h")) + list(CSRC.rglob("*.hpp")) + list(CSRC.rglob("*.cuh")) + [ROOT / "include" / "tfsm.h"]
+    cu = [CSRC / "cuda" / "kernels.cu", CSRC / "engine.cu"]
+    cpp = [CSRC / "miner.cpp", CSRC / "capi.cpp"]
+    jobs = []
+    objs = []
+    for src in cu:
+        obj = BUILD / (src.stem + ".o")
+        objs.append(obj)
+        if _stale(obj, [src] + headers):
+            jobs.append([nvcc, *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(CSRC),
+                         "-c", str(src), "-o", str(obj)])
+    for src in cpp:
+        obj = BUILD / (src.stem + ".o")
+        objs.append(obj)
+        if _stale(obj, [src] + headers):
+            jobs.append(["g++", *CXXFLAGS, "-pthread", "-I", str(CSRC), "-I", str(cuda / "include"), "-c", str(src),
+                         "-o", str(obj)])
+    gen = BIN / "gen_lg"
+    gen_src = CSRC / "tools" / "gen_lg.cpp"
+    if _stale(gen, [gen_src]):
+        jobs.append(["g++", "-std=c++17", "-O2", "-ffp-contract=off", str(gen_src), "-o", str(gen)])
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+        for cmd in jobs:
+            if verbose:
+                print(" ".join(cmd), flush=True)
+        list(ex.map(_run, jobs))
+    if _stale(LIB, objs):
+        cmd = [nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-Xcompiler", "-pthread"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        _run(cmd)
+    run_bin = BIN / "run"
+    run_src = CSRC / "run_main.cpp"
+    if _stale(run_bin, [run_src, LIB]):
+        cmd = ["g++", "-std=c++17", "-O2", str(run_src), "-o", str(run_bin), "-L", str(PKG), "-ltfsm_gb300",
+               "-Wl,-rpath,$ORIGIN/.."]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        _run(cmd)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose="-v" in sys.argv)
+    print(LIB)

@@ -1,0 +1,255 @@
+// C-ABI boundary (declarations and the reference interface each entry point replaces:
+// include/tfsm.h).  Exceptions never cross it; errors become status codes + tfsm_last_error().
+#include <chrono>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+
+#include "../../include/tfsm.h"
+#include "engine.hpp"
+#include "miner.hpp"
+
+struct tfsm_graph {
+    tfsm::LgGraph lg;
+    std::unique_ptr<tfsm::GpuEngine> eng;
+    int tau = 0;
+    double load_ms = 0;
+    std::mutex mu;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+template <class F>
+int guarded(F &&f) {
+    try {
+        g_err.clear();
+        return f();
+    } catch (const tfsm::LgError &e) {
+        return fail(e.code, e.what());
+    } catch (const tfsm::EngineError &e) {
+        return fail(e.code, e.what());
+    } catch (const std::bad_alloc &) {
+        return fail(TFSM_ERR_INTERNAL, "host out of memory");
+    } catch (const std::exception &e) {
+        return fail(TFSM_ERR_INTERNAL, e.what());
+    } catch (...) {
+        return fail(TFSM_ERR_INTERNAL, "unknown error");
+    }
+}
+
+// Validates a DFS code sequence and builds the pattern (Pattern::add_edge semantics).
+bool build_pattern(const tfsm_pattern *tp, tfsm::Pattern &p, std::string &why) {
+    if (!tp || tp->n_codes <= 0 || !tp->codes) {
+        why = "pattern has no DFS codes";
+        return false;
+    }
+    for (int i = 0; i < tp->n_codes; ++i) {
+        const tfsm_dfs_code &c = tp->codes[i];
+        tfsm::DfsCode d{c.from, c.to, c.from_label, c.edge_label, c.to_label};
+        const int n = p.size();
+        if (i == 0) {
+            if (c.from != 0 || c.to != 1) {
+                why = "first DFS code must be (0,1,...)";
+                return false;
+            }
+        } else {
+            const bool fwd = c.to == n && c.from >= 0 && c.from < n;
+            const bool bwd = c.from >= 0 && c.from < n && c.to >= 0 && c.to < n && c.from != c.to;
+            if (!fwd && !bwd) {
+                why = "DFS code " + std::to_string(i) + " neither extends nor closes the pattern";
+                return false;
+            }
+            if (p.label(c.from) != c.from_label || (bwd && p.label(c.to) != c.to_label)) {
+                why = "DFS code " + std::to_string(i) + " has vertex labels inconsistent with earlier codes";
+                return false;
+            }
+            if (bwd && p.adjacent(c.from, c.to)) {
+                why = "DFS code " + std::to_string(i) + " repeats an edge";
+                return false;
+            }
+            if (fwd && n >= TFSM_MAX_PATTERN_VERTICES) {
+                why = "pattern has more than 16 vertices";
+                return false;
+            }
+        }
+        p.push(d);
+    }
+    return true;
+}
+
+void fill_result(const tfsm::EvalResult &r, int n, tfsm_result *out) {
+    std::memset(out, 0, sizeof(*out));
+    out->status = TFSM_OK;
+    out->frequent = r.frequent ? 1 : 0;
+    out->n_vertices = n;
+    out->decided_by_filter = r.by_filter ? 1 : 0;
+    out->support = r.support;
+    for (int i = 0; i < n && i < TFSM_MAX_PATTERN_VERTICES; ++i) out->mni[i] = r.mni[(size_t)i];
+    out->searches = r.searches;
+    out->steps = r.steps;
+}
+
+tfsm::EngineOptions engine_options(uint32_t flags) {
+    tfsm::EngineOptions o;
+    o.exact = (flags & TFSM_FLAG_EXACT) != 0;
+    if (flags & TFSM_FLAG_NO_SPLIT) o.step_budget = 0;
+    return o;
+}
+
+int finish_graph(std::unique_ptr<tfsm_graph> &g, int tau, std::chrono::steady_clock::time_point t0,
+                 tfsm_graph **out) {
+    g->tau = tau;
+    g->eng.reset(new tfsm::GpuEngine(g->lg, 0));
+    g->load_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    *out = g.release();
+    return TFSM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tfsm_graph_load(const char *path, int32_t tau, tfsm_graph **out) {
+    return guarded([&]() -> int {
+        if (!path || !out) return fail(TFSM_ERR_ARG, "null argument");
+        *out = nullptr;
+        auto t0 = std::chrono::steady_clock::now();
+        std::unique_ptr<tfsm_graph> g(new tfsm_graph);
+        g->lg = tfsm::load_lg(path, tau);
+        return finish_graph(g, tau, t0, out);
+    });
+}
+
+int tfsm_graph_from_edges(uint32_t n_vertices, const int32_t *vlabels, uint64_t n_edges, const uint32_t *src,
+                          const uint32_t *dst, const int32_t *elabels, int32_t tau, tfsm_graph **out) {
+    return guarded([&]() -> int {
+        if (!out || (n_vertices && !vlabels) || (n_edges && (!src || !dst || !elabels)))
+            return fail(TFSM_ERR_ARG, "null argument");
+        *out = nullptr;
+        auto t0 = std::chrono::steady_clock::now();
+        tfsm::RawLg raw;
+        raw.vlabel.assign(vlabels, vlabels + n_vertices);
+        raw.edges.reserve((size_t)n_edges);
+        for (uint64_t i = 0; i < n_edges; ++i) {
+            if (src[i] >= n_vertices || dst[i] >= n_vertices) return fail(TFSM_ERR_FORMAT, "edge endpoint out of range");
+            raw.edges.emplace_back(src[i], dst[i], elabels[i]);
+        }
+        std::unique_ptr<tfsm_graph> g(new tfsm_graph);
+        g->lg = tfsm::build_pruned(raw, tau);
+        return finish_graph(g, tau, t0, out);
+    });
+}
+
+void tfsm_graph_free(tfsm_graph *g) { delete g; }
+
+int tfsm_graph_info(const tfsm_graph *g, tfsm_graph_info_t *info) {
+    return guarded([&]() -> int {
+        if (!g || !info) return fail(TFSM_ERR_ARG, "null argument");
+        std::memset(info, 0, sizeof(*info));
+        info->n_vertices = g->lg.n;
+        info->n_edges = g->lg.m;
+        info->n_frequent_vertex_labels = (uint32_t)g->lg.freq_vlabels.size();
+        info->n_frequent_edge_labels = (uint32_t)g->lg.freq_elabels.size();
+        info->n_frequent_edge_patterns = (uint32_t)g->lg.edge_pairs.size();
+        uint32_t md = 0;
+        for (uint32_t v = 0; v < g->lg.n; ++v) md = std::max(md, g->lg.degree(v));
+        info->max_degree = md;
+        info->device_bytes = g->eng->graph_bytes();
+        info->load_ms = g->load_ms;
+        return TFSM_OK;
+    });
+}
+
+int tfsm_evaluate_batch(tfsm_graph *g, const tfsm_pattern *patterns, int32_t n, int32_t tau, uint32_t flags,
+                        tfsm_result *results) {
+    return guarded([&]() -> int {
+        if (!g || (n > 0 && (!patterns || !results)) || n < 0) return fail(TFSM_ERR_ARG, "null argument");
+        std::lock_guard<std::mutex> lk(g->mu);
+        std::vector<tfsm::Pattern> pats((size_t)n);
+        std::vector<const tfsm::Pattern *> ptrs;
+        std::vector<int> idx;
+        int first_err = TFSM_OK;
+        for (int i = 0; i < n; ++i) {
+            std::string why;
+            std::memset(&results[i], 0, sizeof(tfsm_result));
+            if (!build_pattern(&patterns[i], pats[(size_t)i], why)) {
+                results[i].status = why.find("16 vertices") != std::string::npos ? TFSM_ERR_PATTERN : TFSM_ERR_ARG;
+                if (first_err == TFSM_OK) {
+                    first_err = results[i].status;
+                    g_err = why;
+                }
+                continue;
+            }
+            ptrs.push_back(&pats[(size_t)i]);
+            idx.push_back(i);
+        }
+        if (!ptrs.empty()) {
+            tfsm::Level lvl;
+            std::vector<tfsm::EvalResult> res;
+            std::vector<int> par(ptrs.size(), -1);
+            g->eng->evaluate(ptrs, par, nullptr, (uint32_t)std::max(tau, 0), engine_options(flags), lvl, res);
+            for (size_t k = 0; k < ptrs.size(); ++k) fill_result(res[k], ptrs[k]->size(), &results[idx[k]]);
+        }
+        return first_err;
+    });
+}
+
+int tfsm_evaluate_support(tfsm_graph *g, const tfsm_pattern *pattern, int32_t tau, uint32_t flags,
+                          tfsm_result *out) {
+    if (!pattern || !out) return fail(TFSM_ERR_ARG, "null argument");
+    return tfsm_evaluate_batch(g, pattern, 1, tau, flags, out);
+}
+
+int tfsm_mine(tfsm_graph *g, int32_t tau, int32_t max_nodes, uint32_t flags, const char *results_path,
+              tfsm_mine_stats *stats) {
+    return guarded([&]() -> int {
+        if (!g) return fail(TFSM_ERR_ARG, "null graph");
+        std::lock_guard<std::mutex> lk(g->mu);
+        tfsm::MineOptions opt;
+        opt.tau = tau;
+        opt.max_nodes = max_nodes;
+        opt.batched = (flags & TFSM_FLAG_PLAIN) == 0;
+        opt.engine = engine_options(flags);
+        std::vector<tfsm::MinedPattern> pats;
+        tfsm::MineStats st;
+        g->eng->reset_times();
+        tfsm::mine(*g->eng, g->lg, opt, pats, st);
+        if (results_path && !tfsm::write_results(results_path, pats))
+            return fail(TFSM_ERR_IO, std::string("cannot write ") + results_path);
+        if (stats) {
+            std::memset(stats, 0, sizeof(*stats));
+            const tfsm::KernelTimes &kt = g->eng->times();
+            stats->load_ms = g->load_ms;
+            stats->mine_ms = st.mine_ms;
+            stats->extend_ms = st.extend_ms;
+            stats->init_ms = kt.init_ms;
+            stats->refine_ms = kt.refine_ms;
+            stats->search_ms = kt.search_ms;
+            stats->init_launches = kt.init_launches;
+            stats->refine_launches = kt.refine_launches;
+            stats->search_launches = kt.search_launches;
+            stats->init_words = kt.init_words;
+            stats->refine_words = kt.refine_words;
+            stats->evaluations = st.evaluations;
+            stats->frequent = st.frequent;
+            stats->searches = st.searches;
+            stats->steps = st.steps;
+            stats->by_filter = st.by_filter;
+            stats->engine_calls = st.engine_calls;
+            stats->levels = st.levels;
+        }
+        return TFSM_OK;
+    });
+}
+
+const char *tfsm_last_error(void) { return g_err.c_str(); }
+
+}  // extern "C"

@@ -1,0 +1,110 @@
+// Device-side data layout shared by the host engine and the kernels.
+//
+// Data graph in HBM (built once per graph, read-only afterwards):
+//   vertices are renumbered so that each frequent vertex label owns one contiguous id range
+//   [label_start[L], label_start[L+1]) — ids keep the reference's pruned order inside a label.
+//   row_off[n+1] (u32) / col[2m] (u32, ascending) / elab[2m] (u8, dense edge label)
+//   Ascending neighbour ids are therefore ordered by (neighbour label, id): the neighbours of v
+//   that carry label L are one sub-range of v's list, found by two binary searches.
+// Per pattern vertex u, a candidate domain D(u) is a bitmap over the id range of u's label; the
+// same layout holds the "found" (MNI domain members proven by an embedding) and "failed"
+// (proven non-members) bitmaps.  Offsets are in 32-bit words into three level-wide pools.
+#pragma once
+
+#include <cstdint>
+
+namespace tfsm {
+namespace dev {
+
+constexpr int kMaxN = 16;          // pattern vertices supported by the device path
+constexpr uint8_t kNoEdge = 0xff;  // edge-label matrix entry for "not adjacent"
+
+struct Graph {
+    uint32_t n = 0;
+    uint64_t m2 = 0;                 // directed adjacency entries (2 * undirected edges)
+    int n_labels = 0;
+    const uint32_t *row_off = nullptr;   // [n+1]; the host rejects graphs with >= 2^32 adjacency entries
+    const uint32_t *col = nullptr;
+    const uint8_t *elab = nullptr;
+    const uint32_t *label_start = nullptr;  // [n_labels + 1]
+};
+
+// One pattern of a batch.  Plain old data, copied to the device once per batch.
+struct PatDesc {
+    int32_t n;
+    int32_t n_reps;                     // orbit representatives that get search tasks
+    int32_t express;                    // distinct labels + acyclic: decided by arc consistency
+    int32_t lab[kMaxN];                 // dense label index
+    int32_t deg[kMaxN];
+    uint32_t adj[kMaxN];                // adjacency bitmask
+    uint8_t el[kMaxN][kMaxN];           // dense edge label or kNoEdge
+    uint32_t orbit_mask[kMaxN];         // vertices in the automorphism orbit of u (incl. u)
+    int32_t rep[kMaxN];                 // representative of u's orbit
+    uint32_t lstart[kMaxN];             // first id of u's label range
+    uint32_t lsize[kMaxN];              // size of u's label range
+    uint32_t words[kMaxN];              // bitmap words of u = ceil(lsize / 32)
+    uint64_t off[kMaxN];                // word offset of u's bitmaps in the level pools
+    int64_t parent_off[kMaxN];          // word offset of the parent's bitmaps for u, or -1
+    int32_t nlf_n[kMaxN];               // neighbour-label-frequency requirements of u
+    uint8_t nlf_lab[kMaxN][kMaxN];
+    uint8_t nlf_cnt[kMaxN][kMaxN];
+    uint8_t order[kMaxN][kMaxN];        // [start vertex][depth] -> pattern vertex
+    uint32_t bn[kMaxN][kMaxN];          // [start vertex][depth] -> backward-neighbour mask
+};
+
+// Mutable per-pattern state, updated with atomics by the kernels.
+struct PatStatus {
+    uint32_t dom_size[kMaxN];
+    uint32_t found_cnt[kMaxN];
+    uint32_t fail_cnt[kMaxN];
+    uint32_t done_mask;     // representatives whose found count reached tau
+    uint32_t state;         // 0 running, 1 frequent, 2 infrequent
+    uint32_t changed;       // set by a refinement pass that removed a candidate
+    uint32_t pad;
+    unsigned long long searches;      // candidate checks started
+    unsigned long long steps;         // candidate chunks evaluated by the search
+};
+
+enum : uint32_t { kRunning = 0, kFrequent = 1, kInfrequent = 2 };
+
+// Work item of the search kernel: a run of bitmap words of one representative's domain.
+struct SearchItem {
+    uint32_t pat;
+    uint16_t u;
+    uint16_t pad;
+    uint32_t word_lo;
+    uint32_t word_hi;
+};
+
+// Split task produced when a search exceeds its step budget: the depth-1 anchor range of
+// candidate v of representative u is cut into slices that are searched independently.
+struct SplitTask {
+    uint32_t pat;
+    uint16_t u;
+    uint16_t pad;
+    uint32_t v;          // candidate of u (data vertex id)
+    uint32_t lo, hi;     // slice of the depth-1 anchor adjacency positions (absolute)
+    uint32_t group;      // index of the split group (pending counter)
+};
+
+struct SplitGroup {
+    uint32_t pat;
+    uint16_t u;
+    uint16_t pad;
+    uint32_t v;
+    uint32_t pending;    // slices not yet finished
+    uint32_t incomplete; // a slice was skipped (pattern decided): failure cannot be concluded
+};
+
+struct SearchParams {
+    uint32_t tau;
+    uint32_t exact;          // 1: evaluate every candidate, no early exit
+    uint32_t n_items;
+    uint32_t step_budget;    // chunk evaluations before a task is split (0: never split)
+    uint32_t split_slice;    // anchor positions per split slice
+    uint32_t split_cap;      // capacity of the split-task output buffer
+    uint32_t group_cap;      // capacity of the split-group buffer
+};
+
+}  // namespace dev
+}  // namespace tfsm

@@ -1,0 +1,670 @@
+// CUDA kernels of the MNI support evaluation (sm_103a).  Integer gather work: no tensor cores.
+//
+//   k_domain_init  LDF + NLF candidate filter (parallel/gmatch.h:301-415) writing one bitmap
+//                  per pattern vertex over its label's id range; children start from the
+//                  parent's final domain (candidates minus proven non-candidates).
+//   k_refine       one arc-consistency pass over every pattern edge, incl. edge labels
+//                  (pruneCandidates, parallel/gmatch.h:600-658, pull direction).  Iterated to a
+//                  fixpoint for distinct-label trees, whose domains are then the exact MNI
+//                  domains (parallel/comper.h:1619-1653).
+//   k_search       persistent backtracking: one warp per (pattern vertex u, candidate v) task
+//                  looks for one embedding with u -> v (LFTJ, serial/gmatch.h:906-987).  Local
+//                  candidates at each depth are the label sub-range of the smallest backward
+//                  neighbour's adjacency, checked 32 at a time (one per lane) against the domain
+//                  bitmap, injectivity and every other backward neighbour (binary search); the
+//                  survivors are a __ballot_sync mask.  Found embeddings add all their vertices
+//                  (and automorphic images) to the MNI domains; early exit per vertex at tau and
+//                  per pattern when tau can no longer be reached (parallel/comper.h:288-297).
+//                  A task whose search exceeds a step budget splits its depth-1 range into
+//                  slices pushed onto a global queue (hub splitting, parallel/comper.h:640-749).
+//   k_split        processes the slices; the last slice of a group to finish decides failure.
+#include <cstdint>
+#include <cstdio>
+
+#include "dev_common.cuh"
+#include "kernels.h"
+
+namespace tfsm {
+namespace dev {
+
+namespace {
+
+__device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *__restrict__ a, uint32_t lo, uint32_t hi,
+                                                    uint32_t x) {
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(a + mid) < x) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ uint32_t find_item(const uint64_t *__restrict__ prefix, uint32_t n_items, uint64_t gw,
+                                              uint32_t hint) {
+    // items are visited in increasing gw order by a warp: advance from the hint when possible
+    if (hint < n_items && prefix[hint] <= gw && gw < prefix[hint + 1]) return hint;
+    uint32_t lo = 0, hi = n_items;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (prefix[mid] <= gw) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------
+// K1: LDF + NLF filter.  One warp per bitmap word, one lane per vertex of the word.
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_domain_init(Graph g, const PatDesc *__restrict__ descs,
+                                                     PatStatus *__restrict__ st, const uint32_t *__restrict__ item_pu,
+                                                     const uint64_t *__restrict__ prefix, uint32_t n_items,
+                                                     uint32_t *__restrict__ dom, uint32_t *__restrict__ found,
+                                                     uint32_t *__restrict__ failed, const uint32_t *__restrict__ pdom,
+                                                     const uint32_t *__restrict__ pfailed) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint64_t total = prefix[n_items];
+    uint32_t item = 0;
+    for (uint64_t gw = warp; gw < total; gw += nwarps) {
+        item = find_item(prefix, n_items, gw, item);
+        const uint32_t pu = item_pu[item];
+        const uint32_t p = pu >> 8, u = pu & 0xff;
+        const PatDesc &D = descs[p];
+        const uint32_t word = (uint32_t)(gw - prefix[item]);
+        const uint32_t xl = word * 32 + lane;
+        bool pass = xl < D.lsize[u];
+        const int64_t poff = D.parent_off[u];
+        if (poff >= 0) {
+            const uint32_t pw = __ldg(pdom + poff + word) & ~__ldg(pfailed + poff + word);
+            pass = pass && ((pw >> lane) & 1u);
+        }
+        if (__any_sync(0xffffffffu, pass)) {
+            const uint32_t x = D.lstart[u] + xl;
+            uint32_t b = 0, e = 0;
+            if (pass) {
+                b = __ldg(g.row_off + x);
+                e = __ldg(g.row_off + x + 1);
+                pass = (int32_t)(e - b) >= D.deg[u];
+            }
+            const int nn = D.nlf_n[u];
+            for (int k = 0; k < nn && pass; ++k) {
+                const int L = D.nlf_lab[u][k];
+                const uint32_t lo = lower_bound_u32(g.col, b, e, __ldg(g.label_start + L));
+                const uint32_t hi = lower_bound_u32(g.col, lo, e, __ldg(g.label_start + L + 1));
+                pass = (hi - lo) >= (uint32_t)D.nlf_cnt[u][k];
+            }
+        }
+        const uint32_t mask = __ballot_sync(0xffffffffu, pass);
+        if (lane == 0) {
+            const uint64_t o = D.off[u] + word;
+            dom[o] = mask;
+            found[o] = 0;
+            failed[o] = 0;
+            if (mask) atomicAdd(&st[p].dom_size[u], (uint32_t)__popc(mask));
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// K2: one arc-consistency pass.  v stays in D(u) only if, for every pattern neighbour w of u,
+// v has a neighbour x in D(w) reached through an edge with the pattern edge's label.
+// One warp per bitmap word; the warp scans each candidate's label sub-range 32 entries at a time.
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_refine(Graph g, const PatDesc *__restrict__ descs, PatStatus *__restrict__ st,
+                                                const uint32_t *__restrict__ item_pu,
+                                                const uint64_t *__restrict__ prefix, uint32_t n_items,
+                                                uint32_t *__restrict__ dom) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint64_t total = prefix[n_items];
+    uint32_t item = 0;
+    for (uint64_t gw = warp; gw < total; gw += nwarps) {
+        item = find_item(prefix, n_items, gw, item);
+        const uint32_t pu = item_pu[item];
+        const uint32_t p = pu >> 8, u = pu & 0xff;
+        const PatDesc &D = descs[p];
+        const uint32_t word = (uint32_t)(gw - prefix[item]);
+        uint32_t *wp = dom + D.off[u] + word;
+        const uint32_t w0 = __ldcg(wp);
+        if (w0 == 0) continue;
+        uint32_t keep = w0;
+        uint32_t bits = w0;
+        while (bits) {
+            const int bit = __ffs(bits) - 1;
+            bits &= bits - 1;
+            const uint32_t v = D.lstart[u] + word * 32 + bit;
+            const uint32_t vb = __ldg(g.row_off + v), ve = __ldg(g.row_off + v + 1);
+            uint32_t nb = D.adj[u];
+            bool ok = true;
+            while (nb && ok) {
+                const int w = __ffs(nb) - 1;
+                nb &= nb - 1;
+                const uint32_t ls = D.lstart[w], le = ls + D.lsize[w];
+                const uint32_t lo = lower_bound_u32(g.col, vb, ve, ls);
+                const uint32_t hi = lower_bound_u32(g.col, lo, ve, le);
+                const uint8_t el = D.el[u][w];
+                const uint32_t *dw = dom + D.off[w];
+                bool sup = false;
+                for (uint32_t base = lo; base < hi && !sup; base += 32) {
+                    const uint32_t i = base + lane;
+                    bool hit = false;
+                    if (i < hi && __ldg(g.elab + i) == el) {
+                        const uint32_t xl = __ldg(g.col + i) - ls;
+                        hit = (__ldcg(dw + (xl >> 5)) >> (xl & 31)) & 1u;
+                    }
+                    sup = __any_sync(0xffffffffu, hit);
+                }
+                ok = sup;
+            }
+            if (!ok) keep &= ~(1u << bit);
+        }
+        if (keep != w0 && lane == 0) {
+            atomicAnd(wp, keep);
+            atomicSub(&st[p].dom_size[u], (uint32_t)__popc(w0 & ~keep));
+            st[p].changed = 1;
+        }
+    }
+}
+
+
+// ------------------------------------------------------------------------------------------------
+// K5 / K6: persistent search and split slices.
+// ------------------------------------------------------------------------------------------------
+namespace {
+
+struct WarpPlan {
+    uint32_t off[kMaxN];
+    uint32_t lstart[kMaxN];
+    uint32_t lend[kMaxN];
+    uint32_t orbit[kMaxN];
+    uint32_t bn[kMaxN];       // by depth
+    uint8_t order[kMaxN];     // by depth
+    uint8_t el[kMaxN][kMaxN];
+    int32_t n;
+    uint32_t repmask;
+    uint32_t key;             // (pattern << 8 | start vertex) the plan was loaded for
+};
+
+struct WarpState {
+    uint32_t emb[kMaxN];      // by pattern vertex
+    uint32_t pos[kMaxN];      // by depth: next unevaluated anchor position
+    uint32_t end[kMaxN];      // by depth: end of the anchor range
+    uint32_t base[kMaxN];     // by depth: first position of the chunk held in mask
+    uint32_t mask[kMaxN];     // by depth: surviving candidates of that chunk not yet descended into
+    uint8_t anchor[kMaxN];    // by depth: pattern vertex whose adjacency is scanned
+};
+
+enum : int { kFail = 0, kFound = 1, kAbort = 2 };
+
+__device__ __forceinline__ void load_plan(WarpPlan &P, const PatDesc &D, uint32_t p, int u, uint32_t lane) {
+    const uint32_t key = (p << 8) | (uint32_t)u;
+    if (P.key == key) return;  // all lanes read the same shared value
+    __syncwarp();
+    if (lane < (uint32_t)kMaxN) {
+        P.off[lane] = (uint32_t)D.off[lane];
+        P.lstart[lane] = D.lstart[lane];
+        P.lend[lane] = D.lstart[lane] + D.lsize[lane];
+        P.orbit[lane] = D.orbit_mask[lane];
+        P.bn[lane] = D.bn[u][lane];
+        P.order[lane] = D.order[u][lane];
+    }
+    for (uint32_t i = lane; i < (uint32_t)(kMaxN * kMaxN); i += 32) (&P.el[0][0])[i] = (&D.el[0][0])[i];
+    if (lane == 0) {
+        P.n = D.n;
+        uint32_t rm = 0;
+        for (int k = 0; k < D.n; ++k)
+            if (D.rep[k] == k) rm |= 1u << k;
+        P.repmask = rm;
+        P.key = key;
+    }
+    __syncwarp();
+}
+
+// Anchor of depth d: the backward neighbour whose label sub-range is the shortest.  Lane k
+// handles the k-th backward neighbour; a warp minimum picks the winner.
+__device__ __forceinline__ void setup_depth(const Graph &g, const WarpPlan &P, WarpState &S, int d, uint32_t lane) {
+    const int w = P.order[d];
+    const uint32_t bnm = P.bn[d];
+    const int nb = __popc(bnm);
+    unsigned long long key = ~0ull;
+    uint32_t lo = 0, hi = 0;
+    int b = 0;
+    if ((int)lane < nb) {
+        uint32_t m = bnm;
+        for (uint32_t k = 0; k < lane; ++k) m &= m - 1;
+        b = __ffs(m) - 1;
+        const uint32_t y = S.emb[b];
+        const uint32_t rb = __ldg(g.row_off + y), re = __ldg(g.row_off + y + 1);
+        lo = lower_bound_u32(g.col, rb, re, P.lstart[w]);
+        hi = lower_bound_u32(g.col, lo, re, P.lend[w]);
+        key = ((unsigned long long)(hi - lo) << 32) | lane;
+    }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, key, s);
+        key = o < key ? o : key;
+    }
+    const int win = (int)(key & 31ull);
+    lo = __shfl_sync(0xffffffffu, lo, win);
+    hi = __shfl_sync(0xffffffffu, hi, win);
+    b = __shfl_sync(0xffffffffu, b, win);
+    if (lane == 0) {
+        S.pos[d] = lo;
+        S.end[d] = hi;
+        S.mask[d] = 0;
+        S.anchor[d] = (uint8_t)b;
+    }
+    __syncwarp();
+}
+
+// Is adjacency position `idx` of the depth-d anchor a valid extension?  (one lane, one position)
+__device__ __forceinline__ bool check_candidate(const Graph &g, const WarpPlan &P, const WarpState &S,
+                                                const uint32_t *__restrict__ dom, int d, uint32_t idx,
+                                                uint32_t &x_out) {
+    const int w = P.order[d];
+    const int a = S.anchor[d];
+    const uint32_t x = __ldg(g.col + idx);
+    x_out = x;
+    if (__ldg(g.elab + idx) != P.el[w][a]) return false;
+    const uint32_t xl = x - P.lstart[w];
+    if (!((__ldg(dom + P.off[w] + (xl >> 5)) >> (xl & 31)) & 1u)) return false;
+    for (int k = 0; k < d; ++k)
+        if (S.emb[P.order[k]] == x) return false;
+    uint32_t others = P.bn[d] & ~(1u << a);
+    while (others) {
+        const int b = __ffs(others) - 1;
+        others &= others - 1;
+        const uint32_t y = S.emb[b];
+        const uint32_t re = __ldg(g.row_off + y + 1);
+        uint32_t pos = lower_bound_u32(g.col, __ldg(g.row_off + y), re, x);
+        bool hit = false;
+        const uint8_t want = P.el[w][b];
+        while (pos < re && __ldg(g.col + pos) == x) {  // parallel edges: any with the right label
+            if (__ldg(g.elab + pos) == want) {
+                hit = true;
+                break;
+            }
+            ++pos;
+        }
+        if (!hit) return false;
+    }
+    return true;
+}
+
+// Depth-first search for one embedding that extends S.emb[order[0]].  Depth 1 scans positions
+// [lo1, hi1) of its anchor list when `slice` is set.  Returns kAbort once `budget` chunk
+// evaluations are exceeded (budget 0: unlimited).
+__device__ int dfs(const Graph &g, const WarpPlan &P, WarpState &S, const uint32_t *__restrict__ dom, uint32_t lane,
+                   bool slice, uint32_t lo1, uint32_t hi1, uint32_t budget, uint32_t &steps, int &abort_depth) {
+    const int n = P.n;
+    setup_depth(g, P, S, 1, lane);
+    if (slice) {
+        if (lane == 0) {
+            S.pos[1] = lo1;
+            S.end[1] = hi1;
+        }
+        __syncwarp();
+    }
+    int d = 1;
+    for (;;) {
+        const uint32_t m = S.mask[d];
+        if (m == 0) {
+            const uint32_t pos = S.pos[d], end = S.end[d];
+            if (pos >= end) {
+                if (d == 1) return kFail;
+                --d;
+                continue;
+            }
+            if (budget && steps >= budget) {
+                abort_depth = d;
+                return kAbort;
+            }
+            const uint32_t idx = pos + lane;
+            uint32_t x = 0;
+            const bool ok = idx < end && check_candidate(g, P, S, dom, d, idx, x);
+            const uint32_t bal = __ballot_sync(0xffffffffu, ok);
+            ++steps;
+            if (d == n - 1) {
+                if (bal) {
+                    if ((int)lane == __ffs(bal) - 1) S.emb[P.order[d]] = x;
+                    __syncwarp();
+                    return kFound;
+                }
+                if (lane == 0) S.pos[d] = pos + 32;
+                __syncwarp();
+                continue;
+            }
+            if (lane == 0) {
+                S.base[d] = pos;
+                S.pos[d] = pos + 32;
+                S.mask[d] = bal;
+            }
+            __syncwarp();
+            continue;
+        }
+        const int i = __ffs(m) - 1;
+        if (lane == 0) {
+            S.mask[d] = m & (m - 1);
+            S.emb[P.order[d]] = __ldg(g.col + S.base[d] + i);
+        }
+        __syncwarp();
+        ++d;
+        setup_depth(g, P, S, d, lane);
+    }
+}
+
+// Add every vertex of the embedding in S (and its automorphic images) to the found bitmaps.
+__device__ __forceinline__ void mark_found(const WarpPlan &P, const WarpState &S, PatStatus &st,
+                                           uint32_t *__restrict__ found, uint32_t tau, bool exact, uint32_t lane) {
+    if ((int)lane < P.n) {
+        const uint32_t x = S.emb[lane];
+        uint32_t orb = P.orbit[lane];
+        while (orb) {
+            const int k = __ffs(orb) - 1;
+            orb &= orb - 1;
+            const uint32_t xl = x - P.lstart[k];
+            const uint32_t bit = 1u << (xl & 31);
+            const uint32_t old = atomicOr(found + P.off[k] + (xl >> 5), bit);
+            if (!(old & bit)) {
+                const uint32_t c = atomicAdd(&st.found_cnt[k], 1u) + 1;
+                if (!exact && c == tau && ((P.repmask >> k) & 1u)) {
+                    const uint32_t dm = atomicOr(&st.done_mask, 1u << k) | (1u << k);
+                    if ((dm & P.repmask) == P.repmask) atomicCAS(&st.state, kRunning, kFrequent);
+                }
+            }
+        }
+    }
+    __syncwarp();
+}
+
+// v has no embedding as u (nor as any vertex automorphic to u).
+__device__ __forceinline__ void mark_failed(const WarpPlan &P, PatStatus &st, uint32_t *__restrict__ failed, int u,
+                                            uint32_t v, uint32_t tau, bool exact, uint32_t lane) {
+    if (lane == 0) {
+        uint32_t orb = P.orbit[u];
+        while (orb) {
+            const int k = __ffs(orb) - 1;
+            orb &= orb - 1;
+            const uint32_t xl = v - P.lstart[k];
+            const uint32_t bit = 1u << (xl & 31);
+            const uint32_t old = atomicOr(failed + P.off[k] + (xl >> 5), bit);
+            if (k == u && !(old & bit)) {
+                const uint32_t c = atomicAdd(&st.fail_cnt[u], 1u) + 1;
+                if (!exact && __ldcg(&st.dom_size[u]) < c + tau) atomicCAS(&st.state, kRunning, kInfrequent);
+            }
+        }
+    }
+    __syncwarp();
+}
+
+__device__ __forceinline__ bool pattern_stops(const PatStatus &st, int u, bool exact) {
+    if (__ldcg(&st.state) != kRunning) return true;
+    return !exact && ((__ldcg(&st.done_mask) >> u) & 1u);
+}
+
+// Reserve `k` consecutive slots of a bounded buffer; false when full (bounded retries).
+__device__ __forceinline__ bool reserve(uint32_t *counter, uint32_t k, uint32_t cap, uint32_t &first) {
+    uint32_t old = *((volatile uint32_t *)counter);
+    for (int attempt = 0; attempt < 64; ++attempt) {
+        if (old + k > cap || old + k < old) return false;
+        const uint32_t prev = atomicCAS(counter, old, old + k);
+        if (prev == old) {
+            first = old;
+            return true;
+        }
+        old = prev;
+    }
+    return false;
+}
+
+}  // namespace
+
+// counters[0]: next search item, [1]: split tasks written, [2]: split groups written,
+// [3]: next split task to process.
+__global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const PatDesc *__restrict__ descs,
+                                                              PatStatus *__restrict__ st,
+                                                              const SearchItem *__restrict__ items, SearchParams prm,
+                                                              uint32_t *__restrict__ counters,
+                                                              const uint32_t *__restrict__ dom,
+                                                              uint32_t *__restrict__ found,
+                                                              uint32_t *__restrict__ failed,
+                                                              SplitTask *__restrict__ splits,
+                                                              SplitGroup *__restrict__ groups) {
+    __shared__ WarpPlan plans[kSearchWarps];
+    __shared__ WarpState states[kSearchWarps];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t wid = threadIdx.x >> 5;
+    WarpPlan &P = plans[wid];
+    WarpState &S = states[wid];
+    if (lane == 0) P.key = 0xffffffffu;
+    __syncwarp();
+    const bool exact = prm.exact != 0;
+    for (;;) {
+        uint32_t it = 0;
+        if (lane == 0) it = atomicAdd(&counters[0], 1u);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= prm.n_items) break;
+        const SearchItem item = items[it];
+        const uint32_t p = item.pat;
+        const int u = item.u;
+        load_plan(P, descs[p], p, u, lane);
+        PatStatus &ps = st[p];
+        unsigned long long n_search = 0, n_steps = 0;
+        bool stop = false;
+        for (uint32_t word = item.word_lo; word < item.word_hi && !stop; ++word) {
+            if (pattern_stops(ps, u, exact)) break;
+            const uint32_t o = P.off[u] + word;
+            uint32_t cand = __ldg(dom + o) & ~__ldcg(found + o) & ~__ldcg(failed + o);
+            while (cand) {
+                const int b = __ffs(cand) - 1;
+                cand &= cand - 1;
+                if ((__ldcg(found + o) >> b) & 1u) continue;
+                if (pattern_stops(ps, u, exact)) {
+                    stop = true;
+                    break;
+                }
+                const uint32_t v = P.lstart[u] + word * 32 + b;
+                if (lane == 0) S.emb[u] = v;
+                __syncwarp();
+                uint32_t steps = 0;
+                int adepth = 0;
+                ++n_search;
+                int r = dfs(g, P, S, dom, lane, false, 0, 0, prm.step_budget, steps, adepth);
+                if (r == kAbort) {
+                    // Hub splitting: cut the unexplored depth-1 range into slices for k_split.  An
+                    // abort at depth 1 has fully explored every position before pos[1]; deeper, the
+                    // depth-1 chunk that is being explored restarts from its base.
+                    const uint32_t from = (adepth == 1) ? S.pos[1] : S.base[1];
+                    const uint32_t to = S.end[1];
+                    const uint32_t ns = (to - from + prm.split_slice - 1) / prm.split_slice;
+                    bool ok = false;
+                    uint32_t g0 = 0, t0 = 0;
+                    if (lane == 0) {
+                        ok = ns > 0 && reserve(&counters[2], 1, prm.group_cap, g0);
+                        if (ok && !reserve(&counters[1], ns, prm.split_cap, t0)) {
+                            ok = false;
+                            // the group slot stays unused: mark it so k_split never reads it
+                            groups[g0].pending = 0;
+                        }
+                        if (ok) {
+                            groups[g0].pat = p;
+                            groups[g0].u = (uint16_t)u;
+                            groups[g0].v = v;
+                            groups[g0].pending = ns;
+                            groups[g0].incomplete = 0;
+                        }
+                    }
+                    ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+                    g0 = __shfl_sync(0xffffffffu, g0, 0);
+                    t0 = __shfl_sync(0xffffffffu, t0, 0);
+                    if (ok) {
+                        for (uint32_t k = lane; k < ns; k += 32) {
+                            SplitTask t;
+                            t.pat = p;
+                            t.u = (uint16_t)u;
+                            t.pad = 0;
+                            t.v = v;
+                            t.lo = from + k * prm.split_slice;
+                            t.hi = min(to, t.lo + prm.split_slice);
+                            t.group = g0;
+                            splits[t0 + k] = t;
+                        }
+                        n_steps += steps;
+                        continue;  // decided later by the slices
+                    }
+                    // buffers full: finish this task here without a budget
+                    if (lane == 0) S.emb[u] = v;
+                    __syncwarp();
+                    r = dfs(g, P, S, dom, lane, false, 0, 0, 0, steps, adepth);
+                }
+                n_steps += steps;
+                if (r == kFound) mark_found(P, S, ps, found, prm.tau, exact, lane);
+                else mark_failed(P, ps, failed, u, v, prm.tau, exact, lane);
+            }
+        }
+        if (lane == 0 && n_search) {
+            atomicAdd(&ps.searches, n_search);
+            atomicAdd(&ps.steps, n_steps);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kSearchWarps * 32) k_split(Graph g, const PatDesc *__restrict__ descs,
+                                                             PatStatus *__restrict__ st, SearchParams prm,
+                                                             uint32_t *__restrict__ counters,
+                                                             const uint32_t *__restrict__ dom,
+                                                             uint32_t *__restrict__ found,
+                                                             uint32_t *__restrict__ failed,
+                                                             const SplitTask *__restrict__ splits,
+                                                             SplitGroup *__restrict__ groups) {
+    __shared__ WarpPlan plans[kSearchWarps];
+    __shared__ WarpState states[kSearchWarps];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t wid = threadIdx.x >> 5;
+    WarpPlan &P = plans[wid];
+    WarpState &S = states[wid];
+    if (lane == 0) P.key = 0xffffffffu;
+    __syncwarp();
+    const bool exact = prm.exact != 0;
+    const uint32_t n_tasks = min(counters[1], prm.split_cap);
+    for (;;) {
+        uint32_t it = 0;
+        if (lane == 0) it = atomicAdd(&counters[3], 1u);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= n_tasks) break;
+        const SplitTask t = splits[it];
+        const uint32_t p = t.pat;
+        const int u = t.u;
+        load_plan(P, descs[p], p, u, lane);
+        PatStatus &ps = st[p];
+        SplitGroup &grp = groups[t.group];
+        const uint32_t xl = t.v - P.lstart[u];
+        const uint32_t o = P.off[u] + (xl >> 5);
+        const uint32_t bit = 1u << (xl & 31);
+        bool searched = false;
+        if (!pattern_stops(ps, u, exact) && !(__ldcg(found + o) & bit)) {
+            if (lane == 0) S.emb[u] = t.v;
+            __syncwarp();
+            uint32_t steps = 0;
+            int adepth = 0;
+            const int r = dfs(g, P, S, dom, lane, true, t.lo, t.hi, 0, steps, adepth);
+            if (r == kFound) mark_found(P, S, ps, found, prm.tau, exact, lane);
+            if (lane == 0) atomicAdd(&ps.steps, (unsigned long long)steps);
+            searched = true;
+        }
+        if (lane == 0) {
+            if (!searched && !(__ldcg(found + o) & bit)) atomicOr(&grp.incomplete, 1u);
+            __threadfence();
+            const uint32_t left = atomicSub(&grp.pending, 1u) - 1;
+            if (left == 0) {
+                __threadfence();
+                if (!(__ldcg(found + o) & bit) && __ldcg(&grp.incomplete) == 0) {
+                    // every slice finished without an embedding: v fails as u
+                    uint32_t orb = P.orbit[u];
+                    while (orb) {
+                        const int k = __ffs(orb) - 1;
+                        orb &= orb - 1;
+                        const uint32_t kl = t.v - P.lstart[k];
+                        const uint32_t kb = 1u << (kl & 31);
+                        const uint32_t old = atomicOr(failed + P.off[k] + (kl >> 5), kb);
+                        if (k == u && !(old & kb)) {
+                            const uint32_t c = atomicAdd(&ps.fail_cnt[u], 1u) + 1;
+                            if (!exact && __ldcg(&ps.dom_size[u]) < c + prm.tau)
+                                atomicCAS(&ps.state, kRunning, kInfrequent);
+                        }
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Host-side launchers.
+// ------------------------------------------------------------------------------------------------
+static int g_num_sms = 0;
+
+static int num_sms() {
+    if (g_num_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_num_sms <= 0) g_num_sms = 1;
+    }
+    return g_num_sms;
+}
+
+cudaError_t launch_domain_init(const Graph &g, const PatDesc *descs, PatStatus *st, const uint32_t *item_pu,
+                               const uint64_t *prefix, uint32_t n_items, uint64_t total_words, uint32_t *dom,
+                               uint32_t *found, uint32_t *failed, const uint32_t *pdom, const uint32_t *pfailed,
+                               cudaStream_t s) {
+    if (n_items == 0 || total_words == 0) return cudaSuccess;
+    const uint64_t warps = total_words;
+    uint64_t blocks = (warps * 32 + 255) / 256;
+    const uint64_t cap = (uint64_t)num_sms() * 8 * 4;
+    if (blocks > cap) blocks = cap;
+    k_domain_init<<<(unsigned)blocks, 256, 0, s>>>(g, descs, st, item_pu, prefix, n_items, dom, found, failed, pdom,
+                                                   pfailed);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_refine(const Graph &g, const PatDesc *descs, PatStatus *st, const uint32_t *item_pu,
+                          const uint64_t *prefix, uint32_t n_items, uint64_t total_words, uint32_t *dom,
+                          cudaStream_t s) {
+    if (n_items == 0 || total_words == 0) return cudaSuccess;
+    uint64_t blocks = (total_words * 32 + 255) / 256;
+    const uint64_t cap = (uint64_t)num_sms() * 8 * 4;
+    if (blocks > cap) blocks = cap;
+    k_refine<<<(unsigned)blocks, 256, 0, s>>>(g, descs, st, item_pu, prefix, n_items, dom);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchItem *items,
+                          const SearchParams &prm, uint32_t *counters, const uint32_t *dom, uint32_t *found,
+                          uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s) {
+    if (prm.n_items == 0) return cudaSuccess;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search, kSearchWarps * 32, 0);
+    if (per_sm <= 0) per_sm = 1;
+    uint64_t blocks = (uint64_t)num_sms() * (uint64_t)per_sm;
+    const uint64_t need = (prm.n_items + kSearchWarps - 1) / kSearchWarps;
+    if (blocks > need) blocks = need;
+    k_search<<<(unsigned)blocks, kSearchWarps * 32, 0, s>>>(g, descs, st, items, prm, counters, dom, found, failed,
+                                                             splits, groups);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || prm.step_budget == 0) return e;
+    int per_sm2 = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_split, kSearchWarps * 32, 0);
+    if (per_sm2 <= 0) per_sm2 = 1;
+    k_split<<<(unsigned)(num_sms() * per_sm2), kSearchWarps * 32, 0, s>>>(g, descs, st, prm, counters, dom, found,
+                                                                          failed, splits, groups);
+    return cudaGetLastError();
+}
+
+}  // namespace dev
+}  // namespace tfsm

@@ -1,0 +1,29 @@
+// Launchers of the support-evaluation kernels (definitions in kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "dev_common.cuh"
+
+namespace tfsm {
+namespace dev {
+
+constexpr int kSearchWarps = 8;  // warps per block of the search kernels
+
+cudaError_t launch_domain_init(const Graph &g, const PatDesc *descs, PatStatus *st, const uint32_t *item_pu,
+                               const uint64_t *prefix, uint32_t n_items, uint64_t total_words, uint32_t *dom,
+                               uint32_t *found, uint32_t *failed, const uint32_t *pdom, const uint32_t *pfailed,
+                               cudaStream_t s);
+
+cudaError_t launch_refine(const Graph &g, const PatDesc *descs, PatStatus *st, const uint32_t *item_pu,
+                          const uint64_t *prefix, uint32_t n_items, uint64_t total_words, uint32_t *dom,
+                          cudaStream_t s);
+
+// Runs k_search over `prm.n_items` items, then (when a step budget is set) k_split over the
+// slices it produced.  `counters` (4 x u32) must be zero on entry.
+cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchItem *items,
+                          const SearchParams &prm, uint32_t *counters, const uint32_t *dom, uint32_t *found,
+                          uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s);
+
+}  // namespace dev
+}  // namespace tfsm

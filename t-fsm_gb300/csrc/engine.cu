@@ -1,0 +1,466 @@
+// Host orchestration of the GPU support evaluation.
+//
+// evaluate() runs, for one batch of patterns (one pattern in the plain path, a whole growth
+// level in the batched path):
+//   1. k_domain_init     LDF + NLF bitmaps, children starting from their parent's final domains
+//   2. k_refine x R      arc consistency (to a fixpoint for distinct-label trees)
+//   3. host              decide what the domain sizes already decide; matching orders (GQL
+//                        order by domain size, serial/gmatch.h:584-685) for the rest
+//   4. k_search/k_split  backtracking with early exit and hub splitting
+// The device graph is uploaded once in the constructor (label-grouped ids, see dev_common.cuh).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <map>
+#include <numeric>
+
+#include "cuda/dev_common.cuh"
+#include "cuda/kernels.h"
+#include "engine.hpp"
+
+namespace tfsm {
+
+namespace {
+
+#define TFSM_CK(x)                                                                                   \
+    do {                                                                                             \
+        cudaError_t e_ = (x);                                                                        \
+        if (e_ != cudaSuccess) throw EngineError(10, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void ensure(size_t k) {
+        if (k <= n && p) return;
+        release();
+        const size_t bytes = sizeof(T) * std::max<size_t>(k, 1);
+        TFSM_CK(cudaMalloc((void **)&p, bytes));
+        n = std::max<size_t>(k, 1);
+    }
+};
+
+using dev::PatDesc;
+using dev::PatStatus;
+
+}  // namespace
+
+struct Level::Impl {
+    DevBuf<uint32_t> dom, found, failed;
+    DevBuf<PatDesc> descs;
+    std::vector<PatDesc> hdescs;
+    uint64_t words = 0;
+};
+
+Level::Level() : impl(new Impl) {}
+Level::~Level() = default;
+Level::Level(Level &&) noexcept = default;
+Level &Level::operator=(Level &&) noexcept = default;
+size_t Level::size() const { return impl ? impl->hdescs.size() : 0; }
+
+struct GpuEngine::Impl {
+    dev::Graph g;
+    DevBuf<uint32_t> row_off, col, label_start;
+    DevBuf<uint8_t> elab;
+    std::map<int, int> vdense, edense;
+    std::vector<uint32_t> lstart;  // host copy, n_labels + 1
+    uint32_t n = 0;
+    uint64_t m2 = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // per-call scratch
+    DevBuf<PatStatus> status;
+    DevBuf<uint32_t> item_pu;
+    DevBuf<uint64_t> prefix;
+    DevBuf<dev::SearchItem> items;
+    DevBuf<uint32_t> counters;
+    DevBuf<dev::SplitTask> splits;
+    DevBuf<dev::SplitGroup> groups;
+    std::vector<PatStatus> hstatus;
+};
+
+GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
+    auto t0 = std::chrono::steady_clock::now();
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device)
+        throw EngineError(9, "no CUDA device available for the GPU engine");
+    TFSM_CK(cudaSetDevice(device));
+    Impl &I = *impl_;
+    if (lg.offs[lg.n] >= (1ull << 32)) throw EngineError(5, "graph has >= 2^32 adjacency entries");
+    // dense labels
+    for (size_t i = 0; i < lg.freq_vlabels.size(); ++i) I.vdense[lg.freq_vlabels[i]] = (int)i;
+    for (size_t i = 0; i < lg.freq_elabels.size(); ++i) I.edense[lg.freq_elabels[i]] = (int)i;
+    if (I.edense.size() > 250) throw EngineError(5, "more than 250 frequent edge labels");
+    const int NL = (int)lg.freq_vlabels.size();
+    if (NL > 250) throw EngineError(5, "more than 250 frequent vertex labels");
+    // label-grouped renumbering: internal id = label_start[L] + rank within the label
+    std::vector<uint32_t> cnt((size_t)NL + 1, 0);
+    for (uint32_t v = 0; v < lg.n; ++v) cnt[(size_t)I.vdense[lg.vlabel[v]] + 1]++;
+    I.lstart.assign((size_t)NL + 1, 0);
+    for (int L = 0; L < NL; ++L) I.lstart[(size_t)L + 1] = I.lstart[(size_t)L] + cnt[(size_t)L + 1];
+    std::vector<uint32_t> to_int(lg.n), fillv(I.lstart.begin(), I.lstart.end() - 1);
+    std::vector<int> dl(lg.n);
+    for (uint32_t v = 0; v < lg.n; ++v) {
+        dl[v] = I.vdense[lg.vlabel[v]];
+        to_int[v] = fillv[(size_t)dl[v]]++;
+    }
+    std::vector<uint32_t> from_int(lg.n);
+    for (uint32_t v = 0; v < lg.n; ++v) from_int[to_int[v]] = v;
+    // CSR in internal ids; filling lists in increasing source order keeps every list sorted.
+    std::vector<uint32_t> off((size_t)lg.n + 1, 0);
+    for (uint32_t x = 0; x < lg.n; ++x) off[(size_t)x + 1] = off[x] + lg.degree(from_int[x]);
+    std::vector<uint32_t> col(off[lg.n]);
+    std::vector<uint8_t> el(off[lg.n]);
+    std::vector<uint32_t> fill(off.begin(), off.end() - 1);
+    for (uint32_t x = 0; x < lg.n; ++x) {
+        const uint32_t v = from_int[x];
+        for (uint64_t i = lg.offs[v]; i < lg.offs[v + 1]; ++i) {
+            const uint32_t y = to_int[lg.nbr[i]];
+            col[fill[y]] = x;
+            el[fill[y]] = (uint8_t)I.edense[lg.elab[i]];
+            fill[y]++;
+        }
+    }
+    I.n = lg.n;
+    I.m2 = off[lg.n];
+    TFSM_CK(cudaStreamCreateWithFlags(&I.stream, cudaStreamNonBlocking));
+    TFSM_CK(cudaEventCreate(&I.ev0));
+    TFSM_CK(cudaEventCreate(&I.ev1));
+    I.row_off.ensure(off.size());
+    I.col.ensure(col.size());
+    I.elab.ensure(el.size());
+    I.label_start.ensure(I.lstart.size());
+    TFSM_CK(cudaMemcpyAsync(I.row_off.p, off.data(), off.size() * 4, cudaMemcpyHostToDevice, I.stream));
+    if (!col.empty()) {
+        TFSM_CK(cudaMemcpyAsync(I.col.p, col.data(), col.size() * 4, cudaMemcpyHostToDevice, I.stream));
+        TFSM_CK(cudaMemcpyAsync(I.elab.p, el.data(), el.size(), cudaMemcpyHostToDevice, I.stream));
+    }
+    TFSM_CK(cudaMemcpyAsync(I.label_start.p, I.lstart.data(), I.lstart.size() * 4, cudaMemcpyHostToDevice,
+                            I.stream));
+    TFSM_CK(cudaStreamSynchronize(I.stream));
+    I.g.n = lg.n;
+    I.g.m2 = I.m2;
+    I.g.n_labels = NL;
+    I.g.row_off = I.row_off.p;
+    I.g.col = I.col.p;
+    I.g.elab = I.elab.p;
+    I.g.label_start = I.label_start.p;
+    I.counters.ensure(4);
+    I.splits.ensure(1u << 20);
+    I.groups.ensure(1u << 17);
+    upload_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+GpuEngine::~GpuEngine() {
+    if (impl_) {
+        if (impl_->stream) cudaStreamSynchronize(impl_->stream);
+        if (impl_->ev0) cudaEventDestroy(impl_->ev0);
+        if (impl_->ev1) cudaEventDestroy(impl_->ev1);
+        if (impl_->stream) cudaStreamDestroy(impl_->stream);
+    }
+}
+
+uint64_t GpuEngine::graph_bytes() const { return (uint64_t)(impl_->n + 1) * 4 + impl_->m2 * 5; }
+uint32_t GpuEngine::n_vertices() const { return impl_->n; }
+int GpuEngine::dense_label(int label) const {
+    auto it = impl_->vdense.find(label);
+    return it == impl_->vdense.end() ? -1 : it->second;
+}
+
+namespace {
+
+// GQL-style order from `start` (serial/gmatch.h:584-620): repeatedly take the unvisited vertex
+// adjacent to the visited set with the fewest candidates, ties to the larger pattern degree.
+void gql_plan(const Pattern &pat, const uint32_t *dsize, int start, uint8_t *order, uint32_t *bn) {
+    const int n = pat.size();
+    uint32_t visited = 1u << start, adjm = 0;
+    for (auto &e : pat.vertices[start].edges) adjm |= 1u << e.to;
+    order[0] = (uint8_t)start;
+    bn[0] = 0;
+    for (int i = 1; i < n; ++i) {
+        int next = -1;
+        for (int j = 0; j < n; ++j) {
+            if ((visited >> j) & 1u || !((adjm >> j) & 1u)) continue;
+            if (next < 0 || dsize[j] < dsize[next] || (dsize[j] == dsize[next] && pat.degree(j) > pat.degree(next)))
+                next = j;
+        }
+        uint32_t b = 0;
+        for (auto &e : pat.vertices[next].edges)
+            if ((visited >> e.to) & 1u) b |= 1u << e.to;
+        order[i] = (uint8_t)next;
+        bn[i] = b;
+        visited |= 1u << next;
+        for (auto &e : pat.vertices[next].edges) adjm |= 1u << e.to;
+    }
+}
+
+}  // namespace
+
+void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::vector<int> &parent, const Level *prev,
+                         uint32_t tau, const EngineOptions &opt, Level &out, std::vector<EvalResult> &res) {
+    Impl &I = *impl_;
+    const size_t P = pats.size();
+    res.assign(P, EvalResult());
+    if (!out.impl) out.impl.reset(new Level::Impl);
+    Level::Impl &L = *out.impl;
+    L.hdescs.assign(P, PatDesc());
+    std::vector<char> trivial(P, 0), express(P, 0);
+    uint64_t total = 0;
+    for (size_t p = 0; p < P; ++p) {
+        const Pattern &pat = *pats[p];
+        PatDesc &D = L.hdescs[p];
+        std::memset(&D, 0, sizeof(D));
+        const int n = pat.size();
+        if (n > dev::kMaxN) throw EngineError(4, "pattern has more than 16 vertices");
+        D.n = n;
+        res[p].mni.assign((size_t)n, 0);
+        std::memset(D.el, dev::kNoEdge, sizeof(D.el));
+        for (int u = 0; u < n; ++u) {
+            const int dl = dense_label(pat.label(u));
+            if (dl < 0) trivial[p] = 1;
+            D.lab[u] = dl < 0 ? 0 : dl;
+            D.deg[u] = pat.degree(u);
+            for (auto &e : pat.vertices[u].edges) {
+                D.adj[u] |= 1u << e.to;
+                auto it = I.edense.find(e.label);
+                if (it == I.edense.end()) trivial[p] = 1;
+                else D.el[u][e.to] = (uint8_t)it->second;
+            }
+            std::map<int, int> need;
+            for (auto &e : pat.vertices[u].edges) need[dense_label(pat.label(e.to))]++;
+            for (auto &kv : need) {
+                if (kv.first < 0) continue;
+                D.nlf_lab[u][D.nlf_n[u]] = (uint8_t)kv.first;
+                D.nlf_cnt[u][D.nlf_n[u]] = (uint8_t)std::min(kv.second, 255);
+                D.nlf_n[u]++;
+            }
+            D.lstart[u] = I.lstart[(size_t)D.lab[u]];
+            D.lsize[u] = I.lstart[(size_t)D.lab[u] + 1] - D.lstart[u];
+            D.words[u] = (D.lsize[u] + 31) / 32;
+            D.off[u] = total;
+            total += D.words[u];
+            D.parent_off[u] = -1;
+            if (prev && parent[p] >= 0) {
+                const PatDesc &PD = prev->impl->hdescs[(size_t)parent[p]];
+                if (u < PD.n) D.parent_off[u] = (int64_t)PD.off[u];
+            }
+        }
+        const std::vector<int> orb = automorphism_orbits(pat);
+        for (int u = 0; u < n; ++u) {
+            D.rep[u] = orb[u];
+            for (int k = 0; k < n; ++k)
+                if (orb[k] == orb[u]) D.orbit_mask[u] |= 1u << k;
+            if (orb[u] == u) D.n_reps++;
+        }
+        express[p] = pat.distinct_labels() && pat.acyclic();
+        D.express = express[p];
+    }
+    if (total >= (1ull << 32)) throw EngineError(6, "batch needs more than 2^32 bitmap words");
+    L.words = total;
+    L.dom.ensure(total);
+    L.found.ensure(total);
+    L.failed.ensure(total);
+    L.descs.ensure(P);
+    I.status.ensure(P);
+    I.hstatus.assign(P, PatStatus());
+    TFSM_CK(cudaMemcpyAsync(L.descs.p, L.hdescs.data(), P * sizeof(PatDesc), cudaMemcpyHostToDevice, I.stream));
+    TFSM_CK(cudaMemsetAsync(I.status.p, 0, P * sizeof(PatStatus), I.stream));
+
+    const uint32_t *pdom = prev ? prev->impl->dom.p : nullptr;
+    const uint32_t *pfailed = prev ? prev->impl->failed.p : nullptr;
+
+    // ---- domain init over every (pattern, vertex) ----
+    std::vector<uint32_t> item_pu;
+    std::vector<uint64_t> prefix;
+    auto build_items = [&](const std::vector<char> &active) {
+        item_pu.clear();
+        prefix.assign(1, 0);
+        for (size_t p = 0; p < P; ++p) {
+            if (!active[p]) continue;
+            const PatDesc &D = L.hdescs[p];
+            for (int u = 0; u < D.n; ++u) {
+                item_pu.push_back(((uint32_t)p << 8) | (uint32_t)u);
+                prefix.push_back(prefix.back() + D.words[u]);
+            }
+        }
+        I.item_pu.ensure(item_pu.size());
+        I.prefix.ensure(prefix.size());
+        if (!item_pu.empty()) {
+            TFSM_CK(cudaMemcpyAsync(I.item_pu.p, item_pu.data(), item_pu.size() * 4, cudaMemcpyHostToDevice, I.stream));
+            TFSM_CK(cudaMemcpyAsync(I.prefix.p, prefix.data(), prefix.size() * 8, cudaMemcpyHostToDevice, I.stream));
+        }
+    };
+    auto read_status = [&]() {
+        TFSM_CK(cudaMemcpyAsync(I.hstatus.data(), I.status.p, P * sizeof(PatStatus), cudaMemcpyDeviceToHost,
+                                I.stream));
+        TFSM_CK(cudaStreamSynchronize(I.stream));
+    };
+    auto time_since_ev0 = [&]() -> double {
+        TFSM_CK(cudaEventRecord(I.ev1, I.stream));
+        TFSM_CK(cudaEventSynchronize(I.ev1));
+        float ms = 0;
+        TFSM_CK(cudaEventElapsedTime(&ms, I.ev0, I.ev1));
+        return ms;
+    };
+
+    std::vector<char> active(P, 0);
+    for (size_t p = 0; p < P; ++p) active[p] = !trivial[p];
+    build_items(active);
+    if (!item_pu.empty()) {
+        TFSM_CK(cudaEventRecord(I.ev0, I.stream));
+        TFSM_CK(dev::launch_domain_init(I.g, L.descs.p, I.status.p, I.item_pu.p, I.prefix.p, (uint32_t)item_pu.size(),
+                                        prefix.back(), L.dom.p, L.found.p, L.failed.p, pdom, pfailed, I.stream));
+        times_.init_ms += time_since_ev0();
+        times_.init_launches++;
+        times_.init_words += prefix.back();
+    }
+    read_status();
+
+    // ---- arc-consistency rounds ----
+    auto viable = [&](size_t p) {
+        const PatDesc &D = L.hdescs[p];
+        for (int u = 0; u < D.n; ++u) {
+            const uint32_t ds = I.hstatus[p].dom_size[u];
+            if (opt.exact ? ds == 0 : ds < tau) return false;
+        }
+        return true;
+    };
+    for (uint32_t round = 0;; ++round) {
+        for (size_t p = 0; p < P; ++p) {
+            bool a = !trivial[p] && viable(p);
+            if (round > 0) a = a && I.hstatus[p].changed != 0;
+            if (!express[p] && round >= opt.refine_rounds) a = false;
+            if (round >= 64) a = false;
+            active[p] = a;
+        }
+        if (std::find(active.begin(), active.end(), 1) == active.end()) break;
+        for (size_t p = 0; p < P; ++p) I.hstatus[p].changed = 0;
+        TFSM_CK(cudaMemcpyAsync(I.status.p, I.hstatus.data(), P * sizeof(PatStatus), cudaMemcpyHostToDevice,
+                                I.stream));
+        build_items(active);
+        TFSM_CK(cudaEventRecord(I.ev0, I.stream));
+        TFSM_CK(dev::launch_refine(I.g, L.descs.p, I.status.p, I.item_pu.p, I.prefix.p, (uint32_t)item_pu.size(),
+                                   prefix.back(), L.dom.p, I.stream));
+        times_.refine_ms += time_since_ev0();
+        times_.refine_launches++;
+        times_.refine_words += prefix.back();
+        read_status();
+    }
+
+    // ---- decisions from domain sizes; plans for the rest ----
+    std::vector<char> need_search(P, 0);
+    bool any_search = false;
+    for (size_t p = 0; p < P; ++p) {
+        PatDesc &D = L.hdescs[p];
+        EvalResult &r = res[p];
+        if (trivial[p]) {
+            r.by_filter = true;
+            continue;
+        }
+        const PatStatus &s = I.hstatus[p];
+        uint32_t mn = UINT32_MAX;
+        for (int u = 0; u < D.n; ++u) mn = std::min(mn, s.dom_size[u]);
+        if (express[p]) {
+            // an empty domain means no embedding at all; otherwise the arc-consistent domains
+            // of a distinct-label tree are its MNI domains
+            for (int u = 0; u < D.n; ++u) r.mni[(size_t)u] = mn == 0 ? 0 : s.dom_size[u];
+            r.support = mn;
+            r.frequent = mn >= tau;
+            r.by_filter = true;
+            continue;
+        }
+        if (opt.exact ? mn == 0 : mn < tau) {
+            r.by_filter = true;
+            continue;
+        }
+        need_search[p] = 1;
+        any_search = true;
+        for (int u = 0; u < D.n; ++u)
+            if (D.rep[u] == u) gql_plan(*pats[p], s.dom_size, u, D.order[u], D.bn[u]);
+    }
+    if (!any_search) return;
+    TFSM_CK(cudaMemcpyAsync(L.descs.p, L.hdescs.data(), P * sizeof(PatDesc), cudaMemcpyHostToDevice, I.stream));
+
+    // ---- search items, interleaved across patterns and representatives ----
+    std::vector<dev::SearchItem> items;
+    {
+        struct Q {
+            uint32_t p, u, w, words;
+        };
+        std::vector<Q> qs;
+        for (size_t p = 0; p < P; ++p) {
+            if (!need_search[p]) continue;
+            const PatDesc &D = L.hdescs[p];
+            for (int u = 0; u < D.n; ++u)
+                if (D.rep[u] == u) qs.push_back({(uint32_t)p, (uint32_t)u, 0, D.words[u]});
+        }
+        const uint32_t cw = std::max<uint32_t>(1, opt.chunk_words);
+        bool more = true;
+        while (more) {
+            more = false;
+            for (Q &q : qs) {
+                if (q.w >= q.words) continue;
+                dev::SearchItem it;
+                it.pat = q.p;
+                it.u = (uint16_t)q.u;
+                it.pad = 0;
+                it.word_lo = q.w;
+                it.word_hi = std::min(q.words, q.w + cw);
+                q.w = it.word_hi;
+                items.push_back(it);
+                more = true;
+            }
+        }
+    }
+    I.items.ensure(items.size());
+    TFSM_CK(cudaMemcpyAsync(I.items.p, items.data(), items.size() * sizeof(dev::SearchItem), cudaMemcpyHostToDevice,
+                            I.stream));
+    TFSM_CK(cudaMemsetAsync(I.counters.p, 0, 4 * sizeof(uint32_t), I.stream));
+    dev::SearchParams prm;
+    prm.tau = tau;
+    prm.exact = opt.exact ? 1 : 0;
+    prm.n_items = (uint32_t)items.size();
+    prm.step_budget = opt.step_budget;
+    prm.split_slice = std::max<uint32_t>(32, opt.split_slice);
+    prm.split_cap = (uint32_t)I.splits.n;
+    prm.group_cap = (uint32_t)I.groups.n;
+    TFSM_CK(cudaEventRecord(I.ev0, I.stream));
+    TFSM_CK(dev::launch_search(I.g, L.descs.p, I.status.p, I.items.p, prm, I.counters.p, L.dom.p, L.found.p,
+                               L.failed.p, I.splits.p, I.groups.p, I.stream));
+    times_.search_ms += time_since_ev0();
+    times_.search_launches++;
+    read_status();
+
+    for (size_t p = 0; p < P; ++p) {
+        if (!need_search[p]) continue;
+        const PatDesc &D = L.hdescs[p];
+        const PatStatus &s = I.hstatus[p];
+        EvalResult &r = res[p];
+        r.searches = s.searches;
+        r.steps = s.steps;
+        uint32_t mn = UINT32_MAX;
+        bool all_reps = true;
+        for (int u = 0; u < D.n; ++u) {
+            r.mni[(size_t)u] = s.found_cnt[u];
+            mn = std::min(mn, s.found_cnt[u]);
+            if (D.rep[u] == u && s.found_cnt[u] < tau) all_reps = false;
+        }
+        r.support = mn;
+        if (opt.exact) r.frequent = mn >= tau;
+        else r.frequent = s.state == dev::kFrequent || (s.state == dev::kRunning && all_reps);
+    }
+}
+
+}  // namespace tfsm

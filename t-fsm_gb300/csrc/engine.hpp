@@ -1,0 +1,80 @@
+// GPU support-evaluation engine: device graph, batch evaluation of patterns, level memory.
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "host/lg_graph.hpp"
+#include "host/pattern.hpp"
+
+namespace tfsm {
+
+struct EngineError : std::runtime_error {
+    int code;
+    EngineError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+struct EvalResult {
+    bool frequent = false;
+    bool by_filter = false;            // decided without search (domain sizes / arc consistency)
+    std::vector<uint32_t> mni;         // per pattern vertex; exact in exact mode
+    uint32_t support = 0;              // min over vertices of mni
+    uint64_t searches = 0;             // candidate checks
+    uint64_t steps = 0;                // 32-candidate chunks evaluated by the search
+};
+
+struct EngineOptions {
+    bool exact = false;                // evaluate every candidate (exact MNI), no early exit
+    uint32_t step_budget = 4096;       // chunk evaluations before a task is split (0: never)
+    uint32_t split_slice = 256;        // depth-1 anchor positions per split slice
+    uint32_t chunk_words = 4;          // bitmap words per search work item (x32 candidates)
+    uint32_t refine_rounds = 2;        // arc-consistency passes for patterns that need search
+};
+
+struct KernelTimes {                   // accumulated device time (CUDA events), milliseconds
+    double init_ms = 0, refine_ms = 0, search_ms = 0;
+    uint64_t init_launches = 0, refine_launches = 0, search_launches = 0;
+    uint64_t init_words = 0, refine_words = 0;  // bitmap words processed
+};
+
+// Device memory of one evaluated batch; kept while the batch's patterns are parents.
+struct Level {
+    struct Impl;
+    std::unique_ptr<Impl> impl;
+    Level();
+    ~Level();
+    Level(Level &&) noexcept;
+    Level &operator=(Level &&) noexcept;
+    size_t size() const;  // patterns in the batch
+};
+
+class GpuEngine {
+public:
+    GpuEngine(const LgGraph &g, int device = 0);
+    ~GpuEngine();
+    GpuEngine(const GpuEngine &) = delete;
+    GpuEngine &operator=(const GpuEngine &) = delete;
+
+    // Evaluate `pats` against the graph.  parent[i] indexes the pattern's parent in `prev`
+    // (or -1).  `out` receives this batch's device memory for the next level.
+    void evaluate(const std::vector<const Pattern *> &pats, const std::vector<int> &parent, const Level *prev,
+                  uint32_t tau, const EngineOptions &opt, Level &out, std::vector<EvalResult> &res);
+
+    const KernelTimes &times() const { return times_; }
+    void reset_times() { times_ = KernelTimes(); }
+    uint64_t graph_bytes() const;
+    double upload_ms() const { return upload_ms_; }
+    int dense_label(int label) const;  // -1 when the label is not frequent
+    uint32_t n_vertices() const;
+
+private:
+    struct Impl;
+    std::unique_ptr<Impl> impl_;
+    KernelTimes times_;
+    double upload_ms_ = 0;
+};
+
+}  // namespace tfsm

@@ -1,0 +1,165 @@
+#include "miner.hpp"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <fstream>
+#include <memory>
+#include <thread>
+
+namespace tfsm {
+
+namespace {
+
+struct Node {
+    Pattern pat;
+    EvalResult res;
+    Level *lvl = nullptr;  // device memory holding this pattern's final domains
+    int idx = 0;           // index inside lvl
+};
+
+// Extends every frequent node (rightmost extension + canonical check), in parallel over parents.
+void extend_all(const std::vector<Node> &level, const ExtendContext &ctx, int threads,
+                std::vector<std::vector<Pattern>> &kids) {
+    kids.assign(level.size(), {});
+    std::atomic<size_t> next(0);
+    auto work = [&]() {
+        for (;;) {
+            const size_t i = next.fetch_add(1);
+            if (i >= level.size()) break;
+            if (!level[i].res.frequent) continue;
+            extend_pattern(level[i].pat, ctx, kids[i]);
+        }
+    };
+    const int t = std::max(1, std::min<int>(threads, (int)level.size()));
+    if (t == 1) {
+        work();
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int k = 0; k < t; ++k) th.emplace_back(work);
+    for (auto &x : th) x.join();
+}
+
+}  // namespace
+
+void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<MinedPattern> &out, MineStats &st) {
+    auto t0 = std::chrono::steady_clock::now();
+    out.clear();
+    st = MineStats();
+    const int threads = opt.host_threads > 0 ? opt.host_threads : (int)std::max(1u, std::thread::hardware_concurrency());
+    ExtendContext ctx;
+    ctx.freq_elabels = g.freq_elabels;
+    ctx.max_nodes = opt.max_nodes;
+    for (auto &ep : g.edge_pairs) {
+        ctx.neighbor_labels[ep.la].insert(ep.lb);
+        ctx.neighbor_labels[ep.lb].insert(ep.la);
+    }
+    const uint32_t tau = (uint32_t)std::max(opt.tau, 0);
+
+    // Levels own device memory; a level is released once its children are evaluated.
+    std::vector<std::unique_ptr<Level>> prev_levels, cur_levels;
+
+    auto evaluate_level = [&](std::vector<Node> &nodes, const std::vector<int> &parent_of,
+                              const std::vector<Node> *parents) {
+        if (nodes.empty()) return;
+        st.evaluations += nodes.size();
+        if (opt.batched) {
+            std::vector<const Pattern *> pats;
+            std::vector<int> par;
+            const Level *prev = nullptr;
+            for (size_t i = 0; i < nodes.size(); ++i) {
+                pats.push_back(&nodes[i].pat);
+                if (parents && parent_of[i] >= 0) {
+                    const Node &pn = (*parents)[(size_t)parent_of[i]];
+                    par.push_back(pn.idx);
+                    prev = pn.lvl;  // one level object for the whole parent level
+                } else {
+                    par.push_back(-1);
+                }
+            }
+            cur_levels.emplace_back(new Level);
+            std::vector<EvalResult> res;
+            eng.evaluate(pats, par, prev, tau, opt.engine, *cur_levels.back(), res);
+            st.engine_calls++;
+            for (size_t i = 0; i < nodes.size(); ++i) {
+                nodes[i].res = std::move(res[i]);
+                nodes[i].lvl = cur_levels.back().get();
+                nodes[i].idx = (int)i;
+            }
+        } else {
+            for (size_t i = 0; i < nodes.size(); ++i) {
+                std::vector<const Pattern *> pats{&nodes[i].pat};
+                std::vector<int> par{-1};
+                const Level *prev = nullptr;
+                if (parents && parent_of[i] >= 0) {
+                    const Node &pn = (*parents)[(size_t)parent_of[i]];
+                    par[0] = pn.idx;
+                    prev = pn.lvl;
+                }
+                cur_levels.emplace_back(new Level);
+                std::vector<EvalResult> res;
+                eng.evaluate(pats, par, prev, tau, opt.engine, *cur_levels.back(), res);
+                st.engine_calls++;
+                nodes[i].res = std::move(res[0]);
+                nodes[i].lvl = cur_levels.back().get();
+                nodes[i].idx = 0;
+            }
+        }
+        for (auto &nd : nodes) {
+            st.searches += nd.res.searches;
+            st.steps += nd.res.steps;
+            st.by_filter += nd.res.by_filter ? 1 : 0;
+        }
+    };
+
+    // level 1: the frequent 1-edge patterns (frequent by construction of the pair table,
+    // parallel/grami.h:116-153); evaluated on the GPU for their domains
+    std::vector<Node> level;
+    for (auto &ep : g.edge_pairs) {
+        Node nd;
+        nd.pat.push(DfsCode{0, 1, ep.la, ep.el, ep.lb});
+        level.push_back(std::move(nd));
+    }
+    evaluate_level(level, std::vector<int>(level.size(), -1), nullptr);
+    for (auto &nd : level) {
+        if (!opt.engine.exact) nd.res.frequent = true;
+        else nd.res.frequent = nd.res.support >= tau;
+    }
+    st.levels = level.empty() ? 0 : 1;
+    while (!level.empty()) {
+        for (auto &nd : level)
+            if (nd.res.frequent) out.push_back({nd.pat, nd.res});
+        auto te = std::chrono::steady_clock::now();
+        std::vector<std::vector<Pattern>> kids;
+        extend_all(level, ctx, threads, kids);
+        std::vector<Node> next;
+        std::vector<int> parent_of;
+        for (size_t i = 0; i < kids.size(); ++i)
+            for (auto &k : kids[i]) {
+                Node nd;
+                nd.pat = std::move(k);
+                next.push_back(std::move(nd));
+                parent_of.push_back((int)i);
+            }
+        st.extend_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - te).count();
+        if (next.empty()) break;
+        prev_levels = std::move(cur_levels);
+        cur_levels.clear();
+        evaluate_level(next, parent_of, &level);
+        prev_levels.clear();  // parents' device memory
+        level = std::move(next);
+        st.levels++;
+    }
+    st.frequent = out.size();
+    st.mine_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+bool write_results(const std::string &path, const std::vector<MinedPattern> &pats) {
+    std::ofstream f(path);
+    if (!f) return false;
+    for (auto &mp : pats) f << mp.pat.to_results_block();
+    return (bool)f;
+}
+
+}  // namespace tfsm

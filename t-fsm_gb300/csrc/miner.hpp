@@ -1,0 +1,51 @@
+// Frequent-subgraph miner driving the GPU engine.
+//
+// Same search space and output as the reference miners: frequent 1-edge patterns from the label
+// pair table, rightmost extension with the canonical check (host), MNI support evaluated on the
+// GPU, children only of frequent canonical patterns, at most `max_nodes` pattern vertices.
+//   batched: every candidate of one growth level is evaluated by one engine call
+//   plain:   one engine call (one launch sequence) per candidate pattern
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "engine.hpp"
+#include "host/lg_graph.hpp"
+#include "host/pattern.hpp"
+
+namespace tfsm {
+
+struct MineOptions {
+    int tau = 1;
+    int max_nodes = -1;
+    bool batched = true;
+    int host_threads = 0;  // threads for extension + canonical checks (0: hardware concurrency)
+    EngineOptions engine;
+};
+
+struct MinedPattern {
+    Pattern pat;
+    EvalResult res;
+};
+
+struct MineStats {
+    double mine_ms = 0;
+    double extend_ms = 0;           // host pattern growth + canonical checks
+    uint64_t evaluations = 0;       // candidate patterns whose support was evaluated
+    uint64_t frequent = 0;
+    uint64_t searches = 0;
+    uint64_t steps = 0;
+    uint64_t by_filter = 0;         // decided without search
+    uint64_t engine_calls = 0;
+    int levels = 0;
+};
+
+// Mines all frequent patterns; `out` lists them level by level in generation order.
+void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<MinedPattern> &out, MineStats &st);
+
+// Writes `pats` in the serial reference's grami_results.txt format.
+bool write_results(const std::string &path, const std::vector<MinedPattern> &pats);
+
+}  // namespace tfsm

@@ -1,0 +1,69 @@
+// `run`: command-line drop-in for the reference miners (parallel/run.cpp:11-82, serial/run.cpp).
+//
+//   run -file G.lg -freq TAU [-thread T] [-maxNodes N] [-plain] [-exact] [-out PATH]
+//
+// Frequent patterns go to ./grami_results.txt (or -out PATH) in the serial build's format
+// (serial/grami.h:622-635); timing and counts are printed as the parallel build prints them.
+// `-thread` is accepted for compatibility; host work uses all cores and mining runs on the GPU.
+// Unlike the reference, `-file` may appear anywhere on the command line.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "../../include/tfsm.h"
+
+static const char *opt(int argc, char **argv, const char *name) {
+    for (int i = 1; i + 1 < argc; ++i)
+        if (!std::strcmp(argv[i], name)) return argv[i + 1];
+    return nullptr;
+}
+
+static bool flag(int argc, char **argv, const char *name) {
+    for (int i = 1; i < argc; ++i)
+        if (!std::strcmp(argv[i], name)) return true;
+    return false;
+}
+
+int main(int argc, char **argv) {
+    const char *file = opt(argc, argv, "-file");
+    const char *freq = opt(argc, argv, "-freq");
+    if (!file || !freq) {
+        std::fprintf(stderr, "usage: run -file G.lg -freq TAU [-thread T] [-maxNodes N] [-plain] [-exact] [-out PATH]\n");
+        return 2;
+    }
+    const int tau = std::atoi(freq);
+    const int max_nodes = opt(argc, argv, "-maxNodes") ? std::atoi(opt(argc, argv, "-maxNodes")) : -1;
+    const char *out = opt(argc, argv, "-out") ? opt(argc, argv, "-out") : "./grami_results.txt";
+    uint32_t flags = 0;
+    if (flag(argc, argv, "-plain")) flags |= TFSM_FLAG_PLAIN;
+    if (flag(argc, argv, "-exact")) flags |= TFSM_FLAG_EXACT;
+
+    tfsm_graph *g = nullptr;
+    int rc = tfsm_graph_load(file, tau, &g);
+    if (rc != TFSM_OK) {
+        std::fprintf(stderr, "error %d: %s\n", rc, tfsm_last_error());
+        return 1;
+    }
+    tfsm_mine_stats st;
+    rc = tfsm_mine(g, tau, max_nodes, flags, out, &st);
+    if (rc != TFSM_OK) {
+        std::fprintf(stderr, "error %d: %s\n", rc, tfsm_last_error());
+        tfsm_graph_free(g);
+        return 1;
+    }
+    std::printf("[TIME] Loading Graph Time: %.3f s\n", st.load_ms / 1e3);
+    std::printf("[TIME] Mining Time: %.3f s\n", st.mine_ms / 1e3);
+    std::printf("[TIME] Total Elapsed Time: %.3f s\n", (st.load_ms + st.mine_ms) / 1e3);
+    std::printf("[INFO] # Frequent Patterns: %llu\n", (unsigned long long)st.frequent);
+    std::printf("[INFO] # Support Evaluations: %llu (%.0f /s)\n", (unsigned long long)st.evaluations,
+                st.mine_ms > 0 ? st.evaluations / (st.mine_ms / 1e3) : 0.0);
+    std::printf("[INFO] # Searches: %llu, # Chunk steps: %llu, decided by filters: %llu, engine calls: %llu\n",
+                (unsigned long long)st.searches, (unsigned long long)st.steps, (unsigned long long)st.by_filter,
+                (unsigned long long)st.engine_calls);
+    std::printf("[TIME] Device: init %.3f ms (%llu), refine %.3f ms (%llu), search %.3f ms (%llu), host extend %.3f ms\n",
+                st.init_ms, (unsigned long long)st.init_launches, st.refine_ms, (unsigned long long)st.refine_launches,
+                st.search_ms, (unsigned long long)st.search_launches, st.extend_ms);
+    tfsm_graph_free(g);
+    return 0;
+}

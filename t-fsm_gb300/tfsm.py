@@ -1,0 +1,237 @@
+"""ctypes binding of the C ABI in include/tfsm.h (libtfsm_gb300.so in this directory).
+
+The library is the product path: there is no Python or CPU fallback.  Loading fails loudly when
+the shared library has not been built (run t-fsm_gb300/build.py) and every call that fails raises
+TfsmError with the library's message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from pathlib import Path
+from typing import Iterable, Sequence
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libtfsm_gb300.so"
+
+TFSM_OK = 0
+TFSM_ERR_ARG = 1
+TFSM_ERR_IO = 2
+TFSM_ERR_FORMAT = 3
+TFSM_ERR_PATTERN = 4
+TFSM_ERR_LIMIT = 5
+TFSM_ERR_NO_DEVICE = 9
+TFSM_ERR_CUDA = 10
+TFSM_ERR_INTERNAL = 11
+MAX_PATTERN_VERTICES = 16
+
+FLAG_EXACT = 1
+FLAG_PLAIN = 2
+FLAG_NO_SPLIT = 4
+
+EXPORTED = (
+    "tfsm_graph_load",
+    "tfsm_graph_from_edges",
+    "tfsm_graph_free",
+    "tfsm_graph_info",
+    "tfsm_evaluate_support",
+    "tfsm_evaluate_batch",
+    "tfsm_mine",
+    "tfsm_last_error",
+)
+
+
+class TfsmError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"tfsm error {code}: {msg}")
+        self.code = code
+
+
+class DfsCode(C.Structure):
+    _fields_ = [("from_", C.c_int32), ("to", C.c_int32), ("from_label", C.c_int32), ("edge_label", C.c_int32),
+                ("to_label", C.c_int32)]
+
+
+class PatternC(C.Structure):
+    _fields_ = [("n_codes", C.c_int32), ("codes", C.POINTER(DfsCode))]
+
+
+class ResultC(C.Structure):
+    _fields_ = [("status", C.c_int32), ("frequent", C.c_int32), ("n_vertices", C.c_int32),
+                ("decided_by_filter", C.c_int32), ("support", C.c_uint32),
+                ("mni", C.c_uint32 * MAX_PATTERN_VERTICES), ("searches", C.c_uint64), ("steps", C.c_uint64)]
+
+
+class GraphInfoC(C.Structure):
+    _fields_ = [("n_vertices", C.c_uint32), ("n_edges", C.c_uint64), ("n_frequent_vertex_labels", C.c_uint32),
+                ("n_frequent_edge_labels", C.c_uint32), ("n_frequent_edge_patterns", C.c_uint32),
+                ("max_degree", C.c_uint32), ("device_bytes", C.c_uint64), ("load_ms", C.c_double)]
+
+
+class MineStatsC(C.Structure):
+    _fields_ = [("load_ms", C.c_double), ("mine_ms", C.c_double), ("extend_ms", C.c_double),
+                ("init_ms", C.c_double), ("refine_ms", C.c_double), ("search_ms", C.c_double),
+                ("init_launches", C.c_uint64), ("refine_launches", C.c_uint64), ("search_launches", C.c_uint64),
+                ("init_words", C.c_uint64), ("refine_words", C.c_uint64),
+                ("evaluations", C.c_uint64), ("frequent", C.c_uint64), ("searches", C.c_uint64),
+                ("steps", C.c_uint64), ("by_filter", C.c_uint64), ("engine_calls", C.c_uint64),
+                ("levels", C.c_int32)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The loaded C library (raises when it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise FileNotFoundError(f"{LIB_PATH} is missing: build it with t-fsm_gb300/build.py")
+        L = C.CDLL(str(LIB_PATH))
+        L.tfsm_graph_load.argtypes = [C.c_char_p, C.c_int32, C.POINTER(C.c_void_p)]
+        L.tfsm_graph_from_edges.argtypes = [C.c_uint32, C.POINTER(C.c_int32), C.c_uint64, C.POINTER(C.c_uint32),
+                                            C.POINTER(C.c_uint32), C.POINTER(C.c_int32), C.c_int32,
+                                            C.POINTER(C.c_void_p)]
+        L.tfsm_graph_free.argtypes = [C.c_void_p]
+        L.tfsm_graph_free.restype = None
+        L.tfsm_graph_info.argtypes = [C.c_void_p, C.POINTER(GraphInfoC)]
+        L.tfsm_evaluate_support.argtypes = [C.c_void_p, C.POINTER(PatternC), C.c_int32, C.c_uint32,
+                                            C.POINTER(ResultC)]
+        L.tfsm_evaluate_batch.argtypes = [C.c_void_p, C.POINTER(PatternC), C.c_int32, C.c_int32, C.c_uint32,
+                                          C.POINTER(ResultC)]
+        L.tfsm_mine.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_uint32, C.c_char_p, C.POINTER(MineStatsC)]
+        L.tfsm_last_error.argtypes = []
+        L.tfsm_last_error.restype = C.c_char_p
+        for f in EXPORTED:
+            if f not in ("tfsm_graph_free", "tfsm_last_error"):
+                getattr(L, f).restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _check(rc: int) -> None:
+    if rc != TFSM_OK:
+        raise TfsmError(rc, lib().tfsm_last_error().decode(errors="replace"))
+
+
+Code = tuple  # (from, to, from_label, edge_label, to_label)
+
+
+def parse_key(key: str) -> list[Code]:
+    """'0,1,3,1,4 1,2,4,1,4' -> [(0,1,3,1,4), (1,2,4,1,4)]"""
+    return [tuple(int(x) for x in tok.split(",")) for tok in key.split()]
+
+
+def make_key(codes: Sequence[Code]) -> str:
+    return " ".join(",".join(str(x) for x in c) for c in codes)
+
+
+@dataclass
+class Result:
+    status: int
+    frequent: bool
+    support: int
+    mni: list
+    decided_by_filter: bool
+    searches: int
+    steps: int
+
+
+class Graph:
+    """A pruned data graph resident on the GPU (tfsm_graph)."""
+
+    def __init__(self, handle: C.c_void_p, tau: int):
+        self._h = handle
+        self.tau = tau
+
+    @classmethod
+    def load(cls, path: str | Path, tau: int) -> "Graph":
+        h = C.c_void_p()
+        _check(lib().tfsm_graph_load(str(path).encode(), int(tau), C.byref(h)))
+        return cls(h, tau)
+
+    @classmethod
+    def from_edges(cls, vlabels, src, dst, elabels, tau: int) -> "Graph":
+        import numpy as np
+
+        vl = np.ascontiguousarray(vlabels, dtype=np.int32)
+        s = np.ascontiguousarray(src, dtype=np.uint32)
+        d = np.ascontiguousarray(dst, dtype=np.uint32)
+        el = np.ascontiguousarray(elabels, dtype=np.int32)
+        h = C.c_void_p()
+        _check(lib().tfsm_graph_from_edges(
+            len(vl), vl.ctypes.data_as(C.POINTER(C.c_int32)), len(s), s.ctypes.data_as(C.POINTER(C.c_uint32)),
+            d.ctypes.data_as(C.POINTER(C.c_uint32)), el.ctypes.data_as(C.POINTER(C.c_int32)), int(tau),
+            C.byref(h)))
+        return cls(h, tau)
+
+    def close(self) -> None:
+        if self._h:
+            lib().tfsm_graph_free(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> dict:
+        gi = GraphInfoC()
+        _check(lib().tfsm_graph_info(self._h, C.byref(gi)))
+        return {f: getattr(gi, f) for f, _ in GraphInfoC._fields_}
+
+    def evaluate(self, patterns: Iterable[Sequence[Code]], tau: int | None = None, flags: int = 0) -> list[Result]:
+        pats = [list(p) for p in patterns]
+        n = len(pats)
+        keep = []
+        arr = (PatternC * max(n, 1))()
+        for i, p in enumerate(pats):
+            codes = (DfsCode * max(len(p), 1))(*[DfsCode(*c) for c in p])
+            keep.append(codes)
+            arr[i].n_codes = len(p)
+            arr[i].codes = C.cast(codes, C.POINTER(DfsCode))
+        res = (ResultC * max(n, 1))()
+        rc = lib().tfsm_evaluate_batch(self._h, arr, n, int(self.tau if tau is None else tau), int(flags), res)
+        out = [Result(r.status, bool(r.frequent), r.support, list(r.mni[: r.n_vertices]), bool(r.decided_by_filter),
+                      r.searches, r.steps) for r in res[:n]]
+        if rc != TFSM_OK and all(r.status != TFSM_OK for r in out):
+            _check(rc)
+        return out
+
+    def mine(self, max_nodes: int = -1, flags: int = 0, results_path: str | Path | None = None,
+             tau: int | None = None) -> dict:
+        st = MineStatsC()
+        p = str(results_path).encode() if results_path else None
+        _check(lib().tfsm_mine(self._h, int(self.tau if tau is None else tau), int(max_nodes), int(flags), p,
+                               C.byref(st)))
+        return {f: getattr(st, f) for f, _ in MineStatsC._fields_}
+
+
+def read_results(path: str | Path) -> list[str]:
+    """Pattern keys of a grami_results.txt file (serial reference format), in file order."""
+    pats, cur_v, cur_e = [], [], []
+
+    def flush():
+        if cur_v:
+            pats.append(" ".join(f"{a},{b},{cur_v[a]},{l},{cur_v[b]}" for a, b, l in cur_e))
+
+    for line in Path(path).read_text().splitlines():
+        t = line.split()
+        if not t:
+            continue
+        if t[0].startswith("====="):
+            flush()
+            cur_v, cur_e = [], []
+        elif t[0] == "v":
+            cur_v.append(int(t[2]))
+        elif t[0] == "e":
+            cur_e.append((int(t[1]), int(t[2]), int(t[3])))
+    flush()
+    return pats
