@@ -74,8 +74,10 @@ typedef struct {
 typedef struct {
     double load_ms, mine_ms, extend_ms;
     double init_ms, refine_ms, search_ms;   /* device time per kernel family (CUDA events) */
-    uint64_t init_launches, refine_launches, search_launches;
+    uint64_t init_launches, refine_launches, search_launches; /* kernel launches per family */
     uint64_t init_words, refine_words;      /* bitmap words processed */
+    uint64_t search_bytes;  /* algorithmic bytes read by the search kernels (logical loads) */
+    uint64_t h2d_bytes, d2h_bytes;          /* host<->device copies made by the mining run */
     uint64_t evaluations;  /* candidate patterns evaluated (support evaluations) */
     uint64_t frequent;     /* frequent patterns, 1-edge patterns included */
     uint64_t searches, steps, by_filter, engine_calls;
@@ -83,7 +85,8 @@ typedef struct {
 } tfsm_mine_stats;
 
 /* Load a .lg graph and prune it for threshold `tau` (label frequency, edge-label frequency and
- * the frequent 1-edge pattern table), then upload it to the current CUDA device.
+ * the frequent 1-edge pattern table), then upload it to CUDA device 0, or to the device whose
+ * index the environment variable TFSM_DEVICE holds.
  * Replaces Graph::load_graph (parallel/graph.h:557-570, serial/graph.h:485-494). */
 int tfsm_graph_load(const char *path, int32_t tau, tfsm_graph **out);
 
@@ -112,6 +115,20 @@ int tfsm_evaluate_batch(tfsm_graph *g, const tfsm_pattern *patterns, int32_t n, 
  * Replaces GraMi::project (serial/grami.h:224-234) and Worker::run (parallel/worker.h:226-284). */
 int tfsm_mine(tfsm_graph *g, int32_t tau, int32_t max_nodes, uint32_t flags, const char *results_path,
               tfsm_mine_stats *stats);
+
+/* Tuning knobs of the GPU search (no counterpart in the reference, whose only knobs are the
+ * compile-time TIMEOUT_THRESHOLD / DECOMPOSE_TIME_THRESHOLD of parallel/global.h:30-33).
+ * They change speed only, never results. */
+typedef struct {
+    uint32_t step_budget;   /* 32-candidate chunks a search may evaluate before its remaining
+                               depth-1 branches are split into slices (0: never split) */
+    uint32_t split_slice;   /* depth-1 adjacency positions per slice (>= 32) */
+    uint32_t chunk_words;   /* 32-bit domain-bitmap words per search work item (>= 1) */
+    uint32_t refine_rounds; /* arc-consistency passes for patterns that need a search (>= 1) */
+} tfsm_options;
+
+int tfsm_get_options(const tfsm_graph *g, tfsm_options *opt);
+int tfsm_set_options(tfsm_graph *g, const tfsm_options *opt);
 
 /* Message of the last failing call on this thread ("" when none). */
 const char *tfsm_last_error(void);

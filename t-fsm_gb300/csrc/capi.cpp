@@ -13,6 +13,7 @@
 struct tfsm_graph {
     tfsm::LgGraph lg;
     std::unique_ptr<tfsm::GpuEngine> eng;
+    tfsm::EngineOptions opt;  // tuning knobs (tfsm_set_options)
     int tau = 0;
     double load_ms = 0;
     std::mutex mu;
@@ -97,8 +98,8 @@ void fill_result(const tfsm::EvalResult &r, int n, tfsm_result *out) {
     out->steps = r.steps;
 }
 
-tfsm::EngineOptions engine_options(uint32_t flags) {
-    tfsm::EngineOptions o;
+tfsm::EngineOptions engine_options(const tfsm_graph *g, uint32_t flags) {
+    tfsm::EngineOptions o = g->opt;
     o.exact = (flags & TFSM_FLAG_EXACT) != 0;
     if (flags & TFSM_FLAG_NO_SPLIT) o.step_budget = 0;
     return o;
@@ -195,7 +196,7 @@ int tfsm_evaluate_batch(tfsm_graph *g, const tfsm_pattern *patterns, int32_t n, 
             tfsm::Level lvl;
             std::vector<tfsm::EvalResult> res;
             std::vector<int> par(ptrs.size(), -1);
-            g->eng->evaluate(ptrs, par, nullptr, (uint32_t)std::max(tau, 0), engine_options(flags), lvl, res);
+            g->eng->evaluate(ptrs, par, nullptr, (uint32_t)std::max(tau, 0), engine_options(g, flags), lvl, res);
             for (size_t k = 0; k < ptrs.size(); ++k) fill_result(res[k], ptrs[k]->size(), &results[idx[k]]);
         }
         return first_err;
@@ -217,7 +218,7 @@ int tfsm_mine(tfsm_graph *g, int32_t tau, int32_t max_nodes, uint32_t flags, con
         opt.tau = tau;
         opt.max_nodes = max_nodes;
         opt.batched = (flags & TFSM_FLAG_PLAIN) == 0;
-        opt.engine = engine_options(flags);
+        opt.engine = engine_options(g, flags);
         std::vector<tfsm::MinedPattern> pats;
         tfsm::MineStats st;
         g->eng->reset_times();
@@ -238,6 +239,9 @@ int tfsm_mine(tfsm_graph *g, int32_t tau, int32_t max_nodes, uint32_t flags, con
             stats->search_launches = kt.search_launches;
             stats->init_words = kt.init_words;
             stats->refine_words = kt.refine_words;
+            stats->search_bytes = kt.search_bytes;
+            stats->h2d_bytes = kt.h2d_bytes;
+            stats->d2h_bytes = kt.d2h_bytes;
             stats->evaluations = st.evaluations;
             stats->frequent = st.frequent;
             stats->searches = st.searches;
@@ -246,6 +250,31 @@ int tfsm_mine(tfsm_graph *g, int32_t tau, int32_t max_nodes, uint32_t flags, con
             stats->engine_calls = st.engine_calls;
             stats->levels = st.levels;
         }
+        return TFSM_OK;
+    });
+}
+
+int tfsm_get_options(const tfsm_graph *g, tfsm_options *o) {
+    return guarded([&]() -> int {
+        if (!g || !o) return fail(TFSM_ERR_ARG, "null argument");
+        o->step_budget = g->opt.step_budget;
+        o->split_slice = g->opt.split_slice;
+        o->chunk_words = g->opt.chunk_words;
+        o->refine_rounds = g->opt.refine_rounds;
+        return TFSM_OK;
+    });
+}
+
+int tfsm_set_options(tfsm_graph *g, const tfsm_options *o) {
+    return guarded([&]() -> int {
+        if (!g || !o) return fail(TFSM_ERR_ARG, "null argument");
+        if (o->split_slice < 32 || o->chunk_words < 1 || o->refine_rounds < 1)
+            return fail(TFSM_ERR_ARG, "split_slice must be >= 32, chunk_words and refine_rounds >= 1");
+        std::lock_guard<std::mutex> lk(g->mu);
+        g->opt.step_budget = o->step_budget;
+        g->opt.split_slice = o->split_slice;
+        g->opt.chunk_words = o->chunk_words;
+        g->opt.refine_rounds = o->refine_rounds;
         return TFSM_OK;
     });
 }

@@ -63,6 +63,7 @@ struct PatStatus {
     uint32_t pad;
     unsigned long long searches;      // candidate checks started
     unsigned long long steps;         // candidate chunks evaluated by the search
+    unsigned long long bytes;         // algorithmic bytes read by the search (logical loads)
 };
 
 enum : uint32_t { kRunning = 0, kFrequent = 1, kInfrequent = 2 };

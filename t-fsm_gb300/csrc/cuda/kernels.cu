@@ -39,6 +39,18 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *__restrict__
     return lo;
 }
 
+// Same, adding 4 bytes per probed element to `bytes` (algorithmic-traffic accounting).
+__device__ __forceinline__ uint32_t lower_bound_cnt(const uint32_t *__restrict__ a, uint32_t lo, uint32_t hi,
+                                                    uint32_t x, uint32_t &bytes) {
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        bytes += 4;
+        if (__ldg(a + mid) < x) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
 __device__ __forceinline__ uint32_t find_item(const uint64_t *__restrict__ prefix, uint32_t n_items, uint64_t gw,
                                               uint32_t hint) {
     // items are visited in increasing gw order by a warp: advance from the hint when possible
@@ -226,7 +238,8 @@ __device__ __forceinline__ void load_plan(WarpPlan &P, const PatDesc &D, uint32_
 
 // Anchor of depth d: the backward neighbour whose label sub-range is the shortest.  Lane k
 // handles the k-th backward neighbour; a warp minimum picks the winner.
-__device__ __forceinline__ void setup_depth(const Graph &g, const WarpPlan &P, WarpState &S, int d, uint32_t lane) {
+__device__ __forceinline__ void setup_depth(const Graph &g, const WarpPlan &P, WarpState &S, int d, uint32_t lane,
+                                            uint32_t &bytes) {
     const int w = P.order[d];
     const uint32_t bnm = P.bn[d];
     const int nb = __popc(bnm);
@@ -239,8 +252,9 @@ __device__ __forceinline__ void setup_depth(const Graph &g, const WarpPlan &P, W
         b = __ffs(m) - 1;
         const uint32_t y = S.emb[b];
         const uint32_t rb = __ldg(g.row_off + y), re = __ldg(g.row_off + y + 1);
-        lo = lower_bound_u32(g.col, rb, re, P.lstart[w]);
-        hi = lower_bound_u32(g.col, lo, re, P.lend[w]);
+        bytes += 8;
+        lo = lower_bound_cnt(g.col, rb, re, P.lstart[w], bytes);
+        hi = lower_bound_cnt(g.col, lo, re, P.lend[w], bytes);
         key = ((unsigned long long)(hi - lo) << 32) | lane;
     }
 #pragma unroll
@@ -264,13 +278,15 @@ __device__ __forceinline__ void setup_depth(const Graph &g, const WarpPlan &P, W
 // Is adjacency position `idx` of the depth-d anchor a valid extension?  (one lane, one position)
 __device__ __forceinline__ bool check_candidate(const Graph &g, const WarpPlan &P, const WarpState &S,
                                                 const uint32_t *__restrict__ dom, int d, uint32_t idx,
-                                                uint32_t &x_out) {
+                                                uint32_t &x_out, uint32_t &bytes) {
     const int w = P.order[d];
     const int a = S.anchor[d];
     const uint32_t x = __ldg(g.col + idx);
     x_out = x;
+    bytes += 5;  // neighbour id + edge label
     if (__ldg(g.elab + idx) != P.el[w][a]) return false;
     const uint32_t xl = x - P.lstart[w];
+    bytes += 4;  // domain bitmap word
     if (!((__ldg(dom + P.off[w] + (xl >> 5)) >> (xl & 31)) & 1u)) return false;
     for (int k = 0; k < d; ++k)
         if (S.emb[P.order[k]] == x) return false;
@@ -280,10 +296,12 @@ __device__ __forceinline__ bool check_candidate(const Graph &g, const WarpPlan &
         others &= others - 1;
         const uint32_t y = S.emb[b];
         const uint32_t re = __ldg(g.row_off + y + 1);
-        uint32_t pos = lower_bound_u32(g.col, __ldg(g.row_off + y), re, x);
+        bytes += 8;
+        uint32_t pos = lower_bound_cnt(g.col, __ldg(g.row_off + y), re, x, bytes);
         bool hit = false;
         const uint8_t want = P.el[w][b];
         while (pos < re && __ldg(g.col + pos) == x) {  // parallel edges: any with the right label
+            bytes += 5;
             if (__ldg(g.elab + pos) == want) {
                 hit = true;
                 break;
@@ -299,9 +317,10 @@ __device__ __forceinline__ bool check_candidate(const Graph &g, const WarpPlan &
 // [lo1, hi1) of its anchor list when `slice` is set.  Returns kAbort once `budget` chunk
 // evaluations are exceeded (budget 0: unlimited).
 __device__ int dfs(const Graph &g, const WarpPlan &P, WarpState &S, const uint32_t *__restrict__ dom, uint32_t lane,
-                   bool slice, uint32_t lo1, uint32_t hi1, uint32_t budget, uint32_t &steps, int &abort_depth) {
+                   bool slice, uint32_t lo1, uint32_t hi1, uint32_t budget, uint32_t &steps, int &abort_depth,
+                   uint32_t &bytes) {
     const int n = P.n;
-    setup_depth(g, P, S, 1, lane);
+    setup_depth(g, P, S, 1, lane, bytes);
     if (slice) {
         if (lane == 0) {
             S.pos[1] = lo1;
@@ -325,7 +344,7 @@ __device__ int dfs(const Graph &g, const WarpPlan &P, WarpState &S, const uint32
             }
             const uint32_t idx = pos + lane;
             uint32_t x = 0;
-            const bool ok = idx < end && check_candidate(g, P, S, dom, d, idx, x);
+            const bool ok = idx < end && check_candidate(g, P, S, dom, d, idx, x, bytes);
             const uint32_t bal = __ballot_sync(0xffffffffu, ok);
             ++steps;
             if (d == n - 1) {
@@ -352,8 +371,9 @@ __device__ int dfs(const Graph &g, const WarpPlan &P, WarpState &S, const uint32
             S.emb[P.order[d]] = __ldg(g.col + S.base[d] + i);
         }
         __syncwarp();
+        bytes += 4;  // re-read of the chosen neighbour id
         ++d;
-        setup_depth(g, P, S, d, lane);
+        setup_depth(g, P, S, d, lane, bytes);
     }
 }
 
@@ -453,7 +473,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
         const int u = item.u;
         load_plan(P, descs[p], p, u, lane);
         PatStatus &ps = st[p];
-        unsigned long long n_search = 0, n_steps = 0;
+        unsigned long long n_search = 0, n_steps = 0, n_bytes = 0;
         bool stop = false;
         for (uint32_t word = item.word_lo; word < item.word_hi && !stop; ++word) {
             if (pattern_stops(ps, u, exact)) break;
@@ -470,10 +490,10 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
                 const uint32_t v = P.lstart[u] + word * 32 + b;
                 if (lane == 0) S.emb[u] = v;
                 __syncwarp();
-                uint32_t steps = 0;
+                uint32_t steps = 0, bytes = 12;  // + domain, found and failed words of v
                 int adepth = 0;
                 ++n_search;
-                int r = dfs(g, P, S, dom, lane, false, 0, 0, prm.step_budget, steps, adepth);
+                int r = dfs(g, P, S, dom, lane, false, 0, 0, prm.step_budget, steps, adepth, bytes);
                 if (r == kAbort) {
                     // Hub splitting: cut the unexplored depth-1 range into slices for k_split.  An
                     // abort at depth 1 has fully explored every position before pos[1]; deeper, the
@@ -514,14 +534,16 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
                             splits[t0 + k] = t;
                         }
                         n_steps += steps;
+                        n_bytes += __reduce_add_sync(0xffffffffu, bytes);
                         continue;  // decided later by the slices
                     }
                     // buffers full: finish this task here without a budget
                     if (lane == 0) S.emb[u] = v;
                     __syncwarp();
-                    r = dfs(g, P, S, dom, lane, false, 0, 0, 0, steps, adepth);
+                    r = dfs(g, P, S, dom, lane, false, 0, 0, 0, steps, adepth, bytes);
                 }
                 n_steps += steps;
+                n_bytes += __reduce_add_sync(0xffffffffu, bytes);
                 if (r == kFound) mark_found(P, S, ps, found, prm.tau, exact, lane);
                 else mark_failed(P, ps, failed, u, v, prm.tau, exact, lane);
             }
@@ -529,6 +551,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
         if (lane == 0 && n_search) {
             atomicAdd(&ps.searches, n_search);
             atomicAdd(&ps.steps, n_steps);
+            atomicAdd(&ps.bytes, n_bytes);
         }
     }
 }
@@ -569,11 +592,15 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_split(Graph g, const PatD
         if (!pattern_stops(ps, u, exact) && !(__ldcg(found + o) & bit)) {
             if (lane == 0) S.emb[u] = t.v;
             __syncwarp();
-            uint32_t steps = 0;
+            uint32_t steps = 0, bytes = 12;
             int adepth = 0;
-            const int r = dfs(g, P, S, dom, lane, true, t.lo, t.hi, 0, steps, adepth);
+            const int r = dfs(g, P, S, dom, lane, true, t.lo, t.hi, 0, steps, adepth, bytes);
             if (r == kFound) mark_found(P, S, ps, found, prm.tau, exact, lane);
-            if (lane == 0) atomicAdd(&ps.steps, (unsigned long long)steps);
+            const unsigned long long wb = __reduce_add_sync(0xffffffffu, bytes);
+            if (lane == 0) {
+                atomicAdd(&ps.steps, (unsigned long long)steps);
+                atomicAdd(&ps.bytes, wb);
+            }
             searched = true;
         }
         if (lane == 0) {
@@ -646,7 +673,8 @@ cudaError_t launch_refine(const Graph &g, const PatDesc *descs, PatStatus *st, c
 
 cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchItem *items,
                           const SearchParams &prm, uint32_t *counters, const uint32_t *dom, uint32_t *found,
-                          uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s) {
+                          uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s, int *launches) {
+    *launches = 0;
     if (prm.n_items == 0) return cudaSuccess;
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search, kSearchWarps * 32, 0);
@@ -657,12 +685,14 @@ cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, c
     k_search<<<(unsigned)blocks, kSearchWarps * 32, 0, s>>>(g, descs, st, items, prm, counters, dom, found, failed,
                                                              splits, groups);
     cudaError_t e = cudaGetLastError();
+    *launches = 1;
     if (e != cudaSuccess || prm.step_budget == 0) return e;
     int per_sm2 = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_split, kSearchWarps * 32, 0);
     if (per_sm2 <= 0) per_sm2 = 1;
     k_split<<<(unsigned)(num_sms() * per_sm2), kSearchWarps * 32, 0, s>>>(g, descs, st, prm, counters, dom, found,
                                                                           failed, splits, groups);
+    *launches = 2;
     return cudaGetLastError();
 }
 

@@ -23,7 +23,7 @@ cudaError_t launch_refine(const Graph &g, const PatDesc *descs, PatStatus *st, c
 // slices it produced.  `counters` (4 x u32) must be zero on entry.
 cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchItem *items,
                           const SearchParams &prm, uint32_t *counters, const uint32_t *dom, uint32_t *found,
-                          uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s);
+                          uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s, int *launches);
 
 }  // namespace dev
 }  // namespace tfsm

@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <numeric>
@@ -93,6 +94,7 @@ struct GpuEngine::Impl {
 
 GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     auto t0 = std::chrono::steady_clock::now();
+    if (const char *env = std::getenv("TFSM_DEVICE")) device = std::atoi(env);
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device)
         throw EngineError(9, "no CUDA device available for the GPU engine");
@@ -276,6 +278,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     I.status.ensure(P);
     I.hstatus.assign(P, PatStatus());
     TFSM_CK(cudaMemcpyAsync(L.descs.p, L.hdescs.data(), P * sizeof(PatDesc), cudaMemcpyHostToDevice, I.stream));
+    times_.h2d_bytes += P * sizeof(PatDesc);
     TFSM_CK(cudaMemsetAsync(I.status.p, 0, P * sizeof(PatStatus), I.stream));
 
     const uint32_t *pdom = prev ? prev->impl->dom.p : nullptr;
@@ -300,12 +303,14 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         if (!item_pu.empty()) {
             TFSM_CK(cudaMemcpyAsync(I.item_pu.p, item_pu.data(), item_pu.size() * 4, cudaMemcpyHostToDevice, I.stream));
             TFSM_CK(cudaMemcpyAsync(I.prefix.p, prefix.data(), prefix.size() * 8, cudaMemcpyHostToDevice, I.stream));
+            times_.h2d_bytes += item_pu.size() * 4 + prefix.size() * 8;
         }
     };
     auto read_status = [&]() {
         TFSM_CK(cudaMemcpyAsync(I.hstatus.data(), I.status.p, P * sizeof(PatStatus), cudaMemcpyDeviceToHost,
                                 I.stream));
         TFSM_CK(cudaStreamSynchronize(I.stream));
+        times_.d2h_bytes += P * sizeof(PatStatus);
     };
     auto time_since_ev0 = [&]() -> double {
         TFSM_CK(cudaEventRecord(I.ev1, I.stream));
@@ -349,6 +354,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         for (size_t p = 0; p < P; ++p) I.hstatus[p].changed = 0;
         TFSM_CK(cudaMemcpyAsync(I.status.p, I.hstatus.data(), P * sizeof(PatStatus), cudaMemcpyHostToDevice,
                                 I.stream));
+        times_.h2d_bytes += P * sizeof(PatStatus);
         build_items(active);
         TFSM_CK(cudaEventRecord(I.ev0, I.stream));
         TFSM_CK(dev::launch_refine(I.g, L.descs.p, I.status.p, I.item_pu.p, I.prefix.p, (uint32_t)item_pu.size(),
@@ -392,6 +398,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     }
     if (!any_search) return;
     TFSM_CK(cudaMemcpyAsync(L.descs.p, L.hdescs.data(), P * sizeof(PatDesc), cudaMemcpyHostToDevice, I.stream));
+    times_.h2d_bytes += P * sizeof(PatDesc);
 
     // ---- search items, interleaved across patterns and representatives ----
     std::vector<dev::SearchItem> items;
@@ -427,6 +434,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     I.items.ensure(items.size());
     TFSM_CK(cudaMemcpyAsync(I.items.p, items.data(), items.size() * sizeof(dev::SearchItem), cudaMemcpyHostToDevice,
                             I.stream));
+    times_.h2d_bytes += items.size() * sizeof(dev::SearchItem);
     TFSM_CK(cudaMemsetAsync(I.counters.p, 0, 4 * sizeof(uint32_t), I.stream));
     dev::SearchParams prm;
     prm.tau = tau;
@@ -437,10 +445,12 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     prm.split_cap = (uint32_t)I.splits.n;
     prm.group_cap = (uint32_t)I.groups.n;
     TFSM_CK(cudaEventRecord(I.ev0, I.stream));
+    int launches = 0;
     TFSM_CK(dev::launch_search(I.g, L.descs.p, I.status.p, I.items.p, prm, I.counters.p, L.dom.p, L.found.p,
-                               L.failed.p, I.splits.p, I.groups.p, I.stream));
+                               L.failed.p, I.splits.p, I.groups.p, I.stream, &launches));
     times_.search_ms += time_since_ev0();
-    times_.search_launches++;
+    times_.search_launches += (uint64_t)launches;
+    times_.search_calls++;
     read_status();
 
     for (size_t p = 0; p < P; ++p) {
@@ -450,6 +460,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         EvalResult &r = res[p];
         r.searches = s.searches;
         r.steps = s.steps;
+        times_.search_bytes += s.bytes;
         uint32_t mn = UINT32_MAX;
         bool all_reps = true;
         for (int u = 0; u < D.n; ++u) {

@@ -36,8 +36,11 @@ struct EngineOptions {
 
 struct KernelTimes {                   // accumulated device time (CUDA events), milliseconds
     double init_ms = 0, refine_ms = 0, search_ms = 0;
-    uint64_t init_launches = 0, refine_launches = 0, search_launches = 0;
+    uint64_t init_launches = 0, refine_launches = 0, search_launches = 0;  // kernel launches
+    uint64_t search_calls = 0;         // search phases (k_search, plus k_split when splitting)
     uint64_t init_words = 0, refine_words = 0;  // bitmap words processed
+    uint64_t search_bytes = 0;         // algorithmic bytes read by the search kernels
+    uint64_t h2d_bytes = 0, d2h_bytes = 0;      // host<->device copies of the evaluations
 };
 
 // Device memory of one evaluated batch; kept while the batch's patterns are parents.

@@ -37,6 +37,8 @@ EXPORTED = (
     "tfsm_evaluate_support",
     "tfsm_evaluate_batch",
     "tfsm_mine",
+    "tfsm_get_options",
+    "tfsm_set_options",
     "tfsm_last_error",
 )
 
@@ -68,11 +70,17 @@ class GraphInfoC(C.Structure):
                 ("max_degree", C.c_uint32), ("device_bytes", C.c_uint64), ("load_ms", C.c_double)]
 
 
+class OptionsC(C.Structure):
+    _fields_ = [("step_budget", C.c_uint32), ("split_slice", C.c_uint32), ("chunk_words", C.c_uint32),
+                ("refine_rounds", C.c_uint32)]
+
+
 class MineStatsC(C.Structure):
     _fields_ = [("load_ms", C.c_double), ("mine_ms", C.c_double), ("extend_ms", C.c_double),
                 ("init_ms", C.c_double), ("refine_ms", C.c_double), ("search_ms", C.c_double),
                 ("init_launches", C.c_uint64), ("refine_launches", C.c_uint64), ("search_launches", C.c_uint64),
-                ("init_words", C.c_uint64), ("refine_words", C.c_uint64),
+                ("init_words", C.c_uint64), ("refine_words", C.c_uint64), ("search_bytes", C.c_uint64),
+                ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
                 ("evaluations", C.c_uint64), ("frequent", C.c_uint64), ("searches", C.c_uint64),
                 ("steps", C.c_uint64), ("by_filter", C.c_uint64), ("engine_calls", C.c_uint64),
                 ("levels", C.c_int32)]
@@ -100,6 +108,8 @@ def lib() -> C.CDLL:
         L.tfsm_evaluate_batch.argtypes = [C.c_void_p, C.POINTER(PatternC), C.c_int32, C.c_int32, C.c_uint32,
                                           C.POINTER(ResultC)]
         L.tfsm_mine.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_uint32, C.c_char_p, C.POINTER(MineStatsC)]
+        L.tfsm_get_options.argtypes = [C.c_void_p, C.POINTER(OptionsC)]
+        L.tfsm_set_options.argtypes = [C.c_void_p, C.POINTER(OptionsC)]
         L.tfsm_last_error.argtypes = []
         L.tfsm_last_error.restype = C.c_char_p
         for f in EXPORTED:
@@ -204,6 +214,17 @@ class Graph:
         if rc != TFSM_OK and all(r.status != TFSM_OK for r in out):
             _check(rc)
         return out
+
+    def options(self) -> dict:
+        o = OptionsC()
+        _check(lib().tfsm_get_options(self._h, C.byref(o)))
+        return {f: getattr(o, f) for f, _ in OptionsC._fields_}
+
+    def set_options(self, **kw) -> None:
+        cur = self.options()
+        cur.update(kw)
+        o = OptionsC(**cur)
+        _check(lib().tfsm_set_options(self._h, C.byref(o)))
 
     def mine(self, max_nodes: int = -1, flags: int = 0, results_path: str | Path | None = None,
              tau: int | None = None) -> dict:

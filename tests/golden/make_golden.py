@@ -1,0 +1,198 @@
+"""Generate the golden fixtures of the parity tests from the reference T-FSM itself.
+
+Runs only where the reference sources exist (they are read from /root/reference by
+oracle/Makefile): `make -C oracle ref harness port` builds
+  oracle/_ref/serial_run    the reference serial miner   (serial/Makefile flags)
+  oracle/_ref/parallel_run  the reference parallel miner (parallel/Makefile flags)
+  oracle/_ref/mni_harness   exact MNI domains from the reference's GMatchEngine
+  oracle/tfsm_port          the CPU restatement (used here only to list candidate patterns)
+
+For every case it writes, next to this script:
+  <case>.patterns.txt  frequent patterns (DFS-code keys, sorted) from the serial build; the
+                       parallel build must agree, else the script stops
+  <case>.mni.txt       "<key> | c0 c1 ..." exact per-vertex MNI domain sizes from the harness, for
+                       frequent and infrequent candidates alike
+and cases.json with the graph recipe (generator arguments or a committed graph file), tau,
+maxNodes and the graph checksum.
+
+usage: python tests/golden/make_golden.py [case ...]
+"""
+from __future__ import annotations
+
+import json
+import os
+import random
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+REF = ROOT / "oracle" / "_ref"
+GEN = ROOT / "t-fsm_gb300" / "bin" / "gen_lg"
+PORT = ROOT / "oracle" / "tfsm_port"
+sys.path.insert(0, str(ROOT / "tests"))
+from golden_io import read_parallel_stdout, read_results, graph_checksum  # noqa: E402
+
+# Synthetic graphs of the benchmark configurations (Chung-Lu degrees, Zipf labels).
+GEN_CASES = {
+    "cfg1": dict(gen=dict(n=5000, mean=8, gamma=2.5, max_degree=500, labels=10, zipf=1.0, elabels=1, seed=0),
+                 tau=200, max_nodes=4, mni="all"),
+    "el3": dict(gen=dict(n=3000, mean=8, gamma=2.3, max_degree=300, labels=5, zipf=1.0, elabels=3, seed=7),
+                tau=60, max_nodes=4, mni="every5"),
+    "cfg2_t9000": dict(gen=dict(n=100000, mean=22, gamma=2.2, max_degree=1400, labels=29, zipf=1.2, elabels=1,
+                                seed=1), tau=9000, max_nodes=5, mni="all"),
+    "cfg2_t7000": dict(gen=dict(n=100000, mean=22, gamma=2.2, max_degree=1400, labels=29, zipf=1.2, elabels=1,
+                                seed=1), tau=7000, max_nodes=5, mni="none", serial=False),
+}
+
+# Small hand-made graphs for edge cases, written by make_small_graphs().
+FILE_CASES = {
+    "clique": dict(file="graphs/clique.lg", tau=3, max_nodes=5, mni="all"),
+    "star_hub": dict(file="graphs/star_hub.lg", tau=4, max_nodes=4, mni="all"),
+    "quirk_elabels": dict(file="graphs/quirk_elabels.lg", tau=3, max_nodes=5, mni="all"),
+    "no_edges": dict(file="graphs/no_edges.lg", tau=1, max_nodes=4, mni="all"),
+    "no_frequent": dict(file="graphs/no_frequent.lg", tau=50, max_nodes=4, mni="all"),
+    "tau1_small": dict(file="graphs/tau1_small.lg", tau=1, max_nodes=4, mni="all"),
+}
+
+
+def write_lg(path: Path, labels: list[int], edges: list[tuple[int, int, int]]) -> None:
+    lines = [f"t {len(labels)} {len(edges)}"]
+    deg = [0] * len(labels)
+    for a, b, _ in edges:
+        deg[a] += 1
+        deg[b] += 1
+    lines += [f"v {i} {l} {deg[i]}" for i, l in enumerate(labels)]
+    lines += [f"e {a} {b} {l}" for a, b, l in edges]
+    path.write_text("\n".join(lines) + "\n")
+
+
+def make_small_graphs() -> None:
+    g = HERE / "graphs"
+    g.mkdir(exist_ok=True)
+    rnd = random.Random(20240611)
+    # clique: four disjoint K5's with labels 0/1 -> many automorphisms and backward edges
+    labels, edges = [], []
+    for c in range(4):
+        base = len(labels)
+        labels += [0, 0, 1, 1, 0]
+        edges += [(base + i, base + j, 1) for i in range(5) for j in range(i + 1, 5)]
+    write_lg(g / "clique.lg", labels, edges)
+    # star_hub: two hubs joined to many leaves, leaves form a sparse ring -> hub-rooted searches
+    labels = [0, 0] + [1 + (i % 2) for i in range(200)]
+    edges = []
+    for i in range(200):
+        edges.append((0, 2 + i, 1))
+        if i % 3 == 0:
+            edges.append((1, 2 + i, 1))
+        if i + 1 < 200 and i % 4 != 3:
+            edges.append((2 + i, 3 + i, 1))
+    edges.append((0, 1, 1))
+    write_lg(g / "star_hub.lg", labels, edges)
+    # quirk_elabels: small random graph with 3 edge labels and 3 vertex labels, dense enough for
+    # 4-5 vertex patterns with mixed edge labels (exercises the canonical-check ordering)
+    n = 40
+    labels = [rnd.randrange(3) for _ in range(n)]
+    es = set()
+    while len(es) < 110:
+        a, b = rnd.randrange(n), rnd.randrange(n)
+        if a != b:
+            es.add((min(a, b), max(a, b)))
+    edges = [(a, b, 1 + rnd.randrange(3)) for a, b in sorted(es)]
+    write_lg(g / "quirk_elabels.lg", labels, edges)
+    # no_edges: labelled vertices only
+    write_lg(g / "no_edges.lg", [i % 3 for i in range(30)], [])
+    # no_frequent: every label rarer than tau=50
+    n = 60
+    labels = [i % 6 for i in range(n)]
+    edges = [(i, (i * 7 + 3) % n, 1) for i in range(n) if i < (i * 7 + 3) % n]
+    write_lg(g / "no_frequent.lg", labels, edges)
+    # tau1_small: tau = 1, every pattern present at least once is frequent
+    labels = [0, 1, 0, 1, 2, 0, 2]
+    edges = [(0, 1, 1), (1, 2, 1), (2, 3, 1), (3, 0, 1), (0, 4, 1), (4, 5, 1), (5, 6, 1), (2, 6, 1)]
+    write_lg(g / "tau1_small.lg", labels, edges)
+
+
+def gen_args(p: dict) -> list[str]:
+    return ["--n", str(p["n"]), "--mean", str(p["mean"]), "--gamma", str(p["gamma"]), "--max-degree",
+            str(p["max_degree"]), "--labels", str(p["labels"]), "--zipf", str(p["zipf"]), "--elabels",
+            str(p["elabels"]), "--seed", str(p["seed"])]
+
+
+def run(cmd, cwd=None, timeout=None) -> subprocess.CompletedProcess:
+    r = subprocess.run([str(c) for c in cmd], cwd=cwd, capture_output=True, text=True, timeout=timeout)
+    if r.returncode != 0:
+        raise RuntimeError(f"{cmd} failed: {r.stdout[-2000:]} {r.stderr[-2000:]}")
+    return r
+
+
+def main(names: list[str]) -> None:
+    for tool in (REF / "serial_run", REF / "parallel_run", REF / "mni_harness", PORT, GEN):
+        if not tool.exists():
+            sys.exit(f"missing {tool}: run `make -C oracle ref harness port` and t-fsm_gb300/build.py first")
+    make_small_graphs()
+    cases_path = HERE / "cases.json"
+    cases = json.loads(cases_path.read_text()) if cases_path.exists() else {}
+    todo = {**GEN_CASES, **FILE_CASES}
+    for name in names or list(todo):
+        spec = todo[name]
+        with tempfile.TemporaryDirectory() as tmp:
+            tmp = Path(tmp)
+            if "gen" in spec:
+                graph = tmp / "g.lg"
+                run([GEN, "--out", graph, *gen_args(spec["gen"])])
+            else:
+                graph = HERE / spec["file"]
+            tau, mn = spec["tau"], spec["max_nodes"]
+            ser = None
+            if spec.get("serial", True):
+                sdir = tmp / "serial"
+                sdir.mkdir()
+                run([REF / "serial_run", "-file", graph, "-freq", tau, "-maxNodes", mn], cwd=sdir)
+                ser = sorted(read_results(sdir / "grami_results.txt"))
+            # one thread: the parallel build prints patterns from several threads without a lock,
+            # which can garble its stdout; the task-based code path is the same
+            pr = run([REF / "parallel_run", "-file", graph, "-freq", tau, "-thread", 1, "-maxNodes", mn], cwd=tmp)
+            par = sorted(read_parallel_stdout(pr.stdout))
+            if ser is not None:
+                multi = sorted(k for k in ser if " " in k)
+                if multi != par:
+                    sys.exit(f"{name}: serial and parallel reference builds disagree")
+                pats = ser
+            else:
+                pats = par  # parallel prints multi-edge patterns only: add 1-edge ones from the port
+                port_out = tmp / "port.txt"
+                run([PORT, "-file", graph, "-freq", tau, "-maxNodes", mn, "-thread", os.cpu_count() or 4, "-out",
+                     port_out])
+                one_edge = sorted(k for k in read_results(port_out) if " " not in k)
+                pats = sorted(one_edge + par)
+            (HERE / f"{name}.patterns.txt").write_text("".join(k + "\n" for k in pats))
+            mni_lines = 0
+            if spec["mni"] != "none":
+                sup = tmp / "port.sup"
+                run([PORT, "-file", graph, "-freq", tau, "-maxNodes", mn, "-thread", os.cpu_count() or 4,
+                     "-supports", sup])
+                keys = [line.split(" | ")[0][2:] for line in sup.read_text().splitlines()]
+                if spec["mni"] == "every5":
+                    keys = keys[::5]
+                plist = tmp / "pats.txt"
+                plist.write_text("".join(k + "\n" for k in keys))
+                if keys:
+                    h = run([REF / "mni_harness", "-file", graph, "-freq", tau, "-patterns", plist], timeout=7200)
+                    lines = [ln for ln in h.stdout.splitlines() if " | " in ln]
+                else:
+                    lines = []
+                (HERE / f"{name}.mni.txt").write_text("".join(ln + "\n" for ln in lines))
+                mni_lines = len(lines)
+            rec = {"tau": tau, "max_nodes": mn, "n_patterns": len(pats), "n_mni": mni_lines,
+                   "checksum": graph_checksum(graph), "serial_checked": ser is not None}
+            rec.update({"gen": spec["gen"]} if "gen" in spec else {"file": spec["file"]})
+            cases[name] = rec
+            print(name, rec, flush=True)
+        cases_path.write_text(json.dumps(cases, indent=1, sort_keys=True) + "\n")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -1,0 +1,163 @@
+"""Parity of the CUDA path with the reference, through the C ABI (marker: gpu).
+
+* Mining: the frequent-pattern set of tfsm_mine equals the reference serial/parallel builds'
+  (tests/golden/<case>.patterns.txt), batched and plain, with and without hub splitting.
+* Supports: tfsm_evaluate_batch with TFSM_FLAG_EXACT returns, per pattern vertex, exactly the MNI
+  domain sizes the reference's own matching engine computes (tests/golden/<case>.mni.txt).
+* Lazy evaluation (early exit at tau) decides "frequent" exactly when the exact support >= tau.
+Bit-exact integers everywhere: no tolerance.
+"""
+from __future__ import annotations
+
+import subprocess
+
+import pytest
+
+from conftest import CASES, golden_mni, golden_pattern_set
+from golden_io import read_results
+
+pytestmark = pytest.mark.gpu
+
+SMALL = [n for n, c in CASES.items() if "file" in c or c["gen"]["n"] <= 5000]
+ALL = list(CASES)
+
+
+@pytest.fixture(scope="module")
+def graphs(tfsm, case_graph):
+    cache = {}
+
+    def get(case):
+        if case not in cache:
+            cache[case] = tfsm.Graph.load(case_graph(case), CASES[case]["tau"])
+        return cache[case]
+
+    yield get
+    for g in cache.values():
+        g.close()
+
+
+def mine_set(tfsm, g, case, tmp_path, flags=0):
+    out = tmp_path / f"{case}_{flags}.txt"
+    st = g.mine(max_nodes=CASES[case]["max_nodes"], flags=flags, results_path=out)
+    pats = read_results(out)
+    assert len(pats) == len(set(pats)), "a pattern was reported twice"
+    assert st["frequent"] == len(pats)
+    return set(pats), st
+
+
+@pytest.mark.parametrize("case", ALL)
+def test_mining_batched_matches_reference(tfsm, graphs, case, tmp_path):
+    pats, st = mine_set(tfsm, graphs(case), case, tmp_path)
+    assert pats == golden_pattern_set(case)
+
+
+@pytest.mark.parametrize("case", SMALL + ["cfg2_t9000"])
+def test_mining_plain_matches_reference(tfsm, graphs, case, tmp_path):
+    pats, st = mine_set(tfsm, graphs(case), case, tmp_path, flags=tfsm.FLAG_PLAIN)
+    assert pats == golden_pattern_set(case)
+    assert st["engine_calls"] == st["evaluations"]
+
+
+@pytest.mark.parametrize("case", ["cfg1", "el3", "star_hub", "clique"])
+def test_mining_with_forced_hub_splits_matches_reference(tfsm, graphs, case, tmp_path):
+    g = graphs(case)
+    saved = g.options()
+    try:
+        g.set_options(step_budget=1, split_slice=32)  # every search longer than one chunk splits
+        pats, st = mine_set(tfsm, g, case, tmp_path)
+    finally:
+        g.set_options(**saved)
+    assert pats == golden_pattern_set(case)
+
+
+@pytest.mark.parametrize("case", [n for n in ALL if golden_mni(n)])
+@pytest.mark.parametrize("flags", [0, 4])  # with and without splitting
+def test_exact_mni_matches_reference_engine(tfsm, graphs, case, flags):
+    want = golden_mni(case)
+    keys = list(want)
+    g = graphs(case)
+    res = g.evaluate([tfsm.parse_key(k) for k in keys], flags=tfsm.FLAG_EXACT | flags)
+    bad = [(k, want[k], r.mni) for k, r in zip(keys, res) if r.status != 0 or r.mni != want[k]]
+    assert not bad, f"{len(bad)} of {len(keys)} differ, e.g. {bad[:3]}"
+    for k, r in zip(keys, res):
+        assert r.support == min(want[k])
+        assert r.frequent == (min(want[k]) >= CASES[case]["tau"])
+
+
+@pytest.mark.parametrize("case", ["cfg1", "el3", "quirk_elabels", "cfg2_t9000"])
+def test_lazy_decision_matches_exact_support(tfsm, graphs, case):
+    want = golden_mni(case)
+    keys = list(want)
+    tau = CASES[case]["tau"]
+    res = g_res = graphs(case).evaluate([tfsm.parse_key(k) for k in keys])
+    for k, r in zip(keys, g_res):
+        assert r.frequent == (min(want[k]) >= tau), k
+        if r.frequent:
+            assert r.support >= tau
+    # one pattern per call (plain path) agrees with the batch
+    single = [graphs(case).evaluate([tfsm.parse_key(k)])[0] for k in keys[:40]]
+    assert [r.frequent for r in single] == [r.frequent for r in res[:40]]
+
+
+def test_forced_splits_keep_exact_supports(tfsm, graphs):
+    case = "el3"
+    want = golden_mni(case)
+    keys = list(want)[:300]
+    g = graphs(case)
+    saved = g.options()
+    try:
+        for opts in (dict(step_budget=1, split_slice=32, chunk_words=1), dict(step_budget=2, split_slice=64,
+                                                                              chunk_words=7, refine_rounds=1)):
+            g.set_options(**opts)
+            res = g.evaluate([tfsm.parse_key(k) for k in keys], flags=tfsm.FLAG_EXACT)
+            assert [r.mni for r in res] == [want[k] for k in keys]
+    finally:
+        g.set_options(**saved)
+
+
+def test_graph_from_host_arrays_equals_file_load(tfsm, case_graph, tmp_path):
+    case = "cfg1"
+    path = case_graph(case)
+    vl, src, dst, el = [], [], [], []
+    for line in path.read_text().splitlines():
+        t = line.split()
+        if t[0] == "v":
+            vl.append(int(t[2]))
+        elif t[0] == "e":
+            src.append(int(t[1]))
+            dst.append(int(t[2]))
+            el.append(int(t[3]))
+    with tfsm.Graph.from_edges(vl, src, dst, el, CASES[case]["tau"]) as g:
+        assert g.info()["n_vertices"] > 0
+        pats, _ = mine_set(tfsm, g, case, tmp_path)
+    assert pats == golden_pattern_set(case)
+
+
+def test_invalid_patterns_are_rejected(tfsm, graphs):
+    g = graphs("cfg1")
+    bad = [
+        [(0, 2, 0, 1, 0)],                               # first code must be (0,1)
+        [(0, 1, 0, 1, 0), (3, 4, 0, 1, 0)],              # disconnected
+        [(0, 1, 0, 1, 0), (1, 0, 0, 1, 0)],              # repeated edge
+        [(0, 1, 0, 1, 0), (0, 2, 5, 1, 1)],              # label of vertex 0 changes
+    ]
+    res = g.evaluate(bad)
+    assert all(r.status == tfsm.TFSM_ERR_ARG for r in res)
+    big = [(0, 1, 0, 1, 0)] + [(i, i + 1, 0, 1, 0) for i in range(1, 17)]
+    r = g.evaluate([big])[0]
+    assert r.status == tfsm.TFSM_ERR_PATTERN
+    # valid patterns in the same batch are still evaluated
+    mixed = g.evaluate([bad[0], [(0, 1, 0, 1, 0)]])
+    assert mixed[0].status == tfsm.TFSM_ERR_ARG and mixed[1].status == 0
+
+
+def test_cli_writes_reference_format(built, case_graph, tmp_path):
+    case = "cfg1"
+    c = CASES[case]
+    out = tmp_path / "grami_results.txt"
+    r = subprocess.run([str(built / "bin" / "run"), "-file", str(case_graph(case)), "-freq", str(c["tau"]),
+                        "-thread", "4", "-maxNodes", str(c["max_nodes"]), "-out", str(out)], capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "[INFO] # Frequent Patterns: %d" % len(golden_pattern_set(case)) in r.stdout
+    assert set(read_results(out)) == golden_pattern_set(case)

@@ -1,0 +1,61 @@
+"""The CPU oracle (oracle/tfsm_port) pinned against the reference's own outputs.
+
+tests/golden/ holds, per case, the frequent-pattern set of the reference serial and parallel builds
+and exact per-vertex MNI domain sizes from the reference's matching engine (made by
+tests/golden/make_golden.py).  The oracle must reproduce both exactly before it may check the
+CUDA path.
+"""
+from __future__ import annotations
+
+import subprocess
+
+import pytest
+
+from conftest import CASES, golden_mni, golden_pattern_set
+from golden_io import read_mni, read_results
+
+SMALL = [n for n, c in CASES.items() if "file" in c or c["gen"]["n"] <= 5000]
+LARGE = [n for n in CASES if n not in SMALL]
+
+
+def run_port(port, graph, case, tmp_path, exact=False, threads=8):
+    c = CASES[case]
+    out = tmp_path / f"{case}.{int(exact)}.txt"
+    sup = tmp_path / f"{case}.{int(exact)}.sup"
+    cmd = [str(port), "-file", str(graph), "-freq", str(c["tau"]), "-maxNodes", str(c["max_nodes"]), "-thread",
+           str(threads), "-out", str(out), "-supports", str(sup)]
+    if exact:
+        cmd += ["-exact", "1"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout + r.stderr
+    # supports lines are "F|I <key> | counts": drop the frequent/infrequent tag
+    return set(read_results(out)), {k[2:]: v for k, v in read_mni(sup).items()}
+
+
+@pytest.mark.parametrize("case", SMALL + LARGE)
+def test_oracle_pattern_set_matches_reference(case, port, case_graph, tmp_path):
+    pats, _ = run_port(port, case_graph(case), case, tmp_path)
+    assert pats == golden_pattern_set(case)
+
+
+@pytest.mark.parametrize("case", [n for n in SMALL + LARGE if golden_mni(n)])
+def test_oracle_exact_mni_matches_reference_engine(case, port, case_graph, tmp_path):
+    pats, mni = run_port(port, case_graph(case), case, tmp_path, exact=True)
+    want = golden_mni(case)
+    assert set(want) <= set(mni), "oracle evaluated a different candidate set"
+    bad = {k: (mni[k], v) for k, v in want.items() if mni[k] != v}
+    assert not bad, f"{len(bad)} patterns differ, e.g. {list(bad.items())[:3]}"
+    # exact mode decides frequency from exact supports: same pattern set
+    assert pats == golden_pattern_set(case)
+
+
+def test_oracle_lazy_supports_are_consistent(port, case_graph, tmp_path):
+    """Lazy evaluation stops at tau; frequent patterns' lazy counts are >= tau and <= exact."""
+    case = "cfg1"
+    tau = CASES[case]["tau"]
+    _, lazy = run_port(port, case_graph(case), case, tmp_path)
+    exact = golden_mni(case)
+    for k, v in lazy.items():
+        if k in exact and min(exact[k]) >= tau:
+            assert min(v) >= tau
+            assert all(a <= b for a, b in zip(v, exact[k]))
