@@ -106,7 +106,10 @@ int tfsm_graph_info(const tfsm_graph *g, tfsm_graph_info_t *info);
 int tfsm_evaluate_support(tfsm_graph *g, const tfsm_pattern *pattern, int32_t tau, uint32_t flags,
                           tfsm_result *out);
 
-/* Batched form: all `n` patterns are evaluated by one launch sequence. */
+/* Batched form: all `n` patterns are evaluated by one launch sequence.  Returns TFSM_OK when the
+ * batch was processed; a pattern that fails validation gets its error in results[i].status
+ * (TFSM_ERR_ARG or TFSM_ERR_PATTERN) and the others are still evaluated.  tfsm_evaluate_support
+ * returns its single pattern's status. */
 int tfsm_evaluate_batch(tfsm_graph *g, const tfsm_pattern *patterns, int32_t n, int32_t tau, uint32_t flags,
                         tfsm_result *results);
 

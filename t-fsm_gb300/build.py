@@ -17,7 +17,10 @@ from pathlib import Path
 
 PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
-BUILD = PKG / "_build"
+# TFSM_BOUNDS_CHECK=1 builds the self-checking variant (every global access of the search kernels
+# bounds-checked, first violation reported as an error) into its own object directory.
+CHECKED = os.environ.get("TFSM_BOUNDS_CHECK") == "1"
+BUILD = PKG / ("_build_checked" if CHECKED else "_build")
 BIN = PKG / "bin"
 LIB = PKG / "libtfsm_gb300.so"
 ROOT = PKG.parent
@@ -49,6 +52,11 @@ def _stale(target: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
+def _lib_is_checked() -> bool:
+    marker = PKG / "_build_checked" / "linked"
+    return LIB.exists() and marker.exists() and marker.stat().st_mtime >= LIB.stat().st_mtime - 1
+
+
 def build(verbose: bool = False) -> Path:
     cuda = _cuda_home()
     nvcc = str(cuda / "bin" / "nvcc")
@@ -64,7 +72,7 @@ def build(verbose: bool = False) -> Path:
         objs.append(obj)
         if _stale(obj, [src] + headers):
             jobs.append([nvcc, *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(CSRC),
-                         "-c", str(src), "-o", str(obj)])
+                         *(["-DTFSM_BOUNDS_CHECK"] if CHECKED else []), "-c", str(src), "-o", str(obj)])
     for src in cpp:
         obj = BUILD / (src.stem + ".o")
         objs.append(obj)
@@ -80,11 +88,16 @@ def build(verbose: bool = False) -> Path:
             if verbose:
                 print(" ".join(cmd), flush=True)
         list(ex.map(_run, jobs))
-    if _stale(LIB, objs):
+    if _stale(LIB, objs) or CHECKED != _lib_is_checked():
         cmd = [nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-Xcompiler", "-pthread"]
         if verbose:
             print(" ".join(cmd), flush=True)
         _run(cmd)
+        marker = PKG / "_build_checked" / "linked"
+        if CHECKED:
+            marker.write_text("checked build\n")
+        elif marker.exists():
+            marker.unlink()
     run_bin = BIN / "run"
     run_src = CSRC / "run_main.cpp"
     if _stale(run_bin, [run_src, LIB]):

@@ -199,14 +199,16 @@ int tfsm_evaluate_batch(tfsm_graph *g, const tfsm_pattern *patterns, int32_t n, 
             g->eng->evaluate(ptrs, par, nullptr, (uint32_t)std::max(tau, 0), engine_options(g, flags), lvl, res);
             for (size_t k = 0; k < ptrs.size(); ++k) fill_result(res[k], ptrs[k]->size(), &results[idx[k]]);
         }
-        return first_err;
+        (void)first_err;  // per-pattern errors are reported in results[i].status
+        return TFSM_OK;
     });
 }
 
 int tfsm_evaluate_support(tfsm_graph *g, const tfsm_pattern *pattern, int32_t tau, uint32_t flags,
                           tfsm_result *out) {
     if (!pattern || !out) return fail(TFSM_ERR_ARG, "null argument");
-    return tfsm_evaluate_batch(g, pattern, 1, tau, flags, out);
+    const int rc = tfsm_evaluate_batch(g, pattern, 1, tau, flags, out);
+    return rc != TFSM_OK ? rc : out->status;
 }
 
 int tfsm_mine(tfsm_graph *g, int32_t tau, int32_t max_nodes, uint32_t flags, const char *results_path,

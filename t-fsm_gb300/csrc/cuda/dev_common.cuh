@@ -105,6 +105,8 @@ struct SearchParams {
     uint32_t split_slice;    // anchor positions per split slice
     uint32_t split_cap;      // capacity of the split-task output buffer
     uint32_t group_cap;      // capacity of the split-group buffer
+    uint32_t n_pats;         // patterns of the batch
+    uint64_t words;          // size of each level bitmap pool (32-bit words)
 };
 
 }  // namespace dev

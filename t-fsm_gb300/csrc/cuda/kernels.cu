@@ -24,8 +24,34 @@
 #include "dev_common.cuh"
 #include "kernels.h"
 
+// Kernel launch; host-side SIMT emulation builds of this file (tests only) replace the syntax.
+#ifdef TFSM_SIMT_EMULATION
+#define TFSM_LAUNCH(kern, grid, block, stream, ...) tfsm_emu::launch((grid), (block), [&]() { kern(__VA_ARGS__); })
+#else
+#define TFSM_LAUNCH(kern, grid, block, stream, ...) kern<<<(grid), (block), 0, (stream)>>>(__VA_ARGS__)
+#endif
+
 namespace tfsm {
 namespace dev {
+
+// ---- optional self-checking build (TFSM_BOUNDS_CHECK): every global access of the search
+// kernels is checked against its buffer; the first violation is recorded (site, index, bound)
+// and the access is skipped, so the kernel returns normally and the host reports the record.
+#ifdef TFSM_BOUNDS_CHECK
+__device__ unsigned long long g_check[4];  // count, site, index, bound
+__device__ __forceinline__ bool inb(uint32_t site, uint64_t idx, uint64_t bound) {
+    if (idx < bound) return true;
+    if (atomicAdd(&g_check[0], 1ull) == 0) {
+        g_check[1] = site;
+        g_check[2] = idx;
+        g_check[3] = bound;
+    }
+    return false;
+}
+#define TFSM_IN(site, idx, bound) inb((site), (uint64_t)(idx), (uint64_t)(bound))
+#else
+#define TFSM_IN(site, idx, bound) true
+#endif
 
 namespace {
 
@@ -39,12 +65,20 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *__restrict__
     return lo;
 }
 
+// Warp-uniform read of one bitmap word.
+__device__ __forceinline__ uint32_t warp_word(const uint32_t *p, uint32_t lane) {
+    uint32_t w = 0;
+    if (lane == 0) w = __ldcg(p);
+    return __shfl_sync(0xffffffffu, w, 0);
+}
+
 // Same, adding 4 bytes per probed element to `bytes` (algorithmic-traffic accounting).
 __device__ __forceinline__ uint32_t lower_bound_cnt(const uint32_t *__restrict__ a, uint32_t lo, uint32_t hi,
-                                                    uint32_t x, uint32_t &bytes) {
+                                                    uint32_t x, uint32_t &bytes, uint64_t bound = ~0ull) {
     while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
         bytes += 4;
+        if (!TFSM_IN(1, mid, bound)) return hi;
         if (__ldg(a + mid) < x) lo = mid + 1;
         else hi = mid;
     }
@@ -74,7 +108,8 @@ __global__ void __launch_bounds__(256) k_domain_init(Graph g, const PatDesc *__r
                                                      const uint64_t *__restrict__ prefix, uint32_t n_items,
                                                      uint32_t *__restrict__ dom, uint32_t *__restrict__ found,
                                                      uint32_t *__restrict__ failed, const uint32_t *__restrict__ pdom,
-                                                     const uint32_t *__restrict__ pfailed) {
+                                                     const uint32_t *__restrict__ pfailed, uint64_t chk_words,
+                                                     uint64_t chk_pwords) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -89,6 +124,8 @@ __global__ void __launch_bounds__(256) k_domain_init(Graph g, const PatDesc *__r
         const uint32_t xl = word * 32 + lane;
         bool pass = xl < D.lsize[u];
         const int64_t poff = D.parent_off[u];
+        if (!TFSM_IN(30, word, D.words[u]) || !TFSM_IN(31, D.off[u] + word, chk_words)) continue;
+        if (poff >= 0 && !TFSM_IN(32, (uint64_t)poff + word, chk_pwords)) continue;
         if (poff >= 0) {
             const uint32_t pw = __ldg(pdom + poff + word) & ~__ldg(pfailed + poff + word);
             pass = pass && ((pw >> lane) & 1u);
@@ -96,6 +133,7 @@ __global__ void __launch_bounds__(256) k_domain_init(Graph g, const PatDesc *__r
         if (__any_sync(0xffffffffu, pass)) {
             const uint32_t x = D.lstart[u] + xl;
             uint32_t b = 0, e = 0;
+            if (pass && !TFSM_IN(33, x, g.n)) pass = false;
             if (pass) {
                 b = __ldg(g.row_off + x);
                 e = __ldg(g.row_off + x + 1);
@@ -128,7 +166,7 @@ __global__ void __launch_bounds__(256) k_domain_init(Graph g, const PatDesc *__r
 __global__ void __launch_bounds__(256) k_refine(Graph g, const PatDesc *__restrict__ descs, PatStatus *__restrict__ st,
                                                 const uint32_t *__restrict__ item_pu,
                                                 const uint64_t *__restrict__ prefix, uint32_t n_items,
-                                                uint32_t *__restrict__ dom) {
+                                                uint32_t *__restrict__ dom, uint64_t chk_words) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -140,8 +178,11 @@ __global__ void __launch_bounds__(256) k_refine(Graph g, const PatDesc *__restri
         const uint32_t p = pu >> 8, u = pu & 0xff;
         const PatDesc &D = descs[p];
         const uint32_t word = (uint32_t)(gw - prefix[item]);
+        if (!TFSM_IN(34, D.off[u] + word, chk_words)) continue;
         uint32_t *wp = dom + D.off[u] + word;
-        const uint32_t w0 = __ldcg(wp);
+        // other warps clear bits of this pool concurrently: one read, broadcast, keeps the warp's
+        // control flow (and its collectives) uniform
+        const uint32_t w0 = warp_word(wp, lane);
         if (w0 == 0) continue;
         uint32_t keep = w0;
         uint32_t bits = w0;
@@ -149,6 +190,7 @@ __global__ void __launch_bounds__(256) k_refine(Graph g, const PatDesc *__restri
             const int bit = __ffs(bits) - 1;
             bits &= bits - 1;
             const uint32_t v = D.lstart[u] + word * 32 + bit;
+            if (!TFSM_IN(35, v, g.n)) continue;
             const uint32_t vb = __ldg(g.row_off + v), ve = __ldg(g.row_off + v + 1);
             uint32_t nb = D.adj[u];
             bool ok = true;
@@ -164,9 +206,10 @@ __global__ void __launch_bounds__(256) k_refine(Graph g, const PatDesc *__restri
                 for (uint32_t base = lo; base < hi && !sup; base += 32) {
                     const uint32_t i = base + lane;
                     bool hit = false;
-                    if (i < hi && __ldg(g.elab + i) == el) {
+                    if (i < hi && TFSM_IN(36, i, g.m2) && __ldg(g.elab + i) == el) {
                         const uint32_t xl = __ldg(g.col + i) - ls;
-                        hit = (__ldcg(dw + (xl >> 5)) >> (xl & 31)) & 1u;
+                        if (TFSM_IN(37, (uint64_t)D.off[w] + (xl >> 5), chk_words))
+                            hit = (__ldcg(dw + (xl >> 5)) >> (xl & 31)) & 1u;
                     }
                     sup = __any_sync(0xffffffffu, hit);
                 }
@@ -177,7 +220,7 @@ __global__ void __launch_bounds__(256) k_refine(Graph g, const PatDesc *__restri
         if (keep != w0 && lane == 0) {
             atomicAnd(wp, keep);
             atomicSub(&st[p].dom_size[u], (uint32_t)__popc(w0 & ~keep));
-            st[p].changed = 1;
+            atomicOr(&st[p].changed, 1u);
         }
     }
 }
@@ -199,6 +242,7 @@ struct WarpPlan {
     int32_t n;
     uint32_t repmask;
     uint32_t key;             // (pattern << 8 | start vertex) the plan was loaded for
+    uint64_t words;           // size of the level's bitmap pools (checked builds)
 };
 
 struct WarpState {
@@ -212,7 +256,8 @@ struct WarpState {
 
 enum : int { kFail = 0, kFound = 1, kAbort = 2 };
 
-__device__ __forceinline__ void load_plan(WarpPlan &P, const PatDesc &D, uint32_t p, int u, uint32_t lane) {
+__device__ __forceinline__ void load_plan(WarpPlan &P, const PatDesc &D, uint32_t p, int u, uint32_t lane,
+                                          uint64_t words) {
     const uint32_t key = (p << 8) | (uint32_t)u;
     if (P.key == key) return;  // all lanes read the same shared value
     __syncwarp();
@@ -232,6 +277,7 @@ __device__ __forceinline__ void load_plan(WarpPlan &P, const PatDesc &D, uint32_
             if (D.rep[k] == k) rm |= 1u << k;
         P.repmask = rm;
         P.key = key;
+        P.words = words;
     }
     __syncwarp();
 }
@@ -251,10 +297,12 @@ __device__ __forceinline__ void setup_depth(const Graph &g, const WarpPlan &P, W
         for (uint32_t k = 0; k < lane; ++k) m &= m - 1;
         b = __ffs(m) - 1;
         const uint32_t y = S.emb[b];
-        const uint32_t rb = __ldg(g.row_off + y), re = __ldg(g.row_off + y + 1);
-        bytes += 8;
-        lo = lower_bound_cnt(g.col, rb, re, P.lstart[w], bytes);
-        hi = lower_bound_cnt(g.col, lo, re, P.lend[w], bytes);
+        if (TFSM_IN(2, y, g.n)) {
+            const uint32_t rb = __ldg(g.row_off + y), re = __ldg(g.row_off + y + 1);
+            bytes += 8;
+            lo = lower_bound_cnt(g.col, rb, re, P.lstart[w], bytes, g.m2);
+            hi = lower_bound_cnt(g.col, lo, re, P.lend[w], bytes, g.m2);
+        }
         key = ((unsigned long long)(hi - lo) << 32) | lane;
     }
 #pragma unroll
@@ -281,12 +329,14 @@ __device__ __forceinline__ bool check_candidate(const Graph &g, const WarpPlan &
                                                 uint32_t &x_out, uint32_t &bytes) {
     const int w = P.order[d];
     const int a = S.anchor[d];
+    if (!TFSM_IN(3, idx, g.m2)) return false;
     const uint32_t x = __ldg(g.col + idx);
     x_out = x;
     bytes += 5;  // neighbour id + edge label
     if (__ldg(g.elab + idx) != P.el[w][a]) return false;
     const uint32_t xl = x - P.lstart[w];
     bytes += 4;  // domain bitmap word
+    if (!TFSM_IN(4, (uint64_t)P.off[w] + (xl >> 5), P.words)) return false;
     if (!((__ldg(dom + P.off[w] + (xl >> 5)) >> (xl & 31)) & 1u)) return false;
     for (int k = 0; k < d; ++k)
         if (S.emb[P.order[k]] == x) return false;
@@ -295,12 +345,13 @@ __device__ __forceinline__ bool check_candidate(const Graph &g, const WarpPlan &
         const int b = __ffs(others) - 1;
         others &= others - 1;
         const uint32_t y = S.emb[b];
+        if (!TFSM_IN(5, y, g.n)) return false;
         const uint32_t re = __ldg(g.row_off + y + 1);
         bytes += 8;
-        uint32_t pos = lower_bound_cnt(g.col, __ldg(g.row_off + y), re, x, bytes);
+        uint32_t pos = lower_bound_cnt(g.col, __ldg(g.row_off + y), re, x, bytes, g.m2);
         bool hit = false;
         const uint8_t want = P.el[w][b];
-        while (pos < re && __ldg(g.col + pos) == x) {  // parallel edges: any with the right label
+        while (pos < re && TFSM_IN(6, pos, g.m2) && __ldg(g.col + pos) == x) {  // parallel edges: any with the label
             bytes += 5;
             if (__ldg(g.elab + pos) == want) {
                 hit = true;
@@ -331,8 +382,10 @@ __device__ int dfs(const Graph &g, const WarpPlan &P, WarpState &S, const uint32
     int d = 1;
     for (;;) {
         const uint32_t m = S.mask[d];
+        const uint32_t pos = S.pos[d], end = S.end[d];
+        // every lane has read this depth's state before lane 0 may overwrite it below
+        __syncwarp();
         if (m == 0) {
-            const uint32_t pos = S.pos[d], end = S.end[d];
             if (pos >= end) {
                 if (d == 1) return kFail;
                 --d;
@@ -368,10 +421,11 @@ __device__ int dfs(const Graph &g, const WarpPlan &P, WarpState &S, const uint32
         const int i = __ffs(m) - 1;
         if (lane == 0) {
             S.mask[d] = m & (m - 1);
-            S.emb[P.order[d]] = __ldg(g.col + S.base[d] + i);
+            if (TFSM_IN(7, S.base[d] + i, g.m2)) S.emb[P.order[d]] = __ldg(g.col + S.base[d] + i);
         }
         __syncwarp();
         bytes += 4;  // re-read of the chosen neighbour id
+        if (!TFSM_IN(8, d + 1, n)) return kFail;
         ++d;
         setup_depth(g, P, S, d, lane, bytes);
     }
@@ -388,6 +442,7 @@ __device__ __forceinline__ void mark_found(const WarpPlan &P, const WarpState &S
             orb &= orb - 1;
             const uint32_t xl = x - P.lstart[k];
             const uint32_t bit = 1u << (xl & 31);
+            if (!TFSM_IN(9, (uint64_t)P.off[k] + (xl >> 5), P.words)) continue;
             const uint32_t old = atomicOr(found + P.off[k] + (xl >> 5), bit);
             if (!(old & bit)) {
                 const uint32_t c = atomicAdd(&st.found_cnt[k], 1u) + 1;
@@ -411,6 +466,7 @@ __device__ __forceinline__ void mark_failed(const WarpPlan &P, PatStatus &st, ui
             orb &= orb - 1;
             const uint32_t xl = v - P.lstart[k];
             const uint32_t bit = 1u << (xl & 31);
+            if (!TFSM_IN(10, (uint64_t)P.off[k] + (xl >> 5), P.words)) continue;
             const uint32_t old = atomicOr(failed + P.off[k] + (xl >> 5), bit);
             if (k == u && !(old & bit)) {
                 const uint32_t c = atomicAdd(&st.fail_cnt[u], 1u) + 1;
@@ -421,14 +477,20 @@ __device__ __forceinline__ void mark_failed(const WarpPlan &P, PatStatus &st, ui
     __syncwarp();
 }
 
-__device__ __forceinline__ bool pattern_stops(const PatStatus &st, int u, bool exact) {
-    if (__ldcg(&st.state) != kRunning) return true;
-    return !exact && ((__ldcg(&st.done_mask) >> u) & 1u);
+// Warp-uniform: lane 0 reads the shared flags and broadcasts the decision.
+__device__ __forceinline__ bool pattern_stops(const PatStatus &st, int u, bool exact, uint32_t lane) {
+    int stop = 0;
+    if (lane == 0) {
+        stop = __ldcg(&st.state) != kRunning;
+        if (!stop && !exact) stop = (__ldcg(&st.done_mask) >> u) & 1u;
+    }
+    return __shfl_sync(0xffffffffu, stop, 0) != 0;
 }
+
 
 // Reserve `k` consecutive slots of a bounded buffer; false when full (bounded retries).
 __device__ __forceinline__ bool reserve(uint32_t *counter, uint32_t k, uint32_t cap, uint32_t &first) {
-    uint32_t old = *((volatile uint32_t *)counter);
+    uint32_t old = __ldcg(counter);
     for (int attempt = 0; attempt < 64; ++attempt) {
         if (old + k > cap || old + k < old) return false;
         const uint32_t prev = atomicCAS(counter, old, old + k);
@@ -471,19 +533,21 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
         const SearchItem item = items[it];
         const uint32_t p = item.pat;
         const int u = item.u;
-        load_plan(P, descs[p], p, u, lane);
+        if (!TFSM_IN(12, p, prm.n_pats) || !TFSM_IN(20, u, kMaxN)) continue;
+        load_plan(P, descs[p], p, u, lane, prm.words);
         PatStatus &ps = st[p];
         unsigned long long n_search = 0, n_steps = 0, n_bytes = 0;
         bool stop = false;
         for (uint32_t word = item.word_lo; word < item.word_hi && !stop; ++word) {
-            if (pattern_stops(ps, u, exact)) break;
+            if (pattern_stops(ps, u, exact, lane)) break;
             const uint32_t o = P.off[u] + word;
-            uint32_t cand = __ldg(dom + o) & ~__ldcg(found + o) & ~__ldcg(failed + o);
+            if (!TFSM_IN(13, o, prm.words)) break;
+            uint32_t cand = warp_word(dom + o, lane) & ~warp_word(found + o, lane) & ~warp_word(failed + o, lane);
             while (cand) {
                 const int b = __ffs(cand) - 1;
                 cand &= cand - 1;
-                if ((__ldcg(found + o) >> b) & 1u) continue;
-                if (pattern_stops(ps, u, exact)) {
+                if ((warp_word(found + o, lane) >> b) & 1u) continue;
+                if (pattern_stops(ps, u, exact, lane)) {
                     stop = true;
                     break;
                 }
@@ -500,11 +564,15 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
                     // depth-1 chunk that is being explored restarts from its base.
                     const uint32_t from = (adepth == 1) ? S.pos[1] : S.base[1];
                     const uint32_t to = S.end[1];
+                    if (!TFSM_IN(40, from, (uint64_t)to + 1) || !TFSM_IN(41, to, (uint64_t)g.m2 + 1) ||
+                        !TFSM_IN(42, __ldg(g.row_off + v), (uint64_t)from + 1) ||
+                        !TFSM_IN(43, to, (uint64_t)__ldg(g.row_off + v + 1) + 1))
+                        continue;
                     const uint32_t ns = (to - from + prm.split_slice - 1) / prm.split_slice;
                     bool ok = false;
                     uint32_t g0 = 0, t0 = 0;
                     if (lane == 0) {
-                        ok = ns > 0 && reserve(&counters[2], 1, prm.group_cap, g0);
+                        ok = ns > 0 && reserve(&counters[2], 1, prm.group_cap, g0) && TFSM_IN(15, g0, prm.group_cap);
                         if (ok && !reserve(&counters[1], ns, prm.split_cap, t0)) {
                             ok = false;
                             // the group slot stays unused: mark it so k_split never reads it
@@ -531,7 +599,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
                             t.lo = from + k * prm.split_slice;
                             t.hi = min(to, t.lo + prm.split_slice);
                             t.group = g0;
-                            splits[t0 + k] = t;
+                            if (TFSM_IN(14, t0 + k, prm.split_cap)) splits[t0 + k] = t;
                         }
                         n_steps += steps;
                         n_bytes += __reduce_add_sync(0xffffffffu, bytes);
@@ -582,14 +650,19 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_split(Graph g, const PatD
         const SplitTask t = splits[it];
         const uint32_t p = t.pat;
         const int u = t.u;
-        load_plan(P, descs[p], p, u, lane);
+        if (!TFSM_IN(16, p, prm.n_pats) || !TFSM_IN(17, t.group, prm.group_cap) || !TFSM_IN(21, u, kMaxN)) continue;
+        load_plan(P, descs[p], p, u, lane, prm.words);
         PatStatus &ps = st[p];
         SplitGroup &grp = groups[t.group];
         const uint32_t xl = t.v - P.lstart[u];
         const uint32_t o = P.off[u] + (xl >> 5);
+        if (!TFSM_IN(18, o, prm.words)) continue;
+        if (!TFSM_IN(44, t.v, g.n) || !TFSM_IN(45, t.lo, t.hi) || !TFSM_IN(46, __ldg(g.row_off + t.v), (uint64_t)t.lo + 1) ||
+            !TFSM_IN(47, t.hi, (uint64_t)__ldg(g.row_off + t.v + 1) + 1))
+            continue;
         const uint32_t bit = 1u << (xl & 31);
         bool searched = false;
-        if (!pattern_stops(ps, u, exact) && !(__ldcg(found + o) & bit)) {
+        if (!pattern_stops(ps, u, exact, lane) && !(warp_word(found + o, lane) & bit)) {
             if (lane == 0) S.emb[u] = t.v;
             __syncwarp();
             uint32_t steps = 0, bytes = 12;
@@ -617,6 +690,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_split(Graph g, const PatD
                         orb &= orb - 1;
                         const uint32_t kl = t.v - P.lstart[k];
                         const uint32_t kb = 1u << (kl & 31);
+                        if (!TFSM_IN(19, (uint64_t)P.off[k] + (kl >> 5), prm.words)) continue;
                         const uint32_t old = atomicOr(failed + P.off[k] + (kl >> 5), kb);
                         if (k == u && !(old & kb)) {
                             const uint32_t c = atomicAdd(&ps.fail_cnt[u], 1u) + 1;
@@ -634,6 +708,24 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_split(Graph g, const PatD
 // ------------------------------------------------------------------------------------------------
 // Host-side launchers.
 // ------------------------------------------------------------------------------------------------
+bool read_bounds_check(unsigned long long rec[4]) {
+#ifdef TFSM_BOUNDS_CHECK
+    const cudaError_t e = cudaMemcpyFromSymbol(rec, g_check, sizeof(unsigned long long) * 4);
+    if (e != cudaSuccess) {
+        std::fprintf(stderr, "tfsm checked build: cannot read the check record: %s\n", cudaGetErrorString(e));
+        rec[0] = 1;
+        rec[1] = rec[2] = rec[3] = ~0ull;
+        return true;
+    }
+    std::fprintf(stderr, "tfsm checked build: check record count %llu site %llu index %llu bound %llu\n", rec[0],
+                 rec[1], rec[2], rec[3]);
+    return rec[0] != 0;
+#else
+    rec[0] = rec[1] = rec[2] = rec[3] = 0;
+    return false;
+#endif
+}
+
 static int g_num_sms = 0;
 
 static int num_sms() {
@@ -649,25 +741,31 @@ static int num_sms() {
 cudaError_t launch_domain_init(const Graph &g, const PatDesc *descs, PatStatus *st, const uint32_t *item_pu,
                                const uint64_t *prefix, uint32_t n_items, uint64_t total_words, uint32_t *dom,
                                uint32_t *found, uint32_t *failed, const uint32_t *pdom, const uint32_t *pfailed,
-                               cudaStream_t s) {
+                               uint64_t chk_words, uint64_t chk_pwords, cudaStream_t s) {
     if (n_items == 0 || total_words == 0) return cudaSuccess;
     const uint64_t warps = total_words;
     uint64_t blocks = (warps * 32 + 255) / 256;
     const uint64_t cap = (uint64_t)num_sms() * 8 * 4;
     if (blocks > cap) blocks = cap;
-    k_domain_init<<<(unsigned)blocks, 256, 0, s>>>(g, descs, st, item_pu, prefix, n_items, dom, found, failed, pdom,
-                                                   pfailed);
+    TFSM_LAUNCH(k_domain_init, (unsigned)blocks, 256, s, g, descs, st, item_pu, prefix, n_items, dom, found, failed,
+                pdom, pfailed, chk_words, chk_pwords);
+#ifdef TFSM_BOUNDS_CHECK
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cudaGetLastError();
+#endif
     return cudaGetLastError();
 }
 
 cudaError_t launch_refine(const Graph &g, const PatDesc *descs, PatStatus *st, const uint32_t *item_pu,
                           const uint64_t *prefix, uint32_t n_items, uint64_t total_words, uint32_t *dom,
-                          cudaStream_t s) {
+                          uint64_t chk_words, cudaStream_t s) {
     if (n_items == 0 || total_words == 0) return cudaSuccess;
     uint64_t blocks = (total_words * 32 + 255) / 256;
     const uint64_t cap = (uint64_t)num_sms() * 8 * 4;
     if (blocks > cap) blocks = cap;
-    k_refine<<<(unsigned)blocks, 256, 0, s>>>(g, descs, st, item_pu, prefix, n_items, dom);
+    TFSM_LAUNCH(k_refine, (unsigned)blocks, 256, s, g, descs, st, item_pu, prefix, n_items, dom, chk_words);
+#ifdef TFSM_BOUNDS_CHECK
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cudaGetLastError();
+#endif
     return cudaGetLastError();
 }
 
@@ -682,17 +780,35 @@ cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, c
     uint64_t blocks = (uint64_t)num_sms() * (uint64_t)per_sm;
     const uint64_t need = (prm.n_items + kSearchWarps - 1) / kSearchWarps;
     if (blocks > need) blocks = need;
-    k_search<<<(unsigned)blocks, kSearchWarps * 32, 0, s>>>(g, descs, st, items, prm, counters, dom, found, failed,
-                                                             splits, groups);
+    TFSM_LAUNCH(k_search, (unsigned)blocks, kSearchWarps * 32, s, g, descs, st, items, prm, counters, dom, found,
+                failed, splits, groups);
     cudaError_t e = cudaGetLastError();
     *launches = 1;
+#ifdef TFSM_BOUNDS_CHECK
+    if (e == cudaSuccess && cudaStreamSynchronize(s) != cudaSuccess) {
+        std::fprintf(stderr, "tfsm checked build: fault in k_search\n");
+        return cudaGetLastError();
+    }
+    {
+        unsigned long long rec[4];
+        if (read_bounds_check(rec))
+            std::fprintf(stderr, "tfsm checked build: k_search site %llu index %llu bound %llu\n", rec[1], rec[2],
+                         rec[3]);
+    }
+#endif
     if (e != cudaSuccess || prm.step_budget == 0) return e;
     int per_sm2 = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_split, kSearchWarps * 32, 0);
     if (per_sm2 <= 0) per_sm2 = 1;
-    k_split<<<(unsigned)(num_sms() * per_sm2), kSearchWarps * 32, 0, s>>>(g, descs, st, prm, counters, dom, found,
-                                                                          failed, splits, groups);
+    TFSM_LAUNCH(k_split, (unsigned)(num_sms() * per_sm2), kSearchWarps * 32, s, g, descs, st, prm, counters, dom,
+                found, failed, splits, groups);
     *launches = 2;
+#ifdef TFSM_BOUNDS_CHECK
+    if (cudaStreamSynchronize(s) != cudaSuccess) {
+        std::fprintf(stderr, "tfsm checked build: fault in k_split\n");
+        return cudaGetLastError();
+    }
+#endif
     return cudaGetLastError();
 }
 

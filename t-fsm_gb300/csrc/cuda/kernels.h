@@ -13,17 +13,21 @@ constexpr int kSearchWarps = 8;  // warps per block of the search kernels
 cudaError_t launch_domain_init(const Graph &g, const PatDesc *descs, PatStatus *st, const uint32_t *item_pu,
                                const uint64_t *prefix, uint32_t n_items, uint64_t total_words, uint32_t *dom,
                                uint32_t *found, uint32_t *failed, const uint32_t *pdom, const uint32_t *pfailed,
-                               cudaStream_t s);
+                               uint64_t chk_words, uint64_t chk_pwords, cudaStream_t s);
 
 cudaError_t launch_refine(const Graph &g, const PatDesc *descs, PatStatus *st, const uint32_t *item_pu,
                           const uint64_t *prefix, uint32_t n_items, uint64_t total_words, uint32_t *dom,
-                          cudaStream_t s);
+                          uint64_t chk_words, cudaStream_t s);
 
 // Runs k_search over `prm.n_items` items, then (when a step budget is set) k_split over the
 // slices it produced.  `counters` (4 x u32) must be zero on entry.
 cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchItem *items,
                           const SearchParams &prm, uint32_t *counters, const uint32_t *dom, uint32_t *found,
                           uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s, int *launches);
+
+// Checked builds (-DTFSM_BOUNDS_CHECK): the first out-of-bounds access the search kernels
+// detected (count, site, index, bound); false when none or when checks are compiled out.
+bool read_bounds_check(unsigned long long rec[4]);
 
 }  // namespace dev
 }  // namespace tfsm

@@ -326,7 +326,8 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     if (!item_pu.empty()) {
         TFSM_CK(cudaEventRecord(I.ev0, I.stream));
         TFSM_CK(dev::launch_domain_init(I.g, L.descs.p, I.status.p, I.item_pu.p, I.prefix.p, (uint32_t)item_pu.size(),
-                                        prefix.back(), L.dom.p, L.found.p, L.failed.p, pdom, pfailed, I.stream));
+                                        prefix.back(), L.dom.p, L.found.p, L.failed.p, pdom, pfailed, total,
+                                        prev ? prev->impl->words : 0, I.stream));
         times_.init_ms += time_since_ev0();
         times_.init_launches++;
         times_.init_words += prefix.back();
@@ -358,7 +359,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         build_items(active);
         TFSM_CK(cudaEventRecord(I.ev0, I.stream));
         TFSM_CK(dev::launch_refine(I.g, L.descs.p, I.status.p, I.item_pu.p, I.prefix.p, (uint32_t)item_pu.size(),
-                                   prefix.back(), L.dom.p, I.stream));
+                                   prefix.back(), L.dom.p, total, I.stream));
         times_.refine_ms += time_since_ev0();
         times_.refine_launches++;
         times_.refine_words += prefix.back();
@@ -444,6 +445,8 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     prm.split_slice = std::max<uint32_t>(32, opt.split_slice);
     prm.split_cap = (uint32_t)I.splits.n;
     prm.group_cap = (uint32_t)I.groups.n;
+    prm.n_pats = (uint32_t)P;
+    prm.words = total;
     TFSM_CK(cudaEventRecord(I.ev0, I.stream));
     int launches = 0;
     TFSM_CK(dev::launch_search(I.g, L.descs.p, I.status.p, I.items.p, prm, I.counters.p, L.dom.p, L.found.p,
@@ -451,6 +454,13 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     times_.search_ms += time_since_ev0();
     times_.search_launches += (uint64_t)launches;
     times_.search_calls++;
+    {
+        unsigned long long rec[4];
+        if (dev::read_bounds_check(rec))
+            throw EngineError(12, "bounds check failed in the search kernels: site " + std::to_string(rec[1]) +
+                                      " index " + std::to_string(rec[2]) + " bound " + std::to_string(rec[3]) +
+                                      " (" + std::to_string(rec[0]) + " violations)");
+    }
     read_status();
 
     for (size_t p = 0; p < P; ++p) {

@@ -9,11 +9,15 @@
 // which is not a strict weak ordering once there is more than one edge label.  It feeds a
 // std::map, so the same std::map operations are issued in the same sequence to obtain the same
 // "smallest" forward extension; with one edge label the ordering is an ordinary label order.
+// With that ordering libstdc++'s hinted insertion can overwrite a child link and orphan a subtree
+// (the reference leaks those nodes); here every container of one check lives in a monotonic
+// arena released when the check ends, which keeps the tree algorithm unchanged.
 #pragma once
 
 #include <algorithm>
 #include <cstdint>
 #include <map>
+#include <memory_resource>
 #include <set>
 #include <string>
 #include <vector>
@@ -172,14 +176,14 @@ struct FwdKey {
     }
 };
 
-using Trans = std::vector<const PEdge *>;  // edges of one projection, in MIN code order
-using ProjDB = std::vector<Trans>;
+using Trans = std::pmr::vector<const PEdge *>;  // edges of one projection, in MIN code order
+using ProjDB = std::pmr::vector<Trans>;
 
 struct History {
     std::vector<const PEdge *> edges;
     std::vector<char> has_edge, has_vertex;
     History(int n_vertices, int n_edges, const Trans &t)
-        : edges(t), has_edge((size_t)n_edges, 0), has_vertex((size_t)n_vertices, 0) {
+        : edges(t.begin(), t.end()), has_edge((size_t)n_edges, 0), has_vertex((size_t)n_vertices, 0) {
         for (const PEdge *e : t) {
             has_edge[(size_t)e->id] = 1;
             has_vertex[(size_t)e->from] = 1;
@@ -192,6 +196,7 @@ struct Checker {
     const Pattern &pat;      // the pattern whose code is checked
     const Pattern &g;        // the same pattern viewed as a graph (MIN_GRAPH)
     std::vector<DfsCode> min_codes;
+    std::pmr::monotonic_buffer_resource arena;  // owns every map node and projection of the check
 
     explicit Checker(const Pattern &p) : pat(p), g(p) {}
 
@@ -249,7 +254,7 @@ struct Checker {
 
         // backward extensions from the rightmost vertex
         {
-            std::map<int, ProjDB> root;
+            std::pmr::map<int, ProjDB> root(&arena);
             bool flg = false;
             int new_to = 0, new_tolabel = 0;
             // `i` is unsigned in the reference: with a single-edge rightmost path the loop is empty.
@@ -258,7 +263,7 @@ struct Checker {
                     History h(nv, ne, cur);
                     const PEdge *e = get_backward(h.edges[(size_t)rmpath[i]], h.edges[(size_t)rmpath[0]], h);
                     if (e) {
-                        Trans t = cur;
+                        Trans t(cur, &arena);
                         t.push_back(e);
                         root[e->label].push_back(std::move(t));
                         new_to = min_codes[(size_t)rmpath[i]].from;
@@ -285,7 +290,7 @@ struct Checker {
         {
             bool flg = false;
             int new_from = 0, new_fromlabel = 0;
-            std::map<FwdKey, ProjDB> root;
+            std::pmr::map<FwdKey, ProjDB> root(&arena);
             std::vector<const PEdge *> edges;
             for (const Trans &cur : projected) {
                 History h(nv, ne, cur);
@@ -295,7 +300,7 @@ struct Checker {
                         FwdKey k{it->label, lab(it->to)};
                         new_from = maxtoc;
                         new_fromlabel = lab(it->from);
-                        Trans t = cur;
+                        Trans t(cur, &arena);
                         t.push_back(it);
                         root[k].push_back(std::move(t));
                     }
@@ -310,7 +315,7 @@ struct Checker {
                             FwdKey k{it->label, lab(it->to)};
                             new_from = min_codes[(size_t)rmpath[i]].from;
                             new_fromlabel = lab(it->from);
-                            Trans t = cur;
+                            Trans t(cur, &arena);
                             t.push_back(it);
                             root[k].push_back(std::move(t));
                         }
@@ -336,13 +341,15 @@ struct Checker {
 
     bool run() {
         if (pat.codes.size() == 1) return true;
-        std::map<RootKey, ProjDB> root;
+        std::pmr::map<RootKey, ProjDB> root(&arena);
         for (int from = 0; from < g.size(); ++from) {
             const PVertex &v = g.vertices[from];
             for (const PEdge &e : v.edges) {
                 if (v.label <= lab(e.to)) {
                     RootKey k{v.label, e.label, lab(e.to)};
-                    root[k].push_back(Trans{&e});
+                    Trans t(&arena);
+                    t.push_back(&e);
+                    root[k].push_back(std::move(t));
                 }
             }
         }

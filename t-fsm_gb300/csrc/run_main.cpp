@@ -1,6 +1,7 @@
 // `run`: command-line drop-in for the reference miners (parallel/run.cpp:11-82, serial/run.cpp).
 //
 //   run -file G.lg -freq TAU [-thread T] [-maxNodes N] [-plain] [-exact] [-out PATH]
+//       [-step-budget B] [-split-slice S] [-chunk-words W] [-refine-rounds R]
 //
 // Frequent patterns go to ./grami_results.txt (or -out PATH) in the serial build's format
 // (serial/grami.h:622-635); timing and counts are printed as the parallel build prints them.
@@ -43,6 +44,18 @@ int main(int argc, char **argv) {
     int rc = tfsm_graph_load(file, tau, &g);
     if (rc != TFSM_OK) {
         std::fprintf(stderr, "error %d: %s\n", rc, tfsm_last_error());
+        return 1;
+    }
+    tfsm_options o;
+    tfsm_get_options(g, &o);
+    if (opt(argc, argv, "-step-budget")) o.step_budget = (uint32_t)std::atoi(opt(argc, argv, "-step-budget"));
+    if (opt(argc, argv, "-split-slice")) o.split_slice = (uint32_t)std::atoi(opt(argc, argv, "-split-slice"));
+    if (opt(argc, argv, "-chunk-words")) o.chunk_words = (uint32_t)std::atoi(opt(argc, argv, "-chunk-words"));
+    if (opt(argc, argv, "-refine-rounds")) o.refine_rounds = (uint32_t)std::atoi(opt(argc, argv, "-refine-rounds"));
+    rc = tfsm_set_options(g, &o);
+    if (rc != TFSM_OK) {
+        std::fprintf(stderr, "error %d: %s\n", rc, tfsm_last_error());
+        tfsm_graph_free(g);
         return 1;
     }
     tfsm_mine_stats st;

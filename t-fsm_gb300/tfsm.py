@@ -209,11 +209,9 @@ class Graph:
             arr[i].codes = C.cast(codes, C.POINTER(DfsCode))
         res = (ResultC * max(n, 1))()
         rc = lib().tfsm_evaluate_batch(self._h, arr, n, int(self.tau if tau is None else tau), int(flags), res)
-        out = [Result(r.status, bool(r.frequent), r.support, list(r.mni[: r.n_vertices]), bool(r.decided_by_filter),
-                      r.searches, r.steps) for r in res[:n]]
-        if rc != TFSM_OK and all(r.status != TFSM_OK for r in out):
-            _check(rc)
-        return out
+        _check(rc)
+        return [Result(r.status, bool(r.frequent), r.support, list(r.mni[: r.n_vertices]), bool(r.decided_by_filter),
+                       r.searches, r.steps) for r in res[:n]]
 
     def options(self) -> dict:
         o = OptionsC()

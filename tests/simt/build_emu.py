@@ -1,0 +1,39 @@
+"""Build the host-side SIMT emulation of the engine (test infrastructure only).
+
+Compiles the product's kernel and engine sources unchanged, as C++ for the CPU, against
+tests/simt/cuda_runtime.h, with sanitizers, into tests/simt/_build/run_emu (the `run` CLI).
+usage: python tests/simt/build_emu.py [asan|tsan]
+"""
+from __future__ import annotations
+
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+CSRC = ROOT / "t-fsm_gb300" / "csrc"
+
+SANITIZE = {"asan": ["-fsanitize=address,undefined", "-fno-sanitize-recover=undefined"],
+            "tsan": ["-fsanitize=thread"], "none": []}
+
+
+def build(kind: str = "asan") -> Path:
+    out_dir = HERE / "_build"
+    out_dir.mkdir(exist_ok=True)
+    exe = out_dir / f"run_emu_{kind}"
+    srcs = [CSRC / "cuda" / "kernels.cu", CSRC / "engine.cu", CSRC / "miner.cpp", CSRC / "capi.cpp",
+            CSRC / "run_main.cpp"]
+    deps = srcs + list(CSRC.rglob("*.h*")) + list(CSRC.rglob("*.cuh")) + [HERE / "cuda_runtime.h"]
+    if exe.exists() and all(d.stat().st_mtime <= exe.stat().st_mtime for d in deps):
+        return exe
+    cmd = ["g++", "-std=c++20", "-O1", "-g", "-pthread", "-DTFSM_SIMT_EMULATION", "-I", str(HERE), "-I", str(CSRC),
+           *SANITIZE[kind], "-x", "c++", *map(str, srcs), "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(" ".join(cmd) + "\n" + r.stderr[-4000:])
+    return exe
+
+
+if __name__ == "__main__":
+    print(build(sys.argv[1] if len(sys.argv) > 1 else "asan"))
