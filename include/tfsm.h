@@ -133,6 +133,20 @@ typedef struct {
 int tfsm_get_options(const tfsm_graph *g, tfsm_options *opt);
 int tfsm_set_options(tfsm_graph *g, const tfsm_options *opt);
 
+/* Allocation-free variant of tfsm_evaluate_support (no counterpart in the reference).
+ * For callers that must not allocate device memory during the call — for example code under a
+ * framework whose own caching allocator owns the device, or latency-critical code that cannot
+ * afford the device-wide synchronisation of cudaMalloc / cudaFree.  The call makes no device
+ * allocation and calls no allocating library routine: every per-call buffer lives in one fixed
+ * 16 MiB device array that the library holds on each GPU it is used on, until the process exits.
+ * A pattern whose domain bitmaps do not fit is rejected with TFSM_ERR_LIMIT.  Calls share that array
+ * and leave its contents behind (each call clears what must start at zero); calls whose GPU work
+ * overlaps would race on it — calls on one graph handle are serialised by the handle.  The first call
+ * on a device looks up the array's device address, so make it before any stream capture.  Results
+ * equal tfsm_evaluate_support's (mni[] exactly with TFSM_FLAG_EXACT). */
+int tfsm_evaluate_support_noalloc(tfsm_graph *g, const tfsm_pattern *pattern, int32_t tau, uint32_t flags,
+                                  tfsm_result *out);
+
 /* Message of the last failing call on this thread ("" when none). */
 const char *tfsm_last_error(void);
 

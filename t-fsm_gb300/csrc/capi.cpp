@@ -9,6 +9,7 @@
 #include "../../include/tfsm.h"
 #include "engine.hpp"
 #include "miner.hpp"
+#include "noalloc.hpp"
 
 struct tfsm_graph {
     tfsm::LgGraph lg;
@@ -279,6 +280,20 @@ int tfsm_set_options(tfsm_graph *g, const tfsm_options *o) {
         g->opt.refine_rounds = o->refine_rounds;
         return TFSM_OK;
     });
+}
+
+int tfsm_evaluate_support_noalloc(tfsm_graph *g, const tfsm_pattern *pattern, int32_t tau, uint32_t flags,
+                                  tfsm_result *out) {
+    if (!g || !pattern || !out) return fail(TFSM_ERR_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(g->mu);
+    const char *msg = "";
+    const int rc = tfsm::noalloc_evaluate(*g->eng, pattern, (uint32_t)std::max(tau, 0),
+                                          (flags & TFSM_FLAG_EXACT) != 0, out, msg);
+    if (rc != TFSM_OK) {
+        out->status = rc;
+        return fail(rc, msg);
+    }
+    return TFSM_OK;
 }
 
 const char *tfsm_last_error(void) { return g_err.c_str(); }

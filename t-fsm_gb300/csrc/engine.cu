@@ -90,6 +90,7 @@ struct GpuEngine::Impl {
     DevBuf<dev::SplitTask> splits;
     DevBuf<dev::SplitGroup> groups;
     std::vector<PatStatus> hstatus;
+    int device = 0;
 };
 
 GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
@@ -100,6 +101,7 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
         throw EngineError(9, "no CUDA device available for the GPU engine");
     TFSM_CK(cudaSetDevice(device));
     Impl &I = *impl_;
+    I.device = device;
     if (lg.offs[lg.n] >= (1ull << 32)) throw EngineError(5, "graph has >= 2^32 adjacency entries");
     // dense labels
     for (size_t i = 0; i < lg.freq_vlabels.size(); ++i) I.vdense[lg.freq_vlabels[i]] = (int)i;
@@ -179,6 +181,16 @@ uint32_t GpuEngine::n_vertices() const { return impl_->n; }
 int GpuEngine::dense_label(int label) const {
     auto it = impl_->vdense.find(label);
     return it == impl_->vdense.end() ? -1 : it->second;
+}
+int GpuEngine::device() const { return impl_->device; }
+const dev::Graph &GpuEngine::device_graph() const { return impl_->g; }
+int GpuEngine::dense_edge_label(int label) const {
+    auto it = impl_->edense.find(label);
+    return it == impl_->edense.end() ? -1 : it->second;
+}
+uint32_t GpuEngine::label_first(int dense) const { return impl_->lstart[(size_t)dense]; }
+uint32_t GpuEngine::label_size(int dense) const {
+    return impl_->lstart[(size_t)dense + 1] - impl_->lstart[(size_t)dense];
 }
 
 namespace {

@@ -12,6 +12,10 @@
 
 namespace tfsm {
 
+namespace dev {
+struct Graph;
+}
+
 struct EngineError : std::runtime_error {
     int code;
     EngineError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
@@ -72,6 +76,12 @@ public:
     double upload_ms() const { return upload_ms_; }
     int dense_label(int label) const;  // -1 when the label is not frequent
     uint32_t n_vertices() const;
+    // Read-only views used by the allocation-free entry point (noalloc.cu).
+    int device() const;
+    const dev::Graph &device_graph() const;
+    int dense_edge_label(int label) const;           // -1 when the edge label is not frequent
+    uint32_t label_first(int dense) const;           // first vertex id of a dense label
+    uint32_t label_size(int dense) const;            // vertices of a dense label
 
 private:
     struct Impl;

@@ -39,6 +39,7 @@ EXPORTED = (
     "tfsm_mine",
     "tfsm_get_options",
     "tfsm_set_options",
+    "tfsm_evaluate_support_noalloc",
     "tfsm_last_error",
 )
 
@@ -110,6 +111,8 @@ def lib() -> C.CDLL:
         L.tfsm_mine.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_uint32, C.c_char_p, C.POINTER(MineStatsC)]
         L.tfsm_get_options.argtypes = [C.c_void_p, C.POINTER(OptionsC)]
         L.tfsm_set_options.argtypes = [C.c_void_p, C.POINTER(OptionsC)]
+        L.tfsm_evaluate_support_noalloc.argtypes = [C.c_void_p, C.POINTER(PatternC), C.c_int32, C.c_uint32,
+                                                    C.POINTER(ResultC)]
         L.tfsm_last_error.argtypes = []
         L.tfsm_last_error.restype = C.c_char_p
         for f in EXPORTED:

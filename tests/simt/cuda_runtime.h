@@ -30,6 +30,7 @@
 #define __forceinline__ inline
 #define __launch_bounds__(...)
 #define __shared__ static
+#define __align__(n) __attribute__((aligned(n)))
 
 struct dim3 {
     unsigned x = 1, y = 1, z = 1;
@@ -306,6 +307,11 @@ inline cudaError_t cudaMemcpyAsync(void *d, const void *s, size_t n, cudaMemcpyK
 inline cudaError_t cudaMemcpy(void *d, const void *s, size_t n, cudaMemcpyKind k) { return cudaMemcpyAsync(d, s, n, k); }
 inline cudaError_t cudaMemsetAsync(void *d, int v, size_t n, cudaStream_t = nullptr) {
     if (n) std::memset(d, v, n);
+    return cudaSuccess;
+}
+template <class T>
+inline cudaError_t cudaGetSymbolAddress(void **p, const T &sym) {
+    *p = (void *)&sym;
     return cudaSuccess;
 }
 template <class T>
