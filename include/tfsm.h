@@ -82,6 +82,7 @@ typedef struct {
     uint64_t frequent;     /* frequent patterns, 1-edge patterns included */
     uint64_t searches, steps, by_filter, engine_calls;
     int32_t levels;
+    int32_t complete;      /* 0 when the time limit stopped the run early */
 } tfsm_mine_stats;
 
 /* Load a .lg graph and prune it for threshold `tau` (label frequency, edge-label frequency and
@@ -128,6 +129,10 @@ typedef struct {
     uint32_t split_slice;   /* depth-1 adjacency positions per slice (>= 32) */
     uint32_t chunk_words;   /* 32-bit domain-bitmap words per search work item (>= 1) */
     uint32_t refine_rounds; /* arc-consistency passes for patterns that need a search (>= 1) */
+    uint32_t max_batch;     /* tfsm_mine: most patterns per engine call (>= 1) */
+    uint32_t reserved;
+    double time_limit_s;    /* tfsm_mine: stop between engine calls after this many seconds (0: none);
+                               the run is then reported incomplete */
 } tfsm_options;
 
 int tfsm_get_options(const tfsm_graph *g, tfsm_options *opt);

@@ -252,6 +252,7 @@ int tfsm_mine(tfsm_graph *g, int32_t tau, int32_t max_nodes, uint32_t flags, con
             stats->by_filter = st.by_filter;
             stats->engine_calls = st.engine_calls;
             stats->levels = st.levels;
+            stats->complete = st.complete ? 1 : 0;
         }
         return TFSM_OK;
     });
@@ -264,6 +265,9 @@ int tfsm_get_options(const tfsm_graph *g, tfsm_options *o) {
         o->split_slice = g->opt.split_slice;
         o->chunk_words = g->opt.chunk_words;
         o->refine_rounds = g->opt.refine_rounds;
+        o->max_batch = g->opt.max_batch;
+        o->reserved = 0;
+        o->time_limit_s = g->opt.time_limit_s;
         return TFSM_OK;
     });
 }
@@ -271,13 +275,17 @@ int tfsm_get_options(const tfsm_graph *g, tfsm_options *o) {
 int tfsm_set_options(tfsm_graph *g, const tfsm_options *o) {
     return guarded([&]() -> int {
         if (!g || !o) return fail(TFSM_ERR_ARG, "null argument");
-        if (o->split_slice < 32 || o->chunk_words < 1 || o->refine_rounds < 1)
-            return fail(TFSM_ERR_ARG, "split_slice must be >= 32, chunk_words and refine_rounds >= 1");
+        if (o->split_slice < 32 || o->chunk_words < 1 || o->refine_rounds < 1 || o->max_batch < 1 ||
+            !(o->time_limit_s >= 0))
+            return fail(TFSM_ERR_ARG,
+                        "split_slice must be >= 32; chunk_words, refine_rounds and max_batch >= 1; time_limit_s >= 0");
         std::lock_guard<std::mutex> lk(g->mu);
         g->opt.step_budget = o->step_budget;
         g->opt.split_slice = o->split_slice;
         g->opt.chunk_words = o->chunk_words;
         g->opt.refine_rounds = o->refine_rounds;
+        g->opt.max_batch = o->max_batch;
+        g->opt.time_limit_s = o->time_limit_s;
         return TFSM_OK;
     });
 }

@@ -5,7 +5,8 @@
 //   [label_start[L], label_start[L+1]) — ids keep the reference's pruned order inside a label.
 //   row_off[n+1] (u32) / col[2m] (u32, ascending) / elab[2m] (u8, dense edge label)
 //   Ascending neighbour ids are therefore ordered by (neighbour label, id): the neighbours of v
-//   that carry label L are one sub-range of v's list, found by two binary searches.
+//   that carry label L are one sub-range of v's list; a per-vertex table of label offsets gives its
+//   bounds with two independent loads.
 // Per pattern vertex u, a candidate domain D(u) is a bitmap over the id range of u's label; the
 // same layout holds the "found" (MNI domain members proven by an embedding) and "failed"
 // (proven non-members) bitmaps.  Offsets are in 32-bit words into three level-wide pools.
@@ -27,6 +28,10 @@ struct Graph {
     const uint32_t *col = nullptr;
     const uint8_t *elab = nullptr;
     const uint32_t *label_start = nullptr;  // [n_labels + 1]
+    // lab_off[v * lab_stride + L] = position in col of v's first neighbour with label >= L, for
+    // L = 0..n_labels: the neighbours of v with label L are [lab_off[.. + L], lab_off[.. + L + 1]).
+    const uint32_t *lab_off = nullptr;
+    uint32_t lab_stride = 0;                // n_labels + 1
 };
 
 // One pattern of a batch.  Plain old data, copied to the device once per batch.
@@ -64,6 +69,7 @@ struct PatStatus {
     unsigned long long searches;      // candidate checks started
     unsigned long long steps;         // candidate chunks evaluated by the search
     unsigned long long bytes;         // algorithmic bytes read by the search (logical loads)
+    unsigned long long max_steps;     // longest single search (chunk evaluations)
 };
 
 enum : uint32_t { kRunning = 0, kFrequent = 1, kInfrequent = 2 };

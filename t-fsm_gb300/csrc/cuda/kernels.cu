@@ -140,11 +140,10 @@ __global__ void __launch_bounds__(256) k_domain_init(Graph g, const PatDesc *__r
                 pass = (int32_t)(e - b) >= D.deg[u];
             }
             const int nn = D.nlf_n[u];
+            const uint32_t *lo_x = g.lab_off + (size_t)x * g.lab_stride;
             for (int k = 0; k < nn && pass; ++k) {
                 const int L = D.nlf_lab[u][k];
-                const uint32_t lo = lower_bound_u32(g.col, b, e, __ldg(g.label_start + L));
-                const uint32_t hi = lower_bound_u32(g.col, lo, e, __ldg(g.label_start + L + 1));
-                pass = (hi - lo) >= (uint32_t)D.nlf_cnt[u][k];
+                pass = (__ldg(lo_x + L + 1) - __ldg(lo_x + L)) >= (uint32_t)D.nlf_cnt[u][k];
             }
         }
         const uint32_t mask = __ballot_sync(0xffffffffu, pass);
@@ -191,15 +190,14 @@ __global__ void __launch_bounds__(256) k_refine(Graph g, const PatDesc *__restri
             bits &= bits - 1;
             const uint32_t v = D.lstart[u] + word * 32 + bit;
             if (!TFSM_IN(35, v, g.n)) continue;
-            const uint32_t vb = __ldg(g.row_off + v), ve = __ldg(g.row_off + v + 1);
+            const uint32_t *lo_v = g.lab_off + (size_t)v * g.lab_stride;
             uint32_t nb = D.adj[u];
             bool ok = true;
             while (nb && ok) {
                 const int w = __ffs(nb) - 1;
                 nb &= nb - 1;
-                const uint32_t ls = D.lstart[w], le = ls + D.lsize[w];
-                const uint32_t lo = lower_bound_u32(g.col, vb, ve, ls);
-                const uint32_t hi = lower_bound_u32(g.col, lo, ve, le);
+                const uint32_t ls = D.lstart[w];
+                const uint32_t lo = __ldg(lo_v + D.lab[w]), hi = __ldg(lo_v + D.lab[w] + 1);
                 const uint8_t el = D.el[u][w];
                 const uint32_t *dw = dom + D.off[w];
                 bool sup = false;
@@ -238,6 +236,7 @@ struct WarpPlan {
     uint32_t orbit[kMaxN];
     uint32_t bn[kMaxN];       // by depth
     uint8_t order[kMaxN];     // by depth
+    uint8_t lab[kMaxN];       // dense label by pattern vertex
     uint8_t el[kMaxN][kMaxN];
     int32_t n;
     uint32_t repmask;
@@ -249,12 +248,19 @@ struct WarpState {
     uint32_t emb[kMaxN];      // by pattern vertex
     uint32_t pos[kMaxN];      // by depth: next unevaluated anchor position
     uint32_t end[kMaxN];      // by depth: end of the anchor range
-    uint32_t base[kMaxN];     // by depth: first position of the chunk held in mask
-    uint32_t mask[kMaxN];     // by depth: surviving candidates of that chunk not yet descended into
+    uint32_t base[kMaxN];     // by depth: first position of the chunk held in mask / rest
+    uint32_t mask[kMaxN];     // by depth: surviving candidates already known to be in w's MNI domain
+    uint32_t rest[kMaxN];     // by depth: the other surviving candidates (tried after `mask`)
     uint8_t anchor[kMaxN];    // by depth: pattern vertex whose adjacency is scanned
+    uint32_t blo[kMaxN][kMaxN];  // [depth][backward neighbour b]: label range of order[depth]'s
+    uint32_t bhi[kMaxN][kMaxN];  //   label inside emb[b]'s adjacency
 };
 
 enum : int { kFail = 0, kFound = 1, kAbort = 2 };
+
+// Try candidates already known to be in w's MNI domain first.  Measured slower on the benchmark
+// graphs (the extra ballot and found-word loads cost more than the reordering saves): off.
+constexpr bool kFoundFirst = false;
 
 __device__ __forceinline__ void load_plan(WarpPlan &P, const PatDesc &D, uint32_t p, int u, uint32_t lane,
                                           uint64_t words) {
@@ -268,6 +274,7 @@ __device__ __forceinline__ void load_plan(WarpPlan &P, const PatDesc &D, uint32_
         P.orbit[lane] = D.orbit_mask[lane];
         P.bn[lane] = D.bn[u][lane];
         P.order[lane] = D.order[u][lane];
+        P.lab[lane] = (uint8_t)D.lab[lane];
     }
     for (uint32_t i = lane; i < (uint32_t)(kMaxN * kMaxN); i += 32) (&P.el[0][0])[i] = (&D.el[0][0])[i];
     if (lane == 0) {
@@ -298,11 +305,13 @@ __device__ __forceinline__ void setup_depth(const Graph &g, const WarpPlan &P, W
         b = __ffs(m) - 1;
         const uint32_t y = S.emb[b];
         if (TFSM_IN(2, y, g.n)) {
-            const uint32_t rb = __ldg(g.row_off + y), re = __ldg(g.row_off + y + 1);
+            const uint32_t *lo_y = g.lab_off + (size_t)y * g.lab_stride + P.lab[w];
+            lo = __ldg(lo_y);
+            hi = __ldg(lo_y + 1);
             bytes += 8;
-            lo = lower_bound_cnt(g.col, rb, re, P.lstart[w], bytes, g.m2);
-            hi = lower_bound_cnt(g.col, lo, re, P.lend[w], bytes, g.m2);
         }
+        S.blo[d][b] = lo;  // lane k owns backward neighbour b's slot
+        S.bhi[d][b] = hi;
         key = ((unsigned long long)(hi - lo) << 32) | lane;
     }
 #pragma unroll
@@ -318,15 +327,19 @@ __device__ __forceinline__ void setup_depth(const Graph &g, const WarpPlan &P, W
         S.pos[d] = lo;
         S.end[d] = hi;
         S.mask[d] = 0;
+        S.rest[d] = 0;
         S.anchor[d] = (uint8_t)b;
     }
     __syncwarp();
 }
 
 // Is adjacency position `idx` of the depth-d anchor a valid extension?  (one lane, one position)
+// `known` is set when x is already proven to be in w's MNI domain (a found embedding maps w to x).
+// A candidate proven to be in no embedding as w (its `failed` bit) is rejected: sound pruning.
 __device__ __forceinline__ bool check_candidate(const Graph &g, const WarpPlan &P, const WarpState &S,
-                                                const uint32_t *__restrict__ dom, int d, uint32_t idx,
-                                                uint32_t &x_out, uint32_t &bytes) {
+                                                const uint32_t *__restrict__ dom, const uint32_t *found,
+                                                const uint32_t *failed, int d, uint32_t idx, uint32_t &x_out,
+                                                bool &known, uint32_t &bytes) {
     const int w = P.order[d];
     const int a = S.anchor[d];
     if (!TFSM_IN(3, idx, g.m2)) return false;
@@ -337,18 +350,22 @@ __device__ __forceinline__ bool check_candidate(const Graph &g, const WarpPlan &
     const uint32_t xl = x - P.lstart[w];
     bytes += 4;  // domain bitmap word
     if (!TFSM_IN(4, (uint64_t)P.off[w] + (xl >> 5), P.words)) return false;
-    if (!((__ldg(dom + P.off[w] + (xl >> 5)) >> (xl & 31)) & 1u)) return false;
+    const uint32_t wi = P.off[w] + (xl >> 5), bit = 1u << (xl & 31);
+    if (!(__ldg(dom + wi) & bit)) return false;
+    bytes += 4;  // failed word
+    if (__ldcg(failed + wi) & bit) return false;
+    if (kFoundFirst) {
+        bytes += 4;
+        known = (__ldcg(found + wi) & bit) != 0;
+    }
     for (int k = 0; k < d; ++k)
         if (S.emb[P.order[k]] == x) return false;
     uint32_t others = P.bn[d] & ~(1u << a);
     while (others) {
         const int b = __ffs(others) - 1;
         others &= others - 1;
-        const uint32_t y = S.emb[b];
-        if (!TFSM_IN(5, y, g.n)) return false;
-        const uint32_t re = __ldg(g.row_off + y + 1);
-        bytes += 8;
-        uint32_t pos = lower_bound_cnt(g.col, __ldg(g.row_off + y), re, x, bytes, g.m2);
+        const uint32_t re = S.bhi[d][b];
+        uint32_t pos = lower_bound_cnt(g.col, S.blo[d][b], re, x, bytes, g.m2);
         bool hit = false;
         const uint8_t want = P.el[w][b];
         while (pos < re && TFSM_IN(6, pos, g.m2) && __ldg(g.col + pos) == x) {  // parallel edges: any with the label
@@ -367,9 +384,9 @@ __device__ __forceinline__ bool check_candidate(const Graph &g, const WarpPlan &
 // Depth-first search for one embedding that extends S.emb[order[0]].  Depth 1 scans positions
 // [lo1, hi1) of its anchor list when `slice` is set.  Returns kAbort once `budget` chunk
 // evaluations are exceeded (budget 0: unlimited).
-__device__ int dfs(const Graph &g, const WarpPlan &P, WarpState &S, const uint32_t *__restrict__ dom, uint32_t lane,
-                   bool slice, uint32_t lo1, uint32_t hi1, uint32_t budget, uint32_t &steps, int &abort_depth,
-                   uint32_t &bytes) {
+__device__ __forceinline__ int dfs(const Graph &g, const WarpPlan &P, WarpState &S, const uint32_t *__restrict__ dom,
+                   const uint32_t *found, const uint32_t *failed, uint32_t lane, bool slice, uint32_t lo1,
+                   uint32_t hi1, uint32_t budget, uint32_t &steps, int &abort_depth, uint32_t &bytes) {
     const int n = P.n;
     setup_depth(g, P, S, 1, lane, bytes);
     if (slice) {
@@ -381,11 +398,11 @@ __device__ int dfs(const Graph &g, const WarpPlan &P, WarpState &S, const uint32
     }
     int d = 1;
     for (;;) {
-        const uint32_t m = S.mask[d];
+        const uint32_t mk = S.mask[d], mr = S.rest[d];
         const uint32_t pos = S.pos[d], end = S.end[d];
         // every lane has read this depth's state before lane 0 may overwrite it below
         __syncwarp();
-        if (m == 0) {
+        if ((mk | mr) == 0) {
             if (pos >= end) {
                 if (d == 1) return kFail;
                 --d;
@@ -397,8 +414,10 @@ __device__ int dfs(const Graph &g, const WarpPlan &P, WarpState &S, const uint32
             }
             const uint32_t idx = pos + lane;
             uint32_t x = 0;
-            const bool ok = idx < end && check_candidate(g, P, S, dom, d, idx, x, bytes);
+            bool known = false;
+            const bool ok = idx < end && check_candidate(g, P, S, dom, found, failed, d, idx, x, known, bytes);
             const uint32_t bal = __ballot_sync(0xffffffffu, ok);
+            const uint32_t pref = kFoundFirst ? __ballot_sync(0xffffffffu, ok && known) : 0u;
             ++steps;
             if (d == n - 1) {
                 if (bal) {
@@ -413,14 +432,19 @@ __device__ int dfs(const Graph &g, const WarpPlan &P, WarpState &S, const uint32
             if (lane == 0) {
                 S.base[d] = pos;
                 S.pos[d] = pos + 32;
-                S.mask[d] = bal;
+                S.mask[d] = pref;
+                S.rest[d] = bal & ~pref;
             }
             __syncwarp();
             continue;
         }
+        // candidates known to be in w's MNI domain first: they usually complete an embedding
+        const bool from_pref = mk != 0;
+        const uint32_t m = from_pref ? mk : mr;
         const int i = __ffs(m) - 1;
         if (lane == 0) {
-            S.mask[d] = m & (m - 1);
+            if (from_pref) S.mask[d] = m & (m - 1);
+            else S.rest[d] = m & (m - 1);
             if (TFSM_IN(7, S.base[d] + i, g.m2)) S.emb[P.order[d]] = __ldg(g.col + S.base[d] + i);
         }
         __syncwarp();
@@ -536,7 +560,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
         if (!TFSM_IN(12, p, prm.n_pats) || !TFSM_IN(20, u, kMaxN)) continue;
         load_plan(P, descs[p], p, u, lane, prm.words);
         PatStatus &ps = st[p];
-        unsigned long long n_search = 0, n_steps = 0, n_bytes = 0;
+        unsigned long long n_search = 0, n_steps = 0, n_bytes = 0, max_steps = 0;
         bool stop = false;
         for (uint32_t word = item.word_lo; word < item.word_hi && !stop; ++word) {
             if (pattern_stops(ps, u, exact, lane)) break;
@@ -557,7 +581,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
                 uint32_t steps = 0, bytes = 12;  // + domain, found and failed words of v
                 int adepth = 0;
                 ++n_search;
-                int r = dfs(g, P, S, dom, lane, false, 0, 0, prm.step_budget, steps, adepth, bytes);
+                int r = dfs(g, P, S, dom, found, failed, lane, false, 0, 0, prm.step_budget, steps, adepth, bytes);
                 if (r == kAbort) {
                     // Hub splitting: cut the unexplored depth-1 range into slices for k_split.  An
                     // abort at depth 1 has fully explored every position before pos[1]; deeper, the
@@ -608,9 +632,10 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
                     // buffers full: finish this task here without a budget
                     if (lane == 0) S.emb[u] = v;
                     __syncwarp();
-                    r = dfs(g, P, S, dom, lane, false, 0, 0, 0, steps, adepth, bytes);
+                    r = dfs(g, P, S, dom, found, failed, lane, false, 0, 0, 0, steps, adepth, bytes);
                 }
                 n_steps += steps;
+                max_steps = steps > max_steps ? steps : max_steps;
                 n_bytes += __reduce_add_sync(0xffffffffu, bytes);
                 if (r == kFound) mark_found(P, S, ps, found, prm.tau, exact, lane);
                 else mark_failed(P, ps, failed, u, v, prm.tau, exact, lane);
@@ -620,6 +645,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
             atomicAdd(&ps.searches, n_search);
             atomicAdd(&ps.steps, n_steps);
             atomicAdd(&ps.bytes, n_bytes);
+            atomicMax(&ps.max_steps, max_steps);
         }
     }
 }
@@ -667,7 +693,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_split(Graph g, const PatD
             __syncwarp();
             uint32_t steps = 0, bytes = 12;
             int adepth = 0;
-            const int r = dfs(g, P, S, dom, lane, true, t.lo, t.hi, 0, steps, adepth, bytes);
+            const int r = dfs(g, P, S, dom, found, failed, lane, true, t.lo, t.hi, 0, steps, adepth, bytes);
             if (r == kFound) mark_found(P, S, ps, found, prm.tau, exact, lane);
             const unsigned long long wb = __reduce_add_sync(0xffffffffu, bytes);
             if (lane == 0) {

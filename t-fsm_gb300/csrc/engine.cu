@@ -73,7 +73,7 @@ size_t Level::size() const { return impl ? impl->hdescs.size() : 0; }
 
 struct GpuEngine::Impl {
     dev::Graph g;
-    DevBuf<uint32_t> row_off, col, label_start;
+    DevBuf<uint32_t> row_off, col, label_start, lab_off;
     DevBuf<uint8_t> elab;
     std::map<int, int> vdense, edense;
     std::vector<uint32_t> lstart;  // host copy, n_labels + 1
@@ -137,6 +137,19 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
             fill[y]++;
         }
     }
+    // per-vertex label offsets: lab_off[x * (NL + 1) + L] = first position of a neighbour >= label L
+    const size_t stride = (size_t)NL + 1;
+    if ((size_t)lg.n * stride >= (1ull << 34)) throw EngineError(5, "label-offset table too large");
+    std::vector<uint32_t> lab_off((size_t)lg.n * stride);
+    for (uint32_t x = 0; x < lg.n; ++x) {
+        uint32_t pos = off[x];
+        const uint32_t end = off[(size_t)x + 1];
+        for (int L = 0; L <= NL; ++L) {
+            const uint32_t first = I.lstart[(size_t)L];  // lstart[NL] == n: past every id
+            while (pos < end && col[pos] < first) ++pos;
+            lab_off[(size_t)x * stride + (size_t)L] = L == NL ? end : pos;
+        }
+    }
     I.n = lg.n;
     I.m2 = off[lg.n];
     TFSM_CK(cudaStreamCreateWithFlags(&I.stream, cudaStreamNonBlocking));
@@ -146,6 +159,9 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     I.col.ensure(col.size());
     I.elab.ensure(el.size());
     I.label_start.ensure(I.lstart.size());
+    I.lab_off.ensure(lab_off.size());
+    if (!lab_off.empty())
+        TFSM_CK(cudaMemcpyAsync(I.lab_off.p, lab_off.data(), lab_off.size() * 4, cudaMemcpyHostToDevice, I.stream));
     TFSM_CK(cudaMemcpyAsync(I.row_off.p, off.data(), off.size() * 4, cudaMemcpyHostToDevice, I.stream));
     if (!col.empty()) {
         TFSM_CK(cudaMemcpyAsync(I.col.p, col.data(), col.size() * 4, cudaMemcpyHostToDevice, I.stream));
@@ -161,6 +177,8 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     I.g.col = I.col.p;
     I.g.elab = I.elab.p;
     I.g.label_start = I.label_start.p;
+    I.g.lab_off = I.lab_off.p;
+    I.g.lab_stride = (uint32_t)stride;
     I.counters.ensure(4);
     I.splits.ensure(1u << 20);
     I.groups.ensure(1u << 17);
@@ -176,7 +194,9 @@ GpuEngine::~GpuEngine() {
     }
 }
 
-uint64_t GpuEngine::graph_bytes() const { return (uint64_t)(impl_->n + 1) * 4 + impl_->m2 * 5; }
+uint64_t GpuEngine::graph_bytes() const {
+    return (uint64_t)(impl_->n + 1) * 4 + impl_->m2 * 5 + (uint64_t)impl_->n * impl_->lstart.size() * 4;
+}
 uint32_t GpuEngine::n_vertices() const { return impl_->n; }
 int GpuEngine::dense_label(int label) const {
     auto it = impl_->vdense.find(label);
@@ -413,34 +433,49 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     TFSM_CK(cudaMemcpyAsync(L.descs.p, L.hdescs.data(), P * sizeof(PatDesc), cudaMemcpyHostToDevice, I.stream));
     times_.h2d_bytes += P * sizeof(PatDesc);
 
-    // ---- search items, interleaved across patterns and representatives ----
+    // ---- search items ----
+    // Vertex-major, as the reference evaluates one pattern vertex after another
+    // (parallel/comper.h:1181-1239): every pattern first searches its representative with the
+    // smallest domain (an infrequent pattern usually dies there), then the next one, whose
+    // candidates are by then largely marked found by the earlier embeddings.  Within one rank the
+    // chunks of all patterns are interleaved so that every pattern progresses and early exit cuts
+    // the rest.
     std::vector<dev::SearchItem> items;
     {
         struct Q {
             uint32_t p, u, w, words;
         };
-        std::vector<Q> qs;
+        std::vector<std::vector<Q>> ranks;  // ranks[k]: the k-th smallest representative of each pattern
         for (size_t p = 0; p < P; ++p) {
             if (!need_search[p]) continue;
             const PatDesc &D = L.hdescs[p];
+            std::vector<int> reps;
             for (int u = 0; u < D.n; ++u)
-                if (D.rep[u] == u) qs.push_back({(uint32_t)p, (uint32_t)u, 0, D.words[u]});
+                if (D.rep[u] == u) reps.push_back(u);
+            const PatStatus &s = I.hstatus[p];
+            std::stable_sort(reps.begin(), reps.end(), [&](int a, int b) { return s.dom_size[a] < s.dom_size[b]; });
+            for (size_t k = 0; k < reps.size(); ++k) {
+                if (ranks.size() <= k) ranks.emplace_back();
+                ranks[k].push_back({(uint32_t)p, (uint32_t)reps[k], 0, D.words[reps[k]]});
+            }
         }
         const uint32_t cw = std::max<uint32_t>(1, opt.chunk_words);
-        bool more = true;
-        while (more) {
-            more = false;
-            for (Q &q : qs) {
-                if (q.w >= q.words) continue;
-                dev::SearchItem it;
-                it.pat = q.p;
-                it.u = (uint16_t)q.u;
-                it.pad = 0;
-                it.word_lo = q.w;
-                it.word_hi = std::min(q.words, q.w + cw);
-                q.w = it.word_hi;
-                items.push_back(it);
-                more = true;
+        for (auto &qs : ranks) {
+            bool more = true;
+            while (more) {
+                more = false;
+                for (Q &q : qs) {
+                    if (q.w >= q.words) continue;
+                    dev::SearchItem it;
+                    it.pat = q.p;
+                    it.u = (uint16_t)q.u;
+                    it.pad = 0;
+                    it.word_lo = q.w;
+                    it.word_hi = std::min(q.words, q.w + cw);
+                    q.w = it.word_hi;
+                    items.push_back(it);
+                    more = true;
+                }
             }
         }
     }
@@ -482,6 +517,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         EvalResult &r = res[p];
         r.searches = s.searches;
         r.steps = s.steps;
+        r.max_steps = s.max_steps;
         times_.search_bytes += s.bytes;
         uint32_t mn = UINT32_MAX;
         bool all_reps = true;

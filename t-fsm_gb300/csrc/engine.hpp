@@ -28,6 +28,7 @@ struct EvalResult {
     uint32_t support = 0;              // min over vertices of mni
     uint64_t searches = 0;             // candidate checks
     uint64_t steps = 0;                // 32-candidate chunks evaluated by the search
+    uint64_t max_steps = 0;            // longest single search of the pattern (chunk evaluations)
 };
 
 struct EngineOptions {
@@ -36,6 +37,8 @@ struct EngineOptions {
     uint32_t split_slice = 256;        // depth-1 anchor positions per split slice
     uint32_t chunk_words = 4;          // bitmap words per search work item (x32 candidates)
     uint32_t refine_rounds = 2;        // arc-consistency passes for patterns that need search
+    uint32_t max_batch = 4096;         // miner: patterns per engine call
+    double time_limit_s = 0;           // miner: stop between engine calls after this long (0: none)
 };
 
 struct KernelTimes {                   // accumulated device time (CUDA events), milliseconds

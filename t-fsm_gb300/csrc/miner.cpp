@@ -3,6 +3,8 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <fstream>
 #include <memory>
 #include <thread>
@@ -56,39 +58,77 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
         ctx.neighbor_labels[ep.lb].insert(ep.la);
     }
     const uint32_t tau = (uint32_t)std::max(opt.tau, 0);
+    const bool verbose = std::getenv("TFSM_VERBOSE") != nullptr;  // per-engine-call summary on stderr
 
     // Levels own device memory; a level is released once its children are evaluated.
     std::vector<std::unique_ptr<Level>> prev_levels, cur_levels;
 
+    auto out_of_time = [&]() {
+        if (opt.engine.time_limit_s <= 0) return false;
+        const double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (s > opt.engine.time_limit_s) st.complete = false;
+        return !st.complete;
+    };
+    // Evaluates a level's candidates.  Batched: consecutive candidates go into one engine call,
+    // at most max_batch of them, and never mixing parents held by different device levels (an
+    // engine call reads its parents' domains from one level).  Candidates left when the time
+    // limit stops the run are dropped.
     auto evaluate_level = [&](std::vector<Node> &nodes, const std::vector<int> &parent_of,
                               const std::vector<Node> *parents) {
         if (nodes.empty()) return;
-        st.evaluations += nodes.size();
         if (opt.batched) {
-            std::vector<const Pattern *> pats;
-            std::vector<int> par;
-            const Level *prev = nullptr;
-            for (size_t i = 0; i < nodes.size(); ++i) {
-                pats.push_back(&nodes[i].pat);
-                if (parents && parent_of[i] >= 0) {
-                    const Node &pn = (*parents)[(size_t)parent_of[i]];
-                    par.push_back(pn.idx);
-                    prev = pn.lvl;  // one level object for the whole parent level
-                } else {
-                    par.push_back(-1);
+            const size_t step = std::max<size_t>(1, opt.engine.max_batch);
+            auto parent_level = [&](size_t i) -> const Level * {
+                return (parents && parent_of[i] >= 0) ? (*parents)[(size_t)parent_of[i]].lvl : nullptr;
+            };
+            size_t b0 = 0;
+            while (b0 < nodes.size()) {
+                if (out_of_time()) {
+                    nodes.resize(b0);
+                    break;
                 }
-            }
-            cur_levels.emplace_back(new Level);
-            std::vector<EvalResult> res;
-            eng.evaluate(pats, par, prev, tau, opt.engine, *cur_levels.back(), res);
-            st.engine_calls++;
-            for (size_t i = 0; i < nodes.size(); ++i) {
-                nodes[i].res = std::move(res[i]);
-                nodes[i].lvl = cur_levels.back().get();
-                nodes[i].idx = (int)i;
+                const Level *prev = parent_level(b0);
+                size_t b1 = b0 + 1;
+                while (b1 < nodes.size() && b1 - b0 < step && parent_level(b1) == prev) ++b1;
+                std::vector<const Pattern *> pats;
+                std::vector<int> par;
+                for (size_t i = b0; i < b1; ++i) {
+                    pats.push_back(&nodes[i].pat);
+                    par.push_back(prev ? (*parents)[(size_t)parent_of[i]].idx : -1);
+                }
+                cur_levels.emplace_back(new Level);
+                std::vector<EvalResult> res;
+                const double search_before = eng.times().search_ms;
+                eng.evaluate(pats, par, prev, tau, opt.engine, *cur_levels.back(), res);
+                st.engine_calls++;
+                st.evaluations += b1 - b0;
+                if (verbose) {
+                    uint64_t mx = 0, srch = 0, nf = 0;
+                    for (auto &r : res) {
+                        mx = std::max<uint64_t>(mx, r.max_steps);
+                        srch += r.searches;
+                        nf += r.frequent ? 1 : 0;
+                    }
+                    std::fprintf(stderr,
+                                 "[level %d] %zu patterns (%llu frequent), search %.3f ms, %llu searches, longest "
+                                 "search %llu chunk steps\n",
+                                 st.levels + 1, b1 - b0, (unsigned long long)nf, eng.times().search_ms - search_before,
+                                 (unsigned long long)srch, (unsigned long long)mx);
+                }
+                for (size_t i = b0; i < b1; ++i) {
+                    nodes[i].res = std::move(res[i - b0]);
+                    nodes[i].lvl = cur_levels.back().get();
+                    nodes[i].idx = (int)(i - b0);
+                }
+                b0 = b1;
             }
         } else {
             for (size_t i = 0; i < nodes.size(); ++i) {
+                if (out_of_time()) {
+                    nodes.resize(i);
+                    break;
+                }
+                st.evaluations++;
                 std::vector<const Pattern *> pats{&nodes[i].pat};
                 std::vector<int> par{-1};
                 const Level *prev = nullptr;

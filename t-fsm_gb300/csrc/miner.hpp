@@ -40,6 +40,7 @@ struct MineStats {
     uint64_t by_filter = 0;         // decided without search
     uint64_t engine_calls = 0;
     int levels = 0;
+    bool complete = true;           // false when the time limit stopped the run
 };
 
 // Mines all frequent patterns; `out` lists them level by level in generation order.

@@ -1,7 +1,8 @@
 // `run`: command-line drop-in for the reference miners (parallel/run.cpp:11-82, serial/run.cpp).
 //
 //   run -file G.lg -freq TAU [-thread T] [-maxNodes N] [-plain] [-exact] [-out PATH]
-//       [-step-budget B] [-split-slice S] [-chunk-words W] [-refine-rounds R]
+//       [-step-budget B] [-split-slice S] [-chunk-words W] [-refine-rounds R] [-max-batch M]
+//       [-time-limit SECONDS]
 //
 // Frequent patterns go to ./grami_results.txt (or -out PATH) in the serial build's format
 // (serial/grami.h:622-635); timing and counts are printed as the parallel build prints them.
@@ -52,6 +53,8 @@ int main(int argc, char **argv) {
     if (opt(argc, argv, "-split-slice")) o.split_slice = (uint32_t)std::atoi(opt(argc, argv, "-split-slice"));
     if (opt(argc, argv, "-chunk-words")) o.chunk_words = (uint32_t)std::atoi(opt(argc, argv, "-chunk-words"));
     if (opt(argc, argv, "-refine-rounds")) o.refine_rounds = (uint32_t)std::atoi(opt(argc, argv, "-refine-rounds"));
+    if (opt(argc, argv, "-max-batch")) o.max_batch = (uint32_t)std::atoi(opt(argc, argv, "-max-batch"));
+    if (opt(argc, argv, "-time-limit")) o.time_limit_s = std::atof(opt(argc, argv, "-time-limit"));
     rc = tfsm_set_options(g, &o);
     if (rc != TFSM_OK) {
         std::fprintf(stderr, "error %d: %s\n", rc, tfsm_last_error());
@@ -74,6 +77,7 @@ int main(int argc, char **argv) {
     std::printf("[INFO] # Searches: %llu, # Chunk steps: %llu, decided by filters: %llu, engine calls: %llu\n",
                 (unsigned long long)st.searches, (unsigned long long)st.steps, (unsigned long long)st.by_filter,
                 (unsigned long long)st.engine_calls);
+    if (!st.complete) std::printf("[INFO] TIME LIMIT REACHED: the run is incomplete\n");
     std::printf("[TIME] Device: init %.3f ms (%llu), refine %.3f ms (%llu), search %.3f ms (%llu), host extend %.3f ms\n",
                 st.init_ms, (unsigned long long)st.init_launches, st.refine_ms, (unsigned long long)st.refine_launches,
                 st.search_ms, (unsigned long long)st.search_launches, st.extend_ms);

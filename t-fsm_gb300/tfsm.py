@@ -73,7 +73,8 @@ class GraphInfoC(C.Structure):
 
 class OptionsC(C.Structure):
     _fields_ = [("step_budget", C.c_uint32), ("split_slice", C.c_uint32), ("chunk_words", C.c_uint32),
-                ("refine_rounds", C.c_uint32)]
+                ("refine_rounds", C.c_uint32), ("max_batch", C.c_uint32), ("reserved", C.c_uint32),
+                ("time_limit_s", C.c_double)]
 
 
 class MineStatsC(C.Structure):
@@ -84,7 +85,7 @@ class MineStatsC(C.Structure):
                 ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
                 ("evaluations", C.c_uint64), ("frequent", C.c_uint64), ("searches", C.c_uint64),
                 ("steps", C.c_uint64), ("by_filter", C.c_uint64), ("engine_calls", C.c_uint64),
-                ("levels", C.c_int32)]
+                ("levels", C.c_int32), ("complete", C.c_int32)]
 
 
 _lib = None

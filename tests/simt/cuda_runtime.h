@@ -254,6 +254,12 @@ inline unsigned long long atomicAdd(unsigned long long *p, unsigned long long v)
 inline unsigned atomicSub(unsigned *p, unsigned v) { return __atomic_fetch_sub(p, v, __ATOMIC_RELAXED); }
 inline unsigned atomicOr(unsigned *p, unsigned v) { return __atomic_fetch_or(p, v, __ATOMIC_RELAXED); }
 inline unsigned atomicAnd(unsigned *p, unsigned v) { return __atomic_fetch_and(p, v, __ATOMIC_RELAXED); }
+inline unsigned long long atomicMax(unsigned long long *p, unsigned long long v) {
+    unsigned long long cur = __atomic_load_n(p, __ATOMIC_RELAXED);
+    while (cur < v && !__atomic_compare_exchange_n(p, &cur, v, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
+    }
+    return cur;
+}
 inline unsigned atomicCAS(unsigned *p, unsigned cmp, unsigned val) {
     __atomic_compare_exchange_n(p, &cmp, val, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED);
     return cmp;

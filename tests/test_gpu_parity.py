@@ -70,6 +70,31 @@ def test_mining_with_forced_hub_splits_matches_reference(tfsm, graphs, case, tmp
     assert pats == golden_pattern_set(case)
 
 
+@pytest.mark.parametrize("case", ["cfg1", "el3", "clique"])
+def test_mining_in_small_batches_matches_reference(tfsm, graphs, case, tmp_path):
+    """Levels cut into many engine calls (each reading its parents from one device level)."""
+    g = graphs(case)
+    saved = g.options()
+    try:
+        g.set_options(max_batch=5)
+        pats, st = mine_set(tfsm, g, case, tmp_path)
+    finally:
+        g.set_options(**saved)
+    assert pats == golden_pattern_set(case)
+    assert st["complete"] == 1
+
+
+def test_time_limit_stops_between_engine_calls(tfsm, graphs, tmp_path):
+    g = graphs("cfg1")
+    saved = g.options()
+    try:
+        g.set_options(max_batch=1, time_limit_s=1e-6)
+        pats, st = mine_set(tfsm, g, "cfg1", tmp_path)
+    finally:
+        g.set_options(**saved)
+    assert st["complete"] == 0 and pats <= golden_pattern_set("cfg1")
+
+
 @pytest.mark.parametrize("case", [n for n in ALL if golden_mni(n)])
 @pytest.mark.parametrize("flags", [0, 4])  # with and without splitting
 def test_exact_mni_matches_reference_engine(tfsm, graphs, case, flags):

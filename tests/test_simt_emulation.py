@@ -28,7 +28,7 @@ def emu():
 
 
 OPTS = {"default": [], "split": ["-step-budget", "1", "-split-slice", "32", "-chunk-words", "1"],
-        "plain": ["-plain", "-refine-rounds", "1"], "exact": ["-exact"]}
+        "plain": ["-plain", "-refine-rounds", "1"], "exact": ["-exact"], "batch3": ["-max-batch", "3"]}
 RUNS = [(c, o) for c in SMALL for o in OPTS if not (o == "plain" and c == "quirk_elabels")]
 
 
