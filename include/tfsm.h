@@ -124,15 +124,19 @@ int tfsm_mine(tfsm_graph *g, int32_t tau, int32_t max_nodes, uint32_t flags, con
  * compile-time TIMEOUT_THRESHOLD / DECOMPOSE_TIME_THRESHOLD of parallel/global.h:30-33).
  * They change speed only, never results. */
 typedef struct {
-    uint32_t step_budget;   /* 32-candidate chunks a search may evaluate before its remaining
-                               depth-1 branches are split into slices (0: never split) */
-    uint32_t split_slice;   /* depth-1 adjacency positions per slice (>= 32) */
+    uint32_t step_budget;   /* 32-candidate chunks a search may evaluate before its unexplored
+                               branches (at every depth) become split tasks (0: never split) */
+    uint32_t split_slice;   /* adjacency positions per split task (>= 32) */
     uint32_t chunk_words;   /* 32-bit domain-bitmap words per search work item (>= 1) */
     uint32_t refine_rounds; /* arc-consistency passes for patterns that need a search (>= 1) */
     uint32_t max_batch;     /* tfsm_mine: most patterns per engine call (>= 1) */
-    uint32_t reserved;
+    uint32_t split_rounds;  /* split rounds launched right after the search pass (1..64); later rounds
+                               run while tasks remain (64 rounds at most, the last without a budget) */
     double time_limit_s;    /* tfsm_mine: stop between engine calls after this many seconds (0: none);
                                the run is then reported incomplete */
+    uint32_t round_budget;  /* chunk evaluations of a split task before its own remainder is split
+                               again (>= 1) */
+    uint32_t reserved;
 } tfsm_options;
 
 int tfsm_get_options(const tfsm_graph *g, tfsm_options *opt);

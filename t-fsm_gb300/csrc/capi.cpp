@@ -266,8 +266,10 @@ int tfsm_get_options(const tfsm_graph *g, tfsm_options *o) {
         o->chunk_words = g->opt.chunk_words;
         o->refine_rounds = g->opt.refine_rounds;
         o->max_batch = g->opt.max_batch;
-        o->reserved = 0;
+        o->split_rounds = g->opt.split_rounds;
         o->time_limit_s = g->opt.time_limit_s;
+        o->round_budget = g->opt.round_budget;
+        o->reserved = 0;
         return TFSM_OK;
     });
 }
@@ -276,9 +278,10 @@ int tfsm_set_options(tfsm_graph *g, const tfsm_options *o) {
     return guarded([&]() -> int {
         if (!g || !o) return fail(TFSM_ERR_ARG, "null argument");
         if (o->split_slice < 32 || o->chunk_words < 1 || o->refine_rounds < 1 || o->max_batch < 1 ||
-            !(o->time_limit_s >= 0))
+            o->split_rounds < 1 || o->split_rounds > 64 || o->round_budget < 1 || !(o->time_limit_s >= 0))
             return fail(TFSM_ERR_ARG,
-                        "split_slice must be >= 32; chunk_words, refine_rounds and max_batch >= 1; time_limit_s >= 0");
+                        "split_slice must be >= 32; chunk_words, refine_rounds, max_batch and round_budget >= 1; "
+                        "split_rounds in 1..64; time_limit_s >= 0");
         std::lock_guard<std::mutex> lk(g->mu);
         g->opt.step_budget = o->step_budget;
         g->opt.split_slice = o->split_slice;
@@ -286,6 +289,8 @@ int tfsm_set_options(tfsm_graph *g, const tfsm_options *o) {
         g->opt.refine_rounds = o->refine_rounds;
         g->opt.max_batch = o->max_batch;
         g->opt.time_limit_s = o->time_limit_s;
+        g->opt.split_rounds = o->split_rounds;
+        g->opt.round_budget = o->round_budget;
         return TFSM_OK;
     });
 }

@@ -83,34 +83,58 @@ struct SearchItem {
     uint32_t word_hi;
 };
 
-// Split task produced when a search exceeds its step budget: the depth-1 anchor range of
-// candidate v of representative u is cut into slices that are searched independently.
+// Split task: an unexplored part of one (u, v) search — the candidates at positions [lo, hi) of the
+// anchor list at `depth`, below the partial embedding prefix[0..depth-1] (data vertices of the
+// pattern vertices order[0..depth-1] of u's matching order).  A search that exceeds its step budget
+// turns its whole unexplored remainder, at every depth, into such tasks (parallel/comper.h:640-749
+// spawns every remaining branch with its partial embedding the same way).
 struct SplitTask {
     uint32_t pat;
     uint16_t u;
-    uint16_t pad;
-    uint32_t v;          // candidate of u (data vertex id)
-    uint32_t lo, hi;     // slice of the depth-1 anchor adjacency positions (absolute)
-    uint32_t group;      // index of the split group (pending counter)
+    uint8_t depth;
+    uint8_t pad;
+    uint32_t v;              // candidate of u: the search this task belongs to
+    uint32_t lo, hi;         // anchor positions at `depth`
+    uint32_t group;          // index of the group that decides v
+    uint32_t prefix[kMaxN];  // prefix[k] = data vertex of order[k], k < depth
 };
+
+// All tasks of one (u, v) search; the last task to finish decides v when none found an embedding.
+constexpr uint32_t kNullTask = 0xffffffffu;  // SplitTask::pat of a slot that holds no task
 
 struct SplitGroup {
     uint32_t pat;
     uint16_t u;
     uint16_t pad;
     uint32_t v;
-    uint32_t pending;    // slices not yet finished
-    uint32_t incomplete; // a slice was skipped (pattern decided): failure cannot be concluded
+    uint32_t pending;    // tasks not yet finished
+    uint32_t incomplete; // a task was skipped (pattern decided): failure cannot be concluded
 };
+
+// Split rounds after the first search pass: every round but the last possible one (kMaxRounds - 1)
+// has a step budget, so a task keeps being cut until the queue drains.
+constexpr int kMaxRounds = 64;
+// counters of one search pass: [0] next item, [1] groups used, [2 + r] tasks written for round r
+// (may pass the buffer capacity; readers clamp), [kClaimBase + r] next task of round r to process,
+// [kDeferred] searches deferred to the next pass
+constexpr int kClaimBase = 2 + kMaxRounds + 1;
+constexpr int kDeferred = kClaimBase + kMaxRounds + 1;
+constexpr int kNumCounters = kDeferred + 1;
 
 struct SearchParams {
     uint32_t tau;
     uint32_t exact;          // 1: evaluate every candidate, no early exit
     uint32_t n_items;
-    uint32_t step_budget;    // chunk evaluations before a task is split (0: never split)
-    uint32_t split_slice;    // anchor positions per split slice
-    uint32_t split_cap;      // capacity of the split-task output buffer
+    uint32_t step_budget;    // chunk evaluations before a search is split (0: never split)
+    uint32_t split_slice;    // anchor positions per split task
+    uint32_t split_cap;      // capacity of each of the two split-task buffers
+    uint32_t split_slack;    // slots above a sliced-claim limit, kept for compact remainders
+    uint32_t search_fill;    // sliced-claim limit of the search pass (the split rounds use
+                             //    split_cap - split_slack): the rounds' tasks can outnumber it
     uint32_t group_cap;      // capacity of the split-group buffer
+    uint32_t round_budget;   // step budget of every split round but round kMaxRounds - 1
+    uint32_t defer;          // 1: a search whose remainder finds no room is left undecided for the
+                             //    next pass; 0: it finishes in place without a budget
     uint32_t n_pats;         // patterns of the batch
     uint64_t words;          // size of each level bitmap pool (32-bit words)
 };

@@ -256,7 +256,19 @@ struct WarpState {
     uint32_t bhi[kMaxN][kMaxN];  //   label inside emb[b]'s adjacency
 };
 
-enum : int { kFail = 0, kFound = 1, kAbort = 2 };
+enum : int { kFail = 0, kFound = 1, kAbort = 2, kCancel = 3 };
+
+// What makes a running search pointless: the searched (u, v) has been found by another warp's
+// embedding, or the pattern (or, lazily, vertex u) has been decided.  Checked every kCancelEvery
+// chunk steps; a cancelled search proves nothing about v.
+struct Cancel {
+    const uint32_t *found_word;  // found-bitmap word holding (u, v)
+    uint32_t bit;
+    const PatStatus *ps;
+    int u;
+    bool exact;
+};
+constexpr uint32_t kCancelEvery = 16;
 
 // Try candidates already known to be in w's MNI domain first.  Measured slower on the benchmark
 // graphs (the extra ballot and found-word loads cost more than the reordering saves): off.
@@ -381,22 +393,25 @@ __device__ __forceinline__ bool check_candidate(const Graph &g, const WarpPlan &
     return true;
 }
 
-// Depth-first search for one embedding that extends S.emb[order[0]].  Depth 1 scans positions
-// [lo1, hi1) of its anchor list when `slice` is set.  Returns kAbort once `budget` chunk
-// evaluations are exceeded (budget 0: unlimited).
+// Depth-first search for one embedding that extends the partial embedding of depths < start
+// (S.emb[order[0..start-1]]).  With `slice`, depth `start` scans only anchor positions [lo, hi).
+// The search never backtracks above `start`.  Returns kAbort once `budget` chunk evaluations are
+// exceeded (budget 0: unlimited); `abort_depth` then says where it stopped.  Returns kCancel when
+// `cancel` says the search no longer matters.
 __device__ __forceinline__ int dfs(const Graph &g, const WarpPlan &P, WarpState &S, const uint32_t *__restrict__ dom,
-                   const uint32_t *found, const uint32_t *failed, uint32_t lane, bool slice, uint32_t lo1,
-                   uint32_t hi1, uint32_t budget, uint32_t &steps, int &abort_depth, uint32_t &bytes) {
+                                   const uint32_t *found, const uint32_t *failed, uint32_t lane, int start, bool slice,
+                                   uint32_t lo, uint32_t hi, uint32_t budget, const Cancel &cancel, uint32_t &steps,
+                                   int &abort_depth, uint32_t &bytes) {
     const int n = P.n;
-    setup_depth(g, P, S, 1, lane, bytes);
+    setup_depth(g, P, S, start, lane, bytes);
     if (slice) {
         if (lane == 0) {
-            S.pos[1] = lo1;
-            S.end[1] = hi1;
+            S.pos[start] = lo;
+            S.end[start] = hi;
         }
         __syncwarp();
     }
-    int d = 1;
+    int d = start;
     for (;;) {
         const uint32_t mk = S.mask[d], mr = S.rest[d];
         const uint32_t pos = S.pos[d], end = S.end[d];
@@ -404,13 +419,21 @@ __device__ __forceinline__ int dfs(const Graph &g, const WarpPlan &P, WarpState 
         __syncwarp();
         if ((mk | mr) == 0) {
             if (pos >= end) {
-                if (d == 1) return kFail;
+                if (d == start) return kFail;
                 --d;
                 continue;
             }
             if (budget && steps >= budget) {
                 abort_depth = d;
                 return kAbort;
+            }
+            if (steps && steps % kCancelEvery == 0) {
+                int c = 0;
+                if (lane == 0) {
+                    c = (__ldcg(cancel.found_word) & cancel.bit) || __ldcg(&cancel.ps->state) != kRunning ||
+                        (!cancel.exact && ((__ldcg(&cancel.ps->done_mask) >> cancel.u) & 1u));
+                }
+                if (__shfl_sync(0xffffffffu, c, 0)) return kCancel;
             }
             const uint32_t idx = pos + lane;
             uint32_t x = 0;
@@ -453,6 +476,90 @@ __device__ __forceinline__ int dfs(const Graph &g, const WarpPlan &P, WarpState 
         ++d;
         setup_depth(g, P, S, d, lane, bytes);
     }
+}
+
+// Claims `k` consecutive slots below `limit` with one atomicAdd (no retry loop, so no spurious
+// failure under contention); false when they do not all fit.  The counter may then pass `limit`
+// (readers clamp it to the buffer size); a failed claim [first, first + k) still owns its slots
+// that lie inside the buffer and must fill them (split tasks: with null tasks).  A counter already
+// at `limit` is not advanced, so it passes `limit` by at most one claim per running warp.
+__device__ __forceinline__ bool reserve(uint32_t *counter, uint32_t k, uint32_t limit, uint32_t &first) {
+    if (__ldcg(counter) >= limit) {
+        first = 0xffffffffu;
+        return false;
+    }
+    first = atomicAdd(counter, k);
+    return first <= limit && k <= limit - first;
+}
+
+// Unexplored anchor positions left at depth j of a search that stopped at depth `dabort`: the
+// not-yet-taken candidates of j's current chunk, then [pos[j], end[j]).  Candidates of a chunk are
+// taken lowest position first, so everything below the lowest pending one is explored.
+__device__ __forceinline__ void remainder_at(const WarpState &S, int j, int dabort, uint32_t &from, uint32_t &to) {
+    to = S.end[j];
+    const uint32_t m = S.mask[j] | S.rest[j];
+    from = (j == dabort || m == 0) ? S.pos[j] : S.base[j] + (uint32_t)(__ffs(m) - 1);
+    if (from > to) from = to;
+}
+
+// Warp-uniform claim of `k` slots below `limit`; the slots of a failed claim inside the buffer
+// (`cap`) become null tasks.
+__device__ __forceinline__ bool claim_tasks(SplitTask *out, uint32_t *out_count, uint32_t k, uint32_t limit,
+                                            uint32_t cap, uint32_t lane, uint32_t &t0) {
+    int ok = 0;
+    if (lane == 0) ok = reserve(out_count, k, limit, t0) ? 1 : 0;
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    t0 = __shfl_sync(0xffffffffu, t0, 0);
+    if (!ok && t0 < cap) {
+        const uint32_t e = (uint64_t)t0 + k < cap ? t0 + k : cap;
+        for (uint32_t q = t0 + lane; q < e; q += 32) out[q].pat = kNullTask;
+    }
+    return ok != 0;
+}
+
+// Writes the unexplored remainder of the current search (depths start..dabort) as split tasks:
+// sliced (`slice` anchor positions each) below `limit`; when that does not fit, compact (one task
+// per depth, re-split by later rounds) below limit + slack.  Returns how many were written; 0 when
+// neither fits (then nothing is written).
+__device__ uint32_t emit_remainder(const WarpPlan &P, const WarpState &S, uint32_t p, int u, uint32_t v, int start,
+                                   int dabort, uint32_t group, uint32_t slice, SplitTask *out, uint32_t *out_count,
+                                   uint32_t cap, uint32_t limit, uint32_t slack, uint32_t lane, uint64_t m2) {
+    uint32_t total = 0, depths = 0;
+    for (int j = start; j <= dabort; ++j) {
+        uint32_t f, t;
+        remainder_at(S, j, dabort, f, t);
+        total += t > f ? (t - f - 1) / slice + 1 : 0u;
+        depths += t > f ? 1u : 0u;
+    }
+    if (total == 0) return 0;
+    uint32_t t0 = 0;
+    if (!claim_tasks(out, out_count, total, limit, cap, lane, t0)) {
+        if (!claim_tasks(out, out_count, depths, limit + slack, cap, lane, t0)) return 0;
+        slice = 0xffffffffu;  // compact: one task per non-empty depth
+        total = depths;
+    }
+    for (uint32_t k = lane; k < total; k += 32) {
+        uint32_t acc = 0, f = 0, t = 0, c = 0;
+        int j = start;
+        for (; j <= dabort; ++j) {
+            remainder_at(S, j, dabort, f, t);
+            c = t > f ? (t - f - 1) / slice + 1 : 0u;
+            if (k < acc + c) break;
+            acc += c;
+        }
+        SplitTask task;
+        task.pat = p;
+        task.u = (uint16_t)u;
+        task.depth = (uint8_t)j;
+        task.pad = 0;
+        task.v = v;
+        task.lo = f + (k - acc) * slice;  // k - acc is 0 when compact
+        task.hi = t - task.lo > slice ? task.lo + slice : t;
+        task.group = group;
+        for (int q = 0; q < kMaxN; ++q) task.prefix[q] = q < j ? S.emb[P.order[q]] : 0u;
+        if (TFSM_IN(14, t0 + k, cap) && TFSM_IN(48, task.hi, m2 + 1)) out[t0 + k] = task;
+    }
+    return total;
 }
 
 // Add every vertex of the embedding in S (and its automorphic images) to the found bitmaps.
@@ -512,25 +619,10 @@ __device__ __forceinline__ bool pattern_stops(const PatStatus &st, int u, bool e
 }
 
 
-// Reserve `k` consecutive slots of a bounded buffer; false when full (bounded retries).
-__device__ __forceinline__ bool reserve(uint32_t *counter, uint32_t k, uint32_t cap, uint32_t &first) {
-    uint32_t old = __ldcg(counter);
-    for (int attempt = 0; attempt < 64; ++attempt) {
-        if (old + k > cap || old + k < old) return false;
-        const uint32_t prev = atomicCAS(counter, old, old + k);
-        if (prev == old) {
-            first = old;
-            return true;
-        }
-        old = prev;
-    }
-    return false;
-}
-
 }  // namespace
 
-// counters[0]: next search item, [1]: split tasks written, [2]: split groups written,
-// [3]: next split task to process.
+// The search pass.  Counters: see kNumCounters in dev_common.cuh.  Split tasks of round 0 go to
+// `splits` (the first buffer).
 __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const PatDesc *__restrict__ descs,
                                                               PatStatus *__restrict__ st,
                                                               const SearchItem *__restrict__ items, SearchParams prm,
@@ -575,70 +667,61 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
                     stop = true;
                     break;
                 }
+                if (prm.defer && prm.step_budget) {
+                    // the first split round's share of the buffer is full: start no search that
+                    // might need it; the next pass takes v up
+                    int full = 0;
+                    if (lane == 0) full = __ldcg(&counters[2]) >= prm.search_fill;
+                    if (__shfl_sync(0xffffffffu, full, 0)) {
+                        if (lane == 0) atomicAdd(&counters[kDeferred], 1u);
+                        continue;
+                    }
+                }
                 const uint32_t v = P.lstart[u] + word * 32 + b;
                 if (lane == 0) S.emb[u] = v;
                 __syncwarp();
                 uint32_t steps = 0, bytes = 12;  // + domain, found and failed words of v
                 int adepth = 0;
                 ++n_search;
-                int r = dfs(g, P, S, dom, found, failed, lane, false, 0, 0, prm.step_budget, steps, adepth, bytes);
+                const Cancel cancel{found + o, 1u << b, &ps, u, exact};
+                int r = dfs(g, P, S, dom, found, failed, lane, 1, false, 0, 0, prm.step_budget, cancel, steps, adepth,
+                            bytes);
                 if (r == kAbort) {
-                    // Hub splitting: cut the unexplored depth-1 range into slices for k_split.  An
-                    // abort at depth 1 has fully explored every position before pos[1]; deeper, the
-                    // depth-1 chunk that is being explored restarts from its base.
-                    const uint32_t from = (adepth == 1) ? S.pos[1] : S.base[1];
-                    const uint32_t to = S.end[1];
-                    if (!TFSM_IN(40, from, (uint64_t)to + 1) || !TFSM_IN(41, to, (uint64_t)g.m2 + 1) ||
-                        !TFSM_IN(42, __ldg(g.row_off + v), (uint64_t)from + 1) ||
-                        !TFSM_IN(43, to, (uint64_t)__ldg(g.row_off + v + 1) + 1))
-                        continue;
-                    const uint32_t ns = (to - from + prm.split_slice - 1) / prm.split_slice;
-                    bool ok = false;
-                    uint32_t g0 = 0, t0 = 0;
-                    if (lane == 0) {
-                        ok = ns > 0 && reserve(&counters[2], 1, prm.group_cap, g0) && TFSM_IN(15, g0, prm.group_cap);
-                        if (ok && !reserve(&counters[1], ns, prm.split_cap, t0)) {
-                            ok = false;
-                            // the group slot stays unused: mark it so k_split never reads it
-                            groups[g0].pending = 0;
-                        }
-                        if (ok) {
-                            groups[g0].pat = p;
-                            groups[g0].u = (uint16_t)u;
-                            groups[g0].v = v;
-                            groups[g0].pending = ns;
-                            groups[g0].incomplete = 0;
-                        }
-                    }
-                    ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+                    // Hub splitting: the unexplored remainder becomes tasks for the split rounds,
+                    // grouped so that the last one to finish can decide v.
+                    uint32_t g0 = 0;
+                    int okg = 0;
+                    if (lane == 0)
+                        okg = reserve(&counters[1], 1, prm.group_cap, g0) && TFSM_IN(15, g0, prm.group_cap) ? 1 : 0;
+                    okg = __shfl_sync(0xffffffffu, okg, 0);
                     g0 = __shfl_sync(0xffffffffu, g0, 0);
-                    t0 = __shfl_sync(0xffffffffu, t0, 0);
-                    if (ok) {
-                        for (uint32_t k = lane; k < ns; k += 32) {
-                            SplitTask t;
-                            t.pat = p;
-                            t.u = (uint16_t)u;
-                            t.pad = 0;
-                            t.v = v;
-                            t.lo = from + k * prm.split_slice;
-                            t.hi = min(to, t.lo + prm.split_slice);
-                            t.group = g0;
-                            if (TFSM_IN(14, t0 + k, prm.split_cap)) splits[t0 + k] = t;
-                        }
+                    uint32_t added = 0;
+                    if (okg)
+                        added = emit_remainder(P, S, p, u, v, 1, adepth, g0, prm.split_slice, splits, &counters[2],
+                                               prm.split_cap, prm.search_fill, prm.split_slack, lane, g.m2);
+                    if (lane == 0 && okg) {  // read only by the split rounds, which run after this kernel
+                        groups[g0].pat = p;
+                        groups[g0].u = (uint16_t)u;
+                        groups[g0].v = v;
+                        groups[g0].pending = added;
+                        groups[g0].incomplete = 0;
+                    }
+                    if (added || prm.defer) {
+                        if (!added && lane == 0) atomicAdd(&counters[kDeferred], 1u);  // buffers full
                         n_steps += steps;
                         n_bytes += __reduce_add_sync(0xffffffffu, bytes);
-                        continue;  // decided later by the slices
+                        continue;  // decided by the split rounds, or by the next pass
                     }
-                    // buffers full: finish this task here without a budget
+                    // buffers full, last pass: finish this search here without a budget
                     if (lane == 0) S.emb[u] = v;
                     __syncwarp();
-                    r = dfs(g, P, S, dom, found, failed, lane, false, 0, 0, 0, steps, adepth, bytes);
+                    r = dfs(g, P, S, dom, found, failed, lane, 1, false, 0, 0, 0, cancel, steps, adepth, bytes);
                 }
                 n_steps += steps;
                 max_steps = steps > max_steps ? steps : max_steps;
                 n_bytes += __reduce_add_sync(0xffffffffu, bytes);
                 if (r == kFound) mark_found(P, S, ps, found, prm.tau, exact, lane);
-                else mark_failed(P, ps, failed, u, v, prm.tau, exact, lane);
+                else if (r == kFail) mark_failed(P, ps, failed, u, v, prm.tau, exact, lane);
             }
         }
         if (lane == 0 && n_search) {
@@ -650,13 +733,17 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
     }
 }
 
+// One split round: processes the tasks of round `round` (in `in`), searching each below its
+// partial embedding; a task that exceeds `budget` (0: never, as in the last round) emits its own
+// unexplored remainder into `out` for the next round, inside the same group.
 __global__ void __launch_bounds__(kSearchWarps * 32) k_split(Graph g, const PatDesc *__restrict__ descs,
                                                              PatStatus *__restrict__ st, SearchParams prm,
-                                                             uint32_t *__restrict__ counters,
-                                                             const uint32_t *__restrict__ dom,
+                                                             uint32_t *__restrict__ counters, int round,
+                                                             uint32_t budget, const uint32_t *__restrict__ dom,
                                                              uint32_t *__restrict__ found,
                                                              uint32_t *__restrict__ failed,
-                                                             const SplitTask *__restrict__ splits,
+                                                             const SplitTask *__restrict__ in,
+                                                             SplitTask *__restrict__ out,
                                                              SplitGroup *__restrict__ groups) {
     __shared__ WarpPlan plans[kSearchWarps];
     __shared__ WarpState states[kSearchWarps];
@@ -667,49 +754,67 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_split(Graph g, const PatD
     if (lane == 0) P.key = 0xffffffffu;
     __syncwarp();
     const bool exact = prm.exact != 0;
-    const uint32_t n_tasks = min(counters[1], prm.split_cap);
+    const uint32_t n_tasks = min(counters[2 + round], prm.split_cap);
     for (;;) {
         uint32_t it = 0;
-        if (lane == 0) it = atomicAdd(&counters[3], 1u);
+        if (lane == 0) it = atomicAdd(&counters[kClaimBase + round], 1u);
         it = __shfl_sync(0xffffffffu, it, 0);
         if (it >= n_tasks) break;
-        const SplitTask t = splits[it];
+        const SplitTask &t = in[it];  // fields read one by one; the prefix stays in memory
         const uint32_t p = t.pat;
+        if (p == kNullTask) continue;  // a slot of a claim that did not fit
         const int u = t.u;
+        const int depth = t.depth;
         if (!TFSM_IN(16, p, prm.n_pats) || !TFSM_IN(17, t.group, prm.group_cap) || !TFSM_IN(21, u, kMaxN)) continue;
         load_plan(P, descs[p], p, u, lane, prm.words);
         PatStatus &ps = st[p];
         SplitGroup &grp = groups[t.group];
         const uint32_t xl = t.v - P.lstart[u];
         const uint32_t o = P.off[u] + (xl >> 5);
-        if (!TFSM_IN(18, o, prm.words)) continue;
-        if (!TFSM_IN(44, t.v, g.n) || !TFSM_IN(45, t.lo, t.hi) || !TFSM_IN(46, __ldg(g.row_off + t.v), (uint64_t)t.lo + 1) ||
-            !TFSM_IN(47, t.hi, (uint64_t)__ldg(g.row_off + t.v + 1) + 1))
-            continue;
         const uint32_t bit = 1u << (xl & 31);
+        if (!TFSM_IN(18, o, prm.words) || !TFSM_IN(44, depth, P.n) || !TFSM_IN(45, t.lo, (uint64_t)t.hi + 1) ||
+            !TFSM_IN(47, t.hi, g.m2 + 1) || !TFSM_IN(46, depth, kMaxN))
+            continue;
         bool searched = false;
+        uint32_t added = 0;
         if (!pattern_stops(ps, u, exact, lane) && !(warp_word(found + o, lane) & bit)) {
-            if (lane == 0) S.emb[u] = t.v;
+            if ((int)lane < depth) S.emb[P.order[lane]] = t.prefix[lane];
             __syncwarp();
             uint32_t steps = 0, bytes = 12;
             int adepth = 0;
-            const int r = dfs(g, P, S, dom, found, failed, lane, true, t.lo, t.hi, 0, steps, adepth, bytes);
+            const Cancel cancel{found + o, bit, &ps, u, exact};
+            int r = dfs(g, P, S, dom, found, failed, lane, depth, true, t.lo, t.hi, budget, cancel, steps, adepth,
+                        bytes);
+            if (r == kAbort) {
+                added = emit_remainder(P, S, p, u, t.v, depth, adepth, t.group, prm.split_slice, out,
+                                       &counters[2 + round + 1], prm.split_cap, prm.split_cap - prm.split_slack,
+                                       prm.split_slack, lane, g.m2);
+                if (!added && prm.defer) {  // no room: v stays undecided for the next pass
+                    if (lane == 0) atomicAdd(&counters[kDeferred], 1u);
+                    r = kCancel;
+                } else if (!added) {  // no room, last pass: finish the task here
+                    r = dfs(g, P, S, dom, found, failed, lane, depth, true, t.lo, t.hi, 0, cancel, steps, adepth,
+                            bytes);
+                }
+            }
             if (r == kFound) mark_found(P, S, ps, found, prm.tau, exact, lane);
             const unsigned long long wb = __reduce_add_sync(0xffffffffu, bytes);
             if (lane == 0) {
                 atomicAdd(&ps.steps, (unsigned long long)steps);
                 atomicAdd(&ps.bytes, wb);
+                atomicMax(&ps.max_steps, (unsigned long long)steps);
             }
-            searched = true;
+            searched = r != kCancel;
         }
         if (lane == 0) {
             if (!searched && !(__ldcg(found + o) & bit)) atomicOr(&grp.incomplete, 1u);
+            if (added) atomicAdd(&grp.pending, added);  // before this task's own completion below
             __threadfence();
             const uint32_t left = atomicSub(&grp.pending, 1u) - 1;
             if (left == 0) {
                 __threadfence();
                 if (!(__ldcg(found + o) & bit) && __ldcg(&grp.incomplete) == 0) {
-                    // every slice finished without an embedding: v fails as u
+                    // every task of the search finished without an embedding: v fails as u
                     uint32_t orb = P.orbit[u];
                     while (orb) {
                         const int k = __ffs(orb) - 1;
@@ -797,8 +902,7 @@ cudaError_t launch_refine(const Graph &g, const PatDesc *descs, PatStatus *st, c
 
 cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchItem *items,
                           const SearchParams &prm, uint32_t *counters, const uint32_t *dom, uint32_t *found,
-                          uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s, int *launches) {
-    *launches = 0;
+                          uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s) {
     if (prm.n_items == 0) return cudaSuccess;
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search, kSearchWarps * 32, 0);
@@ -809,33 +913,35 @@ cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, c
     TFSM_LAUNCH(k_search, (unsigned)blocks, kSearchWarps * 32, s, g, descs, st, items, prm, counters, dom, found,
                 failed, splits, groups);
     cudaError_t e = cudaGetLastError();
-    *launches = 1;
 #ifdef TFSM_BOUNDS_CHECK
     if (e == cudaSuccess && cudaStreamSynchronize(s) != cudaSuccess) {
         std::fprintf(stderr, "tfsm checked build: fault in k_search\n");
         return cudaGetLastError();
     }
-    {
-        unsigned long long rec[4];
-        if (read_bounds_check(rec))
-            std::fprintf(stderr, "tfsm checked build: k_search site %llu index %llu bound %llu\n", rec[1], rec[2],
-                         rec[3]);
-    }
 #endif
-    if (e != cudaSuccess || prm.step_budget == 0) return e;
-    int per_sm2 = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_split, kSearchWarps * 32, 0);
-    if (per_sm2 <= 0) per_sm2 = 1;
-    TFSM_LAUNCH(k_split, (unsigned)(num_sms() * per_sm2), kSearchWarps * 32, s, g, descs, st, prm, counters, dom,
-                found, failed, splits, groups);
-    *launches = 2;
+    return e;
+}
+
+cudaError_t launch_split_round(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchParams &prm,
+                               uint32_t *counters, int round, const uint32_t *dom, uint32_t *found, uint32_t *failed,
+                               SplitTask *splits, SplitGroup *groups, cudaStream_t s) {
+    if (round < 0 || round >= kMaxRounds) return cudaErrorInvalidValue;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_split, kSearchWarps * 32, 0);
+    if (per_sm <= 0) per_sm = 1;
+    const SplitTask *in = splits + (size_t)(round % 2) * prm.split_cap;
+    SplitTask *out = splits + (size_t)((round + 1) % 2) * prm.split_cap;
+    const uint32_t budget = round + 1 < kMaxRounds ? prm.round_budget : 0u;  // the last possible round completes
+    TFSM_LAUNCH(k_split, (unsigned)(num_sms() * per_sm), kSearchWarps * 32, s, g, descs, st, prm, counters, round,
+                budget, dom, found, failed, in, out, groups);
+    cudaError_t e = cudaGetLastError();
 #ifdef TFSM_BOUNDS_CHECK
-    if (cudaStreamSynchronize(s) != cudaSuccess) {
+    if (e == cudaSuccess && cudaStreamSynchronize(s) != cudaSuccess) {
         std::fprintf(stderr, "tfsm checked build: fault in k_split\n");
         return cudaGetLastError();
     }
 #endif
-    return cudaGetLastError();
+    return e;
 }
 
 }  // namespace dev

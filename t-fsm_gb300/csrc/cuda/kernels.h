@@ -19,11 +19,17 @@ cudaError_t launch_refine(const Graph &g, const PatDesc *descs, PatStatus *st, c
                           const uint64_t *prefix, uint32_t n_items, uint64_t total_words, uint32_t *dom,
                           uint64_t chk_words, cudaStream_t s);
 
-// Runs k_search over `prm.n_items` items, then (when a step budget is set) k_split over the
-// slices it produced.  `counters` (4 x u32) must be zero on entry.
+// The search pass: k_search over `prm.n_items` items.  `counters` (kNumCounters x u32) must be
+// zero on entry; `splits` holds two buffers of prm.split_cap tasks each.
 cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchItem *items,
                           const SearchParams &prm, uint32_t *counters, const uint32_t *dom, uint32_t *found,
-                          uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s, int *launches);
+                          uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s);
+
+// Split round `round` (0 <= round < kMaxRounds): the tasks written for it by the previous phase.
+// Rounds run in order on one stream; round kMaxRounds - 1 has no step budget.
+cudaError_t launch_split_round(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchParams &prm,
+                               uint32_t *counters, int round, const uint32_t *dom, uint32_t *found, uint32_t *failed,
+                               SplitTask *splits, SplitGroup *groups, cudaStream_t s);
 
 // Checked builds (-DTFSM_BOUNDS_CHECK): the first out-of-bounds access the search kernels
 // detected (count, site, index, bound); false when none or when checks are compiled out.

@@ -179,9 +179,21 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     I.g.label_start = I.label_start.p;
     I.g.lab_off = I.lab_off.p;
     I.g.lab_stride = (uint32_t)stride;
-    I.counters.ensure(4);
-    I.splits.ensure(1u << 20);
-    I.groups.ensure(1u << 17);
+    I.counters.ensure(dev::kNumCounters);
+    // Two buffers of split tasks (88 B each) and as many groups (20 B each): one task per directed
+    // adjacency entry, 1 M..32 M (at most 6.3 GB; searches that find no room wait for another
+    // pass).  TFSM_SPLIT_CAPACITY sets both counts (tests use a tiny one to drive the buffer-full
+    // paths).
+    size_t task_cap = 1u << 20;
+    while (task_cap < (32u << 20) && task_cap < (size_t)lg.offs[lg.n]) task_cap *= 2;
+    size_t group_cap = task_cap;
+    if (const char *env = std::getenv("TFSM_SPLIT_CAPACITY")) {
+        const long c = std::atol(env);
+        if (c < 1 || c > (1l << 26)) throw EngineError(1, "TFSM_SPLIT_CAPACITY must be in 1..2^26");
+        task_cap = group_cap = (size_t)c;
+    }
+    I.splits.ensure(2 * task_cap);
+    I.groups.ensure(group_cap);
     upload_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
@@ -483,23 +495,68 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     TFSM_CK(cudaMemcpyAsync(I.items.p, items.data(), items.size() * sizeof(dev::SearchItem), cudaMemcpyHostToDevice,
                             I.stream));
     times_.h2d_bytes += items.size() * sizeof(dev::SearchItem);
-    TFSM_CK(cudaMemsetAsync(I.counters.p, 0, 4 * sizeof(uint32_t), I.stream));
+    TFSM_CK(cudaMemsetAsync(I.counters.p, 0, dev::kNumCounters * sizeof(uint32_t), I.stream));
     dev::SearchParams prm;
     prm.tau = tau;
     prm.exact = opt.exact ? 1 : 0;
     prm.n_items = (uint32_t)items.size();
     prm.step_budget = opt.step_budget;
     prm.split_slice = std::max<uint32_t>(32, opt.split_slice);
-    prm.split_cap = (uint32_t)I.splits.n;
+    prm.split_cap = (uint32_t)(I.splits.n / 2);
+    prm.split_slack = prm.split_cap / 8;
+    prm.search_fill = prm.split_cap / 4;
     prm.group_cap = (uint32_t)I.groups.n;
+    prm.round_budget = std::max<uint32_t>(1, opt.round_budget);
+    prm.defer = 0;
     prm.n_pats = (uint32_t)P;
     prm.words = total;
+    // A search pass, then split rounds: `split_rounds` of them unconditionally (one launch
+    // sequence, no host round trip), then one at a time while the previous round left tasks.
+    // Searches whose remainder found no room in the split buffers were left undecided: another
+    // pass over the same items takes them up (the last allowed pass finishes them in place).
     TFSM_CK(cudaEventRecord(I.ev0, I.stream));
-    int launches = 0;
-    TFSM_CK(dev::launch_search(I.g, L.descs.p, I.status.p, I.items.p, prm, I.counters.p, L.dom.p, L.found.p,
-                               L.failed.p, I.splits.p, I.groups.p, I.stream, &launches));
+    uint64_t launches = 0;
+    static_assert(KernelTimes::kRoundSlots == dev::kMaxRounds + 1, "split round slots");
+    uint32_t hcnt[dev::kNumCounters];
+    constexpr int kMaxPasses = 16;
+    for (int pass = 0; pass < kMaxPasses; ++pass) {
+        if (pass > 0) TFSM_CK(cudaMemsetAsync(I.counters.p, 0, dev::kNumCounters * sizeof(uint32_t), I.stream));
+        prm.defer = pass + 1 < kMaxPasses ? 1u : 0u;
+        TFSM_CK(dev::launch_search(I.g, L.descs.p, I.status.p, I.items.p, prm, I.counters.p, L.dom.p, L.found.p,
+                                   L.failed.p, I.splits.p, I.groups.p, I.stream));
+        launches += items.empty() ? 0 : 1;
+        if (prm.step_budget && !items.empty()) {
+            const int fixed = (int)std::min<uint32_t>(std::max<uint32_t>(1, opt.split_rounds), dev::kMaxRounds);
+            int r = 0;
+            for (; r < fixed; ++r) {
+                TFSM_CK(dev::launch_split_round(I.g, L.descs.p, I.status.p, prm, I.counters.p, r, L.dom.p,
+                                                L.found.p, L.failed.p, I.splits.p, I.groups.p, I.stream));
+                ++launches;
+            }
+            for (; r < dev::kMaxRounds; ++r) {
+                uint32_t pending = 0;
+                TFSM_CK(cudaMemcpyAsync(&pending, I.counters.p + 2 + r, sizeof(pending), cudaMemcpyDeviceToHost,
+                                        I.stream));
+                TFSM_CK(cudaStreamSynchronize(I.stream));
+                times_.d2h_bytes += sizeof(pending);
+                if (pending == 0) break;
+                TFSM_CK(dev::launch_split_round(I.g, L.descs.p, I.status.p, prm, I.counters.p, r, L.dom.p,
+                                                L.found.p, L.failed.p, I.splits.p, I.groups.p, I.stream));
+                ++launches;
+            }
+        }
+        TFSM_CK(cudaMemcpyAsync(hcnt, I.counters.p, sizeof(hcnt), cudaMemcpyDeviceToHost, I.stream));
+        TFSM_CK(cudaStreamSynchronize(I.stream));
+        times_.d2h_bytes += sizeof(hcnt);
+        times_.split_groups += std::min<uint32_t>(hcnt[1], prm.group_cap);
+        for (int r = 0; r < KernelTimes::kRoundSlots; ++r)
+            times_.split_tasks[r] += std::min(hcnt[2 + r], prm.split_cap);
+        times_.deferred += hcnt[dev::kDeferred];
+        times_.search_passes++;
+        if (hcnt[dev::kDeferred] == 0) break;
+    }
     times_.search_ms += time_since_ev0();
-    times_.search_launches += (uint64_t)launches;
+    times_.search_launches += launches;
     times_.search_calls++;
     {
         unsigned long long rec[4];

@@ -33,8 +33,10 @@ struct EvalResult {
 
 struct EngineOptions {
     bool exact = false;                // evaluate every candidate (exact MNI), no early exit
-    uint32_t step_budget = 4096;       // chunk evaluations before a task is split (0: never)
-    uint32_t split_slice = 256;        // depth-1 anchor positions per split slice
+    uint32_t step_budget = 16;         // chunk evaluations before a search is split (0: never)
+    uint32_t split_slice = 64;         // anchor positions per split task
+    uint32_t round_budget = 16;        // step budget of a split task (the 64th round has none)
+    uint32_t split_rounds = 4;         // split rounds launched without checking for remaining tasks
     uint32_t chunk_words = 4;          // bitmap words per search work item (x32 candidates)
     uint32_t refine_rounds = 2;        // arc-consistency passes for patterns that need search
     uint32_t max_batch = 4096;         // miner: patterns per engine call
@@ -48,6 +50,11 @@ struct KernelTimes {                   // accumulated device time (CUDA events),
     uint64_t init_words = 0, refine_words = 0;  // bitmap words processed
     uint64_t search_bytes = 0;         // algorithmic bytes read by the search kernels
     uint64_t h2d_bytes = 0, d2h_bytes = 0;      // host<->device copies of the evaluations
+    static constexpr int kRoundSlots = 65;      // split rounds + one
+    uint64_t split_groups = 0;                  // searches handed to the split rounds
+    uint64_t deferred = 0;                      // searches left for another pass (buffers full)
+    uint64_t search_passes = 0;
+    uint64_t split_tasks[kRoundSlots] = {};     // tasks written for each split round
 };
 
 // Device memory of one evaluated batch; kept while the batch's patterns are parents.

@@ -98,7 +98,8 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                 }
                 cur_levels.emplace_back(new Level);
                 std::vector<EvalResult> res;
-                const double search_before = eng.times().search_ms;
+                const KernelTimes before = eng.times();
+                const double search_before = before.search_ms;
                 eng.evaluate(pats, par, prev, tau, opt.engine, *cur_levels.back(), res);
                 st.engine_calls++;
                 st.evaluations += b1 - b0;
@@ -114,6 +115,19 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                                  "search %llu chunk steps\n",
                                  st.levels + 1, b1 - b0, (unsigned long long)nf, eng.times().search_ms - search_before,
                                  (unsigned long long)srch, (unsigned long long)mx);
+                    const KernelTimes &now = eng.times();
+                    if (now.split_groups > before.split_groups) {
+                        std::fprintf(stderr, "          split: %llu searches, %llu passes, %llu deferred, tasks per round",
+                                     (unsigned long long)(now.split_groups - before.split_groups),
+                                     (unsigned long long)(now.search_passes - before.search_passes),
+                                     (unsigned long long)(now.deferred - before.deferred));
+                        int last = 0;
+                        for (int r = 0; r < KernelTimes::kRoundSlots; ++r)
+                            if (now.split_tasks[r] != before.split_tasks[r]) last = r;
+                        for (int r = 0; r <= last; ++r)
+                            std::fprintf(stderr, " %llu", (unsigned long long)(now.split_tasks[r] - before.split_tasks[r]));
+                        std::fprintf(stderr, "\n");
+                    }
                 }
                 for (size_t i = b0; i < b1; ++i) {
                     nodes[i].res = std::move(res[i - b0]);

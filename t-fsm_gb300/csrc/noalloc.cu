@@ -205,7 +205,7 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     const size_t o_desc = 0;
     const size_t o_status = align_up(o_desc + sizeof(PatDesc));
     const size_t o_counters = align_up(o_status + sizeof(PatStatus));
-    const size_t o_item_pu = align_up(o_counters + 4 * sizeof(uint32_t));
+    const size_t o_item_pu = align_up(o_counters + dev::kNumCounters * sizeof(uint32_t));
     const size_t o_prefix = align_up(o_item_pu + dev::kMaxN * sizeof(uint32_t));
     const size_t o_items = align_up(o_prefix + (dev::kMaxN + 1) * sizeof(uint64_t));
     const size_t o_pools = align_up(o_items + max_items * sizeof(dev::SearchItem));
@@ -244,7 +244,7 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     }
     NA_CK(cudaMemcpyAsync(d_desc, &D, sizeof(D), cudaMemcpyHostToDevice, s));
     NA_CK(cudaMemsetAsync(d_status, 0, sizeof(PatStatus), s));  // the previous call's status stays behind
-    NA_CK(cudaMemsetAsync(d_counters, 0, 4 * sizeof(uint32_t), s));
+    NA_CK(cudaMemsetAsync(d_counters, 0, dev::kNumCounters * sizeof(uint32_t), s));
     NA_CK(cudaMemcpyAsync(d_item_pu, item_pu, n * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     NA_CK(cudaMemcpyAsync(d_prefix, prefix, (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
     // every bitmap word of every vertex is written here, so no clearing of the pools is needed
@@ -315,9 +315,8 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     prm.split_slice = 32;
     prm.n_pats = 1;
     prm.words = words;
-    int launches = 0;
     NA_CK(dev::launch_search(g, d_desc, d_status, d_items, prm, d_counters, d_dom, d_found, d_failed, nullptr, nullptr,
-                             s, &launches));
+                             s));
     NA_CK(cudaMemcpyAsync(&st, d_status, sizeof(st), cudaMemcpyDeviceToHost, s));
     NA_CK(cudaStreamSynchronize(s));
     mn = UINT32_MAX;

@@ -2,7 +2,7 @@
 //
 //   run -file G.lg -freq TAU [-thread T] [-maxNodes N] [-plain] [-exact] [-out PATH]
 //       [-step-budget B] [-split-slice S] [-chunk-words W] [-refine-rounds R] [-max-batch M]
-//       [-time-limit SECONDS]
+//       [-split-rounds K] [-round-budget B] [-time-limit SECONDS]
 //
 // Frequent patterns go to ./grami_results.txt (or -out PATH) in the serial build's format
 // (serial/grami.h:622-635); timing and counts are printed as the parallel build prints them.
@@ -54,6 +54,8 @@ int main(int argc, char **argv) {
     if (opt(argc, argv, "-chunk-words")) o.chunk_words = (uint32_t)std::atoi(opt(argc, argv, "-chunk-words"));
     if (opt(argc, argv, "-refine-rounds")) o.refine_rounds = (uint32_t)std::atoi(opt(argc, argv, "-refine-rounds"));
     if (opt(argc, argv, "-max-batch")) o.max_batch = (uint32_t)std::atoi(opt(argc, argv, "-max-batch"));
+    if (opt(argc, argv, "-split-rounds")) o.split_rounds = (uint32_t)std::atoi(opt(argc, argv, "-split-rounds"));
+    if (opt(argc, argv, "-round-budget")) o.round_budget = (uint32_t)std::atoi(opt(argc, argv, "-round-budget"));
     if (opt(argc, argv, "-time-limit")) o.time_limit_s = std::atof(opt(argc, argv, "-time-limit"));
     rc = tfsm_set_options(g, &o);
     if (rc != TFSM_OK) {

@@ -58,12 +58,19 @@ def test_mining_plain_matches_reference(tfsm, graphs, case, tmp_path):
     assert st["engine_calls"] == st["evaluations"]
 
 
+SPLIT_OPTS = [dict(step_budget=1, split_slice=32, round_budget=1),   # splits again in every round
+              dict(step_budget=1, split_slice=32, split_rounds=1, round_budget=1 << 30),  # no re-splitting
+              dict(step_budget=3, split_slice=64, round_budget=2, split_rounds=3),
+              dict(step_budget=0)]                                    # no splitting
+
+
 @pytest.mark.parametrize("case", ["cfg1", "el3", "star_hub", "clique"])
-def test_mining_with_forced_hub_splits_matches_reference(tfsm, graphs, case, tmp_path):
+@pytest.mark.parametrize("opts", range(len(SPLIT_OPTS)))
+def test_mining_with_forced_hub_splits_matches_reference(tfsm, graphs, case, opts, tmp_path):
     g = graphs(case)
     saved = g.options()
     try:
-        g.set_options(step_budget=1, split_slice=32)  # every search longer than one chunk splits
+        g.set_options(**SPLIT_OPTS[opts])  # every search longer than a few chunks splits
         pats, st = mine_set(tfsm, g, case, tmp_path)
     finally:
         g.set_options(**saved)
@@ -131,8 +138,8 @@ def test_forced_splits_keep_exact_supports(tfsm, graphs):
     g = graphs(case)
     saved = g.options()
     try:
-        for opts in (dict(step_budget=1, split_slice=32, chunk_words=1), dict(step_budget=2, split_slice=64,
-                                                                              chunk_words=7, refine_rounds=1)):
+        for opts in (dict(step_budget=1, split_slice=32, chunk_words=1, round_budget=1),
+                     dict(step_budget=2, split_slice=64, chunk_words=7, refine_rounds=1, split_rounds=2)):
             g.set_options(**opts)
             res = g.evaluate([tfsm.parse_key(k) for k in keys], flags=tfsm.FLAG_EXACT)
             assert [r.mni for r in res] == [want[k] for k in keys]
@@ -185,4 +192,18 @@ def test_cli_writes_reference_format(built, case_graph, tmp_path):
                        text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     assert "[INFO] # Frequent Patterns: %d" % len(golden_pattern_set(case)) in r.stdout
+    assert set(read_results(out)) == golden_pattern_set(case)
+
+
+@pytest.mark.parametrize("case", ["star_hub", "clique", "el3"])
+def test_split_buffers_full_keep_results(built, case_graph, case, tmp_path):
+    """Split buffers of 5 tasks / 5 groups: claims straddle the end, searches finish in place."""
+    import os
+    c = CASES[case]
+    out = tmp_path / "grami_results.txt"
+    env = dict(os.environ, TFSM_SPLIT_CAPACITY="5")
+    r = subprocess.run([str(built / "bin" / "run"), "-file", str(case_graph(case)), "-freq", str(c["tau"]),
+                        "-maxNodes", str(c["max_nodes"]), "-step-budget", "1", "-round-budget", "1", "-split-slice",
+                        "32", "-out", str(out)], capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 0, r.stderr
     assert set(read_results(out)) == golden_pattern_set(case)

@@ -27,9 +27,12 @@ def emu():
     return build_emu.build("asan")
 
 
-OPTS = {"default": [], "split": ["-step-budget", "1", "-split-slice", "32", "-chunk-words", "1"],
+OPTS = {"default": [], "split": ["-step-budget", "1", "-split-slice", "32", "-chunk-words", "1", "-round-budget", "1"],
+        "split1": ["-step-budget", "2", "-split-slice", "32", "-split-rounds", "1", "-round-budget", "1000000"],
         "plain": ["-plain", "-refine-rounds", "1"], "exact": ["-exact"], "batch3": ["-max-batch", "3"]}
 RUNS = [(c, o) for c in SMALL for o in OPTS if not (o == "plain" and c == "quirk_elabels")]
+RUNS += [(c, "tiny_buffers") for c in ("clique", "star_hub")]
+OPTS["tiny_buffers"] = OPTS["split"]  # with TFSM_SPLIT_CAPACITY=5: claims straddle and overflow
 
 
 @pytest.mark.parametrize("case,opt", RUNS)
@@ -38,6 +41,8 @@ def test_emulated_kernels_match_reference(emu, case, opt, tmp_path):
     c = CASES[case]
     out = tmp_path / "res.txt"
     env = dict(os.environ, ASAN_OPTIONS="detect_leaks=1:abort_on_error=1", UBSAN_OPTIONS="halt_on_error=1")
+    if opt == "tiny_buffers":
+        env["TFSM_SPLIT_CAPACITY"] = "5"
     r = subprocess.run([str(emu), "-file", str(GOLDEN / c["file"]), "-freq", str(c["tau"]), "-maxNodes",
                         str(c["max_nodes"]), "-out", str(out), *opts], capture_output=True, text=True, timeout=600,
                        env=env)
