@@ -653,7 +653,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
         load_plan(P, descs[p], p, u, lane, prm.words);
         PatStatus &ps = st[p];
         unsigned long long n_search = 0, n_steps = 0, n_bytes = 0, max_steps = 0;
-        bool stop = false;
+        bool stop = false, abandon = false;
         for (uint32_t word = item.word_lo; word < item.word_hi && !stop; ++word) {
             if (pattern_stops(ps, u, exact, lane)) break;
             const uint32_t o = P.off[u] + word;
@@ -668,13 +668,13 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
                     break;
                 }
                 if (prm.defer && prm.step_budget) {
-                    // the first split round's share of the buffer is full: start no search that
-                    // might need it; the next pass takes v up
+                    // the first split round's share of the buffer is full: this warp starts no
+                    // more searches in this pass; the next pass takes up what is left
                     int full = 0;
                     if (lane == 0) full = __ldcg(&counters[2]) >= prm.search_fill;
                     if (__shfl_sync(0xffffffffu, full, 0)) {
-                        if (lane == 0) atomicAdd(&counters[kDeferred], 1u);
-                        continue;
+                        abandon = stop = true;
+                        break;
                     }
                 }
                 const uint32_t v = P.lstart[u] + word * 32 + b;
@@ -729,6 +729,10 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
             atomicAdd(&ps.steps, n_steps);
             atomicAdd(&ps.bytes, n_bytes);
             atomicMax(&ps.max_steps, max_steps);
+        }
+        if (abandon) {
+            if (lane == 0) atomicAdd(&counters[kDeferred], 1u);
+            return;
         }
     }
 }
@@ -923,15 +927,15 @@ cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, c
 }
 
 cudaError_t launch_split_round(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchParams &prm,
-                               uint32_t *counters, int round, const uint32_t *dom, uint32_t *found, uint32_t *failed,
-                               SplitTask *splits, SplitGroup *groups, cudaStream_t s) {
+                               uint32_t *counters, int round, uint32_t budget, const uint32_t *dom, uint32_t *found,
+                               uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s) {
     if (round < 0 || round >= kMaxRounds) return cudaErrorInvalidValue;
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_split, kSearchWarps * 32, 0);
     if (per_sm <= 0) per_sm = 1;
     const SplitTask *in = splits + (size_t)(round % 2) * prm.split_cap;
     SplitTask *out = splits + (size_t)((round + 1) % 2) * prm.split_cap;
-    const uint32_t budget = round + 1 < kMaxRounds ? prm.round_budget : 0u;  // the last possible round completes
+    if (round + 1 == kMaxRounds) budget = 0;  // the last possible round completes every task
     TFSM_LAUNCH(k_split, (unsigned)(num_sms() * per_sm), kSearchWarps * 32, s, g, descs, st, prm, counters, round,
                 budget, dom, found, failed, in, out, groups);
     cudaError_t e = cudaGetLastError();

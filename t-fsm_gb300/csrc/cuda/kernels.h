@@ -25,11 +25,12 @@ cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, c
                           const SearchParams &prm, uint32_t *counters, const uint32_t *dom, uint32_t *found,
                           uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s);
 
-// Split round `round` (0 <= round < kMaxRounds): the tasks written for it by the previous phase.
-// Rounds run in order on one stream; round kMaxRounds - 1 has no step budget.
+// Split round `round` (0 <= round < kMaxRounds): the tasks written for it by the previous phase,
+// each with a step budget of `budget` chunk evaluations (0: none).  Rounds run in order on one
+// stream; round kMaxRounds - 1 has no step budget.
 cudaError_t launch_split_round(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchParams &prm,
-                               uint32_t *counters, int round, const uint32_t *dom, uint32_t *found, uint32_t *failed,
-                               SplitTask *splits, SplitGroup *groups, cudaStream_t s);
+                               uint32_t *counters, int round, uint32_t budget, const uint32_t *dom, uint32_t *found,
+                               uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s);
 
 // Checked builds (-DTFSM_BOUNDS_CHECK): the first out-of-bounds access the search kernels
 // detected (count, site, index, bound); false when none or when checks are compiled out.

@@ -181,10 +181,10 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     I.g.lab_stride = (uint32_t)stride;
     I.counters.ensure(dev::kNumCounters);
     // Two buffers of split tasks (88 B each) and as many groups (20 B each): one task per directed
-    // adjacency entry, 1 M..32 M (at most 6.3 GB; searches that find no room wait for another
+    // adjacency entry, 2 M..32 M (at most 6.3 GB; searches that find no room wait for another
     // pass).  TFSM_SPLIT_CAPACITY sets both counts (tests use a tiny one to drive the buffer-full
     // paths).
-    size_t task_cap = 1u << 20;
+    size_t task_cap = 2u << 20;
     while (task_cap < (32u << 20) && task_cap < (size_t)lg.offs[lg.n]) task_cap *= 2;
     size_t group_cap = task_cap;
     if (const char *env = std::getenv("TFSM_SPLIT_CAPACITY")) {
@@ -504,7 +504,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     prm.split_slice = std::max<uint32_t>(32, opt.split_slice);
     prm.split_cap = (uint32_t)(I.splits.n / 2);
     prm.split_slack = prm.split_cap / 8;
-    prm.search_fill = prm.split_cap / 4;
+    prm.search_fill = prm.split_cap / 2;
     prm.group_cap = (uint32_t)I.groups.n;
     prm.round_budget = std::max<uint32_t>(1, opt.round_budget);
     prm.defer = 0;
@@ -529,8 +529,8 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
             const int fixed = (int)std::min<uint32_t>(std::max<uint32_t>(1, opt.split_rounds), dev::kMaxRounds);
             int r = 0;
             for (; r < fixed; ++r) {
-                TFSM_CK(dev::launch_split_round(I.g, L.descs.p, I.status.p, prm, I.counters.p, r, L.dom.p,
-                                                L.found.p, L.failed.p, I.splits.p, I.groups.p, I.stream));
+                TFSM_CK(dev::launch_split_round(I.g, L.descs.p, I.status.p, prm, I.counters.p, r, prm.round_budget,
+                                                L.dom.p, L.found.p, L.failed.p, I.splits.p, I.groups.p, I.stream));
                 ++launches;
             }
             for (; r < dev::kMaxRounds; ++r) {
@@ -540,7 +540,11 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
                 TFSM_CK(cudaStreamSynchronize(I.stream));
                 times_.d2h_bytes += sizeof(pending);
                 if (pending == 0) break;
-                TFSM_CK(dev::launch_split_round(I.g, L.descs.p, I.status.p, prm, I.counters.p, r, L.dom.p,
+                // later rounds double the budget: the long searches that remain finish in a few
+                // rounds instead of paying a round trip per `round_budget` steps
+                const uint32_t budget = (uint32_t)std::min<uint64_t>(
+                    (uint64_t)prm.round_budget << std::min(r - fixed + 1, 20), 1u << 30);
+                TFSM_CK(dev::launch_split_round(I.g, L.descs.p, I.status.p, prm, I.counters.p, r, budget, L.dom.p,
                                                 L.found.p, L.failed.p, I.splits.p, I.groups.p, I.stream));
                 ++launches;
             }
