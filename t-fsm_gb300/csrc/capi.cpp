@@ -8,6 +8,7 @@
 
 #include "../../include/tfsm.h"
 #include "engine.hpp"
+#include "host/lg_fast.hpp"
 #include "miner.hpp"
 #include "noalloc.hpp"
 
@@ -125,7 +126,7 @@ int tfsm_graph_load(const char *path, int32_t tau, tfsm_graph **out) {
         *out = nullptr;
         auto t0 = std::chrono::steady_clock::now();
         std::unique_ptr<tfsm_graph> g(new tfsm_graph);
-        g->lg = tfsm::load_lg(path, tau);
+        g->lg = tfsm::load_lg_fast(path, tau);
         return finish_graph(g, tau, t0, out);
     });
 }
@@ -145,7 +146,7 @@ int tfsm_graph_from_edges(uint32_t n_vertices, const int32_t *vlabels, uint64_t 
             raw.edges.emplace_back(src[i], dst[i], elabels[i]);
         }
         std::unique_ptr<tfsm_graph> g(new tfsm_graph);
-        g->lg = tfsm::build_pruned(raw, tau);
+        g->lg = tfsm::build_pruned_fast(raw, tau);
         return finish_graph(g, tau, t0, out);
     });
 }

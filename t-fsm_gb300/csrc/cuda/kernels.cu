@@ -162,6 +162,8 @@ __global__ void __launch_bounds__(256) k_domain_init(Graph g, const PatDesc *__r
 // v has a neighbour x in D(w) reached through an edge with the pattern edge's label.
 // One warp per bitmap word; the warp scans each candidate's label sub-range 32 entries at a time.
 // ------------------------------------------------------------------------------------------------
+constexpr uint32_t kLaneScan = 16;  // k_refine: longest label range a single lane scans
+
 __global__ void __launch_bounds__(256) k_refine(Graph g, const PatDesc *__restrict__ descs, PatStatus *__restrict__ st,
                                                 const uint32_t *__restrict__ item_pu,
                                                 const uint64_t *__restrict__ prefix, uint32_t n_items,
@@ -183,8 +185,42 @@ __global__ void __launch_bounds__(256) k_refine(Graph g, const PatDesc *__restri
         // control flow (and its collectives) uniform
         const uint32_t w0 = warp_word(wp, lane);
         if (w0 == 0) continue;
-        uint32_t keep = w0;
-        uint32_t bits = w0;
+        // Pass 1, one candidate per lane: every pattern neighbour w needs a supporting data
+        // neighbour (label, edge label, in w's domain) inside a short label range, scanned serially.
+        // A candidate with a range longer than kLaneScan goes to pass 2 (the warp scans it).
+        uint32_t keep_lane = 1, hard_lane = 0;
+        if ((w0 >> lane) & 1u) {
+            const uint32_t v = D.lstart[u] + word * 32 + lane;
+            if (TFSM_IN(38, v, g.n)) {
+                const uint32_t *lo_v = g.lab_off + (size_t)v * g.lab_stride;
+                uint32_t nb = D.adj[u];
+                while (nb && keep_lane && !hard_lane) {
+                    const int w = __ffs(nb) - 1;
+                    nb &= nb - 1;
+                    const uint32_t lo = __ldg(lo_v + D.lab[w]), hi = __ldg(lo_v + D.lab[w] + 1);
+                    if (hi - lo > kLaneScan) {
+                        hard_lane = 1;
+                        break;
+                    }
+                    const uint32_t ls = D.lstart[w];
+                    const uint8_t el = D.el[u][w];
+                    const uint32_t *dw = dom + D.off[w];
+                    bool sup = false;
+                    for (uint32_t i = lo; i < hi && !sup; ++i) {
+                        if (!TFSM_IN(39, i, g.m2) || __ldg(g.elab + i) != el) continue;
+                        const uint32_t xl = __ldg(g.col + i) - ls;
+                        if (TFSM_IN(40, (uint64_t)D.off[w] + (xl >> 5), chk_words))
+                            sup = (__ldcg(dw + (xl >> 5)) >> (xl & 31)) & 1u;
+                    }
+                    keep_lane = sup ? 1u : 0u;
+                }
+            }
+        }
+        const uint32_t hard = __ballot_sync(0xffffffffu, hard_lane) & w0;
+        const uint32_t dropped = __ballot_sync(0xffffffffu, !keep_lane && !hard_lane) & w0;
+        uint32_t keep = w0 & ~dropped;
+        // Pass 2: the warp scans the long ranges of the remaining candidates together.
+        uint32_t bits = hard;
         while (bits) {
             const int bit = __ffs(bits) - 1;
             bits &= bits - 1;

@@ -20,6 +20,7 @@
 #include "cuda/dev_common.cuh"
 #include "cuda/kernels.h"
 #include "engine.hpp"
+#include "host/lg_fast.hpp"
 
 namespace tfsm {
 
@@ -109,47 +110,50 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     if (I.edense.size() > 250) throw EngineError(5, "more than 250 frequent edge labels");
     const int NL = (int)lg.freq_vlabels.size();
     if (NL > 250) throw EngineError(5, "more than 250 frequent vertex labels");
+    const fast::LabelIndex vidx(lg.freq_vlabels), eidx(lg.freq_elabels);
+    const int threads = fast::default_threads();
     // label-grouped renumbering: internal id = label_start[L] + rank within the label
+    std::vector<int> dl(lg.n);
     std::vector<uint32_t> cnt((size_t)NL + 1, 0);
-    for (uint32_t v = 0; v < lg.n; ++v) cnt[(size_t)I.vdense[lg.vlabel[v]] + 1]++;
+    for (uint32_t v = 0; v < lg.n; ++v) cnt[(size_t)(dl[v] = vidx(lg.vlabel[v])) + 1]++;
     I.lstart.assign((size_t)NL + 1, 0);
     for (int L = 0; L < NL; ++L) I.lstart[(size_t)L + 1] = I.lstart[(size_t)L] + cnt[(size_t)L + 1];
     std::vector<uint32_t> to_int(lg.n), fillv(I.lstart.begin(), I.lstart.end() - 1);
-    std::vector<int> dl(lg.n);
-    for (uint32_t v = 0; v < lg.n; ++v) {
-        dl[v] = I.vdense[lg.vlabel[v]];
-        to_int[v] = fillv[(size_t)dl[v]]++;
-    }
+    for (uint32_t v = 0; v < lg.n; ++v) to_int[v] = fillv[(size_t)dl[v]]++;
     std::vector<uint32_t> from_int(lg.n);
     for (uint32_t v = 0; v < lg.n; ++v) from_int[to_int[v]] = v;
-    // CSR in internal ids; filling lists in increasing source order keeps every list sorted.
+    // CSR in internal ids, each list sorted by (internal id, edge label): row x is v's list mapped
+    // through to_int and re-sorted (ids of one label keep their order, labels are regrouped).
     std::vector<uint32_t> off((size_t)lg.n + 1, 0);
     for (uint32_t x = 0; x < lg.n; ++x) off[(size_t)x + 1] = off[x] + lg.degree(from_int[x]);
     std::vector<uint32_t> col(off[lg.n]);
     std::vector<uint8_t> el(off[lg.n]);
-    std::vector<uint32_t> fill(off.begin(), off.end() - 1);
-    for (uint32_t x = 0; x < lg.n; ++x) {
-        const uint32_t v = from_int[x];
-        for (uint64_t i = lg.offs[v]; i < lg.offs[v + 1]; ++i) {
-            const uint32_t y = to_int[lg.nbr[i]];
-            col[fill[y]] = x;
-            el[fill[y]] = (uint8_t)I.edense[lg.elab[i]];
-            fill[y]++;
-        }
-    }
     // per-vertex label offsets: lab_off[x * (NL + 1) + L] = first position of a neighbour >= label L
     const size_t stride = (size_t)NL + 1;
     if ((size_t)lg.n * stride >= (1ull << 34)) throw EngineError(5, "label-offset table too large");
     std::vector<uint32_t> lab_off((size_t)lg.n * stride);
-    for (uint32_t x = 0; x < lg.n; ++x) {
-        uint32_t pos = off[x];
-        const uint32_t end = off[(size_t)x + 1];
-        for (int L = 0; L <= NL; ++L) {
-            const uint32_t first = I.lstart[(size_t)L];  // lstart[NL] == n: past every id
-            while (pos < end && col[pos] < first) ++pos;
-            lab_off[(size_t)x * stride + (size_t)L] = L == NL ? end : pos;
+    fast::parallel_ranges(lg.n, threads, [&](int, size_t x0, size_t x1) {
+        std::vector<uint64_t> key;
+        for (size_t x = x0; x < x1; ++x) {
+            const uint32_t v = from_int[x];
+            key.clear();
+            for (uint64_t i = lg.offs[v]; i < lg.offs[v + 1]; ++i)
+                key.push_back(((uint64_t)to_int[lg.nbr[i]] << 8) | (uint64_t)eidx(lg.elab[i]));
+            std::sort(key.begin(), key.end());
+            const uint32_t b = off[x];
+            for (size_t k = 0; k < key.size(); ++k) {
+                col[b + k] = (uint32_t)(key[k] >> 8);
+                el[b + k] = (uint8_t)(key[k] & 0xffu);
+            }
+            uint32_t pos = b;
+            const uint32_t end = off[x + 1];
+            for (int L = 0; L <= NL; ++L) {
+                const uint32_t first = I.lstart[(size_t)L];  // lstart[NL] == n: past every id
+                while (pos < end && col[pos] < first) ++pos;
+                lab_off[x * stride + (size_t)L] = L == NL ? end : pos;
+            }
         }
-    }
+    });
     I.n = lg.n;
     I.m2 = off[lg.n];
     TFSM_CK(cudaStreamCreateWithFlags(&I.stream, cudaStreamNonBlocking));

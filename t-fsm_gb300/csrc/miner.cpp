@@ -3,10 +3,13 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
+#include <functional>
 #include <memory>
+#include <mutex>
 #include <thread>
 
 namespace tfsm {
@@ -20,12 +23,72 @@ struct Node {
     int idx = 0;           // index inside lvl
 };
 
+// Workers kept for the whole mining run: a level's extension is a few milliseconds of work, of
+// the same order as creating and joining a thread per core for it.
+class Pool {
+  public:
+    explicit Pool(int n) {
+        for (int i = 0; i + 1 < n; ++i) th_.emplace_back([this]() { loop(); });
+    }
+    ~Pool() {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            quit_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : th_) t.join();
+    }
+    // Runs fn on every worker and the calling thread; returns when all calls have returned.
+    void run(const std::function<void()> &fn) {
+        if (th_.empty()) {
+            fn();
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            fn_ = &fn;
+            busy_ = (int)th_.size();
+            ++gen_;
+        }
+        cv_.notify_all();
+        fn();
+        std::unique_lock<std::mutex> lk(mu_);
+        done_.wait(lk, [this]() { return busy_ == 0; });
+        fn_ = nullptr;
+    }
+
+  private:
+    void loop() {
+        uint64_t seen = 0;
+        for (;;) {
+            const std::function<void()> *fn;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&]() { return quit_ || gen_ != seen; });
+                if (quit_) return;
+                seen = gen_;
+                fn = fn_;
+            }
+            (*fn)();
+            std::lock_guard<std::mutex> lk(mu_);
+            if (--busy_ == 0) done_.notify_one();
+        }
+    }
+    std::vector<std::thread> th_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_;
+    const std::function<void()> *fn_ = nullptr;
+    int busy_ = 0;
+    uint64_t gen_ = 0;
+    bool quit_ = false;
+};
+
 // Extends every frequent node (rightmost extension + canonical check), in parallel over parents.
-void extend_all(const std::vector<Node> &level, const ExtendContext &ctx, int threads,
+void extend_all(const std::vector<Node> &level, const ExtendContext &ctx, Pool &pool,
                 std::vector<std::vector<Pattern>> &kids) {
     kids.assign(level.size(), {});
     std::atomic<size_t> next(0);
-    auto work = [&]() {
+    const std::function<void()> work = [&]() {
         for (;;) {
             const size_t i = next.fetch_add(1);
             if (i >= level.size()) break;
@@ -33,14 +96,10 @@ void extend_all(const std::vector<Node> &level, const ExtendContext &ctx, int th
             extend_pattern(level[i].pat, ctx, kids[i]);
         }
     };
-    const int t = std::max(1, std::min<int>(threads, (int)level.size()));
-    if (t == 1) {
-        work();
-        return;
-    }
-    std::vector<std::thread> th;
-    for (int k = 0; k < t; ++k) th.emplace_back(work);
-    for (auto &x : th) x.join();
+    size_t n_freq = 0;
+    for (auto &nd : level) n_freq += nd.res.frequent ? 1 : 0;
+    if (n_freq <= 2) work();  // not worth waking the workers
+    else pool.run(work);
 }
 
 }  // namespace
@@ -50,6 +109,7 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
     out.clear();
     st = MineStats();
     const int threads = opt.host_threads > 0 ? opt.host_threads : (int)std::max(1u, std::thread::hardware_concurrency());
+    Pool pool(threads);
     ExtendContext ctx;
     ctx.freq_elabels = g.freq_elabels;
     ctx.max_nodes = opt.max_nodes;
@@ -186,7 +246,7 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
             if (nd.res.frequent) out.push_back({nd.pat, nd.res});
         auto te = std::chrono::steady_clock::now();
         std::vector<std::vector<Pattern>> kids;
-        extend_all(level, ctx, threads, kids);
+        extend_all(level, ctx, pool, kids);
         std::vector<Node> next;
         std::vector<int> parent_of;
         for (size_t i = 0; i < kids.size(); ++i)
