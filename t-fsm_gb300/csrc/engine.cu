@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <numeric>
 
 #include "cuda/dev_common.cuh"
@@ -32,25 +33,62 @@ namespace {
         if (e_ != cudaSuccess) throw EngineError(10, std::string(#x) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
+// Device buffers released by the levels of one engine, handed to its later levels: a mining run
+// allocates each level's bitmap pools once instead of a cudaMalloc / cudaFree (which synchronises
+// the device) per engine call.  Shared by the levels, so it outlives the engine if they do.
+struct BufferCache {
+    std::mutex mu;
+    std::multimap<size_t, void *> free;  // bytes -> buffer
+    ~BufferCache() {
+        for (auto &kv : free) cudaFree(kv.second);
+    }
+    void *take(size_t bytes, size_t &got) {  // best fit, at most twice the size asked for
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = free.lower_bound(bytes);
+        if (it == free.end() || it->first > 2 * bytes) return nullptr;
+        void *p = it->second;
+        got = it->first;
+        free.erase(it);
+        return p;
+    }
+    void give(void *p, size_t bytes) {
+        std::lock_guard<std::mutex> lk(mu);
+        free.emplace(bytes, p);
+    }
+};
+
 template <class T>
 struct DevBuf {
     T *p = nullptr;
     size_t n = 0;
+    size_t bytes = 0;
+    std::shared_ptr<BufferCache> cache;  // null: plain cudaMalloc / cudaFree
     DevBuf() = default;
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
     ~DevBuf() { release(); }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            if (cache) cache->give(p, bytes);
+            else cudaFree(p);
+        }
         p = nullptr;
         n = 0;
+        bytes = 0;
     }
     void ensure(size_t k) {
         if (k <= n && p) return;
         release();
-        const size_t bytes = sizeof(T) * std::max<size_t>(k, 1);
-        TFSM_CK(cudaMalloc((void **)&p, bytes));
-        n = std::max<size_t>(k, 1);
+        const size_t want = sizeof(T) * std::max<size_t>(k, 1);
+        size_t got = 0;
+        void *q = cache ? cache->take(want, got) : nullptr;
+        if (!q) {
+            TFSM_CK(cudaMalloc(&q, want));
+            got = want;
+        }
+        p = static_cast<T *>(q);
+        bytes = got;
+        n = got / sizeof(T);
     }
 };
 
@@ -60,7 +98,7 @@ using dev::PatStatus;
 }  // namespace
 
 struct Level::Impl {
-    DevBuf<uint32_t> dom, found, failed;
+    DevBuf<uint32_t> dom, found, failed;  // from the engine's BufferCache
     DevBuf<PatDesc> descs;
     std::vector<PatDesc> hdescs;
     uint64_t words = 0;
@@ -92,6 +130,7 @@ struct GpuEngine::Impl {
     DevBuf<dev::SplitGroup> groups;
     std::vector<PatStatus> hstatus;
     int device = 0;
+    std::shared_ptr<BufferCache> cache = std::make_shared<BufferCache>();
 };
 
 GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
@@ -261,10 +300,19 @@ void gql_plan(const Pattern &pat, const uint32_t *dsize, int start, uint8_t *ord
 void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::vector<int> &parent, const Level *prev,
                          uint32_t tau, const EngineOptions &opt, Level &out, std::vector<EvalResult> &res) {
     Impl &I = *impl_;
+    struct WallClock {  // host wall time of the whole call, every return path
+        double &acc;
+        std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+        ~WallClock() {
+            acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        }
+    } wall{times_.engine_ms};
     const size_t P = pats.size();
     res.assign(P, EvalResult());
     if (!out.impl) out.impl.reset(new Level::Impl);
     Level::Impl &L = *out.impl;
+    L.dom.cache = L.found.cache = L.failed.cache = I.cache;
+    L.descs.cache = I.cache;
     L.hdescs.assign(P, PatDesc());
     std::vector<char> trivial(P, 0), express(P, 0);
     uint64_t total = 0;
@@ -360,9 +408,13 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         TFSM_CK(cudaStreamSynchronize(I.stream));
         times_.d2h_bytes += P * sizeof(PatStatus);
     };
-    auto time_since_ev0 = [&]() -> double {
+    // end of a timed phase followed by a status read: one host round trip for both
+    auto time_and_read_status = [&]() -> double {
         TFSM_CK(cudaEventRecord(I.ev1, I.stream));
-        TFSM_CK(cudaEventSynchronize(I.ev1));
+        TFSM_CK(cudaMemcpyAsync(I.hstatus.data(), I.status.p, P * sizeof(PatStatus), cudaMemcpyDeviceToHost,
+                                I.stream));
+        TFSM_CK(cudaStreamSynchronize(I.stream));
+        times_.d2h_bytes += P * sizeof(PatStatus);
         float ms = 0;
         TFSM_CK(cudaEventElapsedTime(&ms, I.ev0, I.ev1));
         return ms;
@@ -376,11 +428,12 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         TFSM_CK(dev::launch_domain_init(I.g, L.descs.p, I.status.p, I.item_pu.p, I.prefix.p, (uint32_t)item_pu.size(),
                                         prefix.back(), L.dom.p, L.found.p, L.failed.p, pdom, pfailed, total,
                                         prev ? prev->impl->words : 0, I.stream));
-        times_.init_ms += time_since_ev0();
+        times_.init_ms += time_and_read_status();
         times_.init_launches++;
         times_.init_words += prefix.back();
+    } else {
+        read_status();
     }
-    read_status();
 
     // ---- arc-consistency rounds ----
     auto viable = [&](size_t p) {
@@ -408,10 +461,9 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         TFSM_CK(cudaEventRecord(I.ev0, I.stream));
         TFSM_CK(dev::launch_refine(I.g, L.descs.p, I.status.p, I.item_pu.p, I.prefix.p, (uint32_t)item_pu.size(),
                                    prefix.back(), L.dom.p, total, I.stream));
-        times_.refine_ms += time_since_ev0();
+        times_.refine_ms += time_and_read_status();
         times_.refine_launches++;
         times_.refine_words += prefix.back();
-        read_status();
     }
 
     // ---- decisions from domain sizes; plans for the rest ----
@@ -553,9 +605,12 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
                 ++launches;
             }
         }
+        TFSM_CK(cudaEventRecord(I.ev1, I.stream));
         TFSM_CK(cudaMemcpyAsync(hcnt, I.counters.p, sizeof(hcnt), cudaMemcpyDeviceToHost, I.stream));
+        TFSM_CK(cudaMemcpyAsync(I.hstatus.data(), I.status.p, P * sizeof(PatStatus), cudaMemcpyDeviceToHost,
+                                I.stream));
         TFSM_CK(cudaStreamSynchronize(I.stream));
-        times_.d2h_bytes += sizeof(hcnt);
+        times_.d2h_bytes += sizeof(hcnt) + P * sizeof(PatStatus);
         times_.split_groups += std::min<uint32_t>(hcnt[1], prm.group_cap);
         for (int r = 0; r < KernelTimes::kRoundSlots; ++r)
             times_.split_tasks[r] += std::min(hcnt[2 + r], prm.split_cap);
@@ -563,7 +618,11 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         times_.search_passes++;
         if (hcnt[dev::kDeferred] == 0) break;
     }
-    times_.search_ms += time_since_ev0();
+    {
+        float ms = 0;  // ev1 was recorded before the last pass's reads
+        TFSM_CK(cudaEventElapsedTime(&ms, I.ev0, I.ev1));
+        times_.search_ms += ms;
+    }
     times_.search_launches += launches;
     times_.search_calls++;
     {
@@ -573,7 +632,6 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
                                       " index " + std::to_string(rec[2]) + " bound " + std::to_string(rec[3]) +
                                       " (" + std::to_string(rec[0]) + " violations)");
     }
-    read_status();
 
     for (size_t p = 0; p < P; ++p) {
         if (!need_search[p]) continue;

@@ -171,10 +171,12 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                         nf += r.frequent ? 1 : 0;
                     }
                     std::fprintf(stderr,
-                                 "[level %d] %zu patterns (%llu frequent), search %.3f ms, %llu searches, longest "
-                                 "search %llu chunk steps\n",
-                                 st.levels + 1, b1 - b0, (unsigned long long)nf, eng.times().search_ms - search_before,
-                                 (unsigned long long)srch, (unsigned long long)mx);
+                                 "[level %d] %zu patterns (%llu frequent), engine call %.3f ms (init %.3f, refine "
+                                 "%.3f, search %.3f), %llu searches, longest search %llu chunk steps\n",
+                                 st.levels + 1, b1 - b0, (unsigned long long)nf, eng.times().engine_ms - before.engine_ms,
+                                 eng.times().init_ms - before.init_ms, eng.times().refine_ms - before.refine_ms,
+                                 eng.times().search_ms - search_before, (unsigned long long)srch,
+                                 (unsigned long long)mx);
                     const KernelTimes &now = eng.times();
                     if (now.split_groups > before.split_groups) {
                         std::fprintf(stderr, "          split: %llu searches, %llu passes, %llu deferred, tasks per round",
