@@ -159,6 +159,40 @@ int tfsm_evaluate_support_noalloc(tfsm_graph *g, const tfsm_pattern *pattern, in
 /* Message of the last failing call on this thread ("" when none). */
 const char *tfsm_last_error(void);
 
+/* ---- Learned matching-order cost model (no counterpart in the reference) ----------------------
+ * A 32-64-64-1 MLP (BF16 weights, FP32 accumulation) trained and evaluated on the GPU.  It predicts
+ * log2(1 + chunk evaluations per search) of searching a pattern vertex's candidates with a given
+ * matching order; with order policy 2 the engine takes the order with the lowest prediction.
+ * A matching order never changes a result, only the work. */
+#define TFSM_COST_FEATURES 32
+#define TFSM_COST_PARAMS 6337 /* W1[32][64], b1[64], W2[64][64], b2[64], W3[64], b3 (FP32 master copy) */
+
+typedef struct tfsm_cost_model tfsm_cost_model;
+
+int tfsm_cost_model_create(uint64_t seed, tfsm_cost_model **out); /* random initial weights */
+void tfsm_cost_model_free(tfsm_cost_model *m);
+int tfsm_cost_model_get_params(const tfsm_cost_model *m, float *params);
+int tfsm_cost_model_set_params(tfsm_cost_model *m, const float *params); /* resets the optimiser */
+int tfsm_cost_model_predict(const tfsm_cost_model *m, const float *features, uint64_t n, float *costs);
+/* Gradient of the mean squared error of one batch at the current weights (parameter layout). */
+int tfsm_cost_model_gradients(const tfsm_cost_model *m, const float *features, const float *costs, uint64_t n,
+                              float *grads);
+/* Adam over `epochs` shuffled passes in minibatches of `batch` (>= 16) records. */
+int tfsm_cost_model_train(tfsm_cost_model *m, const float *features, const float *costs, uint64_t n, int32_t epochs,
+                          int32_t batch, float lr, uint64_t seed, double *final_mse);
+
+/* Matching order of every searched pattern vertex on this handle: 0 the GQL order (default;
+ * the fixed-order path), 1 a random connected order drawn with `seed` (for logging training
+ * records), 2 the order the cost model predicts cheapest (GQL on ties).  The model must outlive its
+ * use by the handle. */
+int tfsm_set_order_policy(tfsm_graph *g, uint32_t policy, uint64_t seed, const tfsm_cost_model *model);
+/* While enabled, every engine call appends one training record per searched pattern vertex:
+ * TFSM_COST_FEATURES features of the order used and the measured cost. */
+int tfsm_record_orders(tfsm_graph *g, int32_t enable);
+/* Moves up to `cap` records out (features: cap x TFSM_COST_FEATURES); features == NULL only
+ * counts them into *n. */
+int tfsm_take_records(tfsm_graph *g, float *features, float *costs, uint64_t cap, uint64_t *n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,6 +1,10 @@
 // C-ABI boundary (declarations and the reference interface each entry point replaces:
 // include/tfsm.h).  Exceptions never cross it; errors become status codes + tfsm_last_error().
+#include <cuda_runtime.h>
+
+#include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -15,10 +19,16 @@
 struct tfsm_graph {
     tfsm::LgGraph lg;
     std::unique_ptr<tfsm::GpuEngine> eng;
-    tfsm::EngineOptions opt;  // tuning knobs (tfsm_set_options)
+    tfsm::EngineOptions opt;  // tuning knobs (tfsm_set_options), order policy and cost model
     int tau = 0;
     double load_ms = 0;
+    bool recording = false;
+    mutable std::vector<float> records;  // tfsm_record_orders: 33 floats per record
     std::mutex mu;
+};
+
+struct tfsm_cost_model {
+    std::unique_ptr<tfsm::CostModel> m;
 };
 
 namespace {
@@ -104,6 +114,7 @@ tfsm::EngineOptions engine_options(const tfsm_graph *g, uint32_t flags) {
     tfsm::EngineOptions o = g->opt;
     o.exact = (flags & TFSM_FLAG_EXACT) != 0;
     if (flags & TFSM_FLAG_NO_SPLIT) o.step_budget = 0;
+    o.records = g->recording ? &g->records : nullptr;
     return o;
 }
 
@@ -313,3 +324,112 @@ int tfsm_evaluate_support_noalloc(tfsm_graph *g, const tfsm_pattern *pattern, in
 const char *tfsm_last_error(void) { return g_err.c_str(); }
 
 }  // extern "C"
+
+// ---- learned matching-order cost model ----
+
+int tfsm_cost_model_create(uint64_t seed, tfsm_cost_model **out) {
+    return guarded([&]() -> int {
+        if (!out) return fail(TFSM_ERR_ARG, "null argument");
+        *out = nullptr;
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(TFSM_ERR_NO_DEVICE, "no CUDA device");
+        int device = 0;
+        if (const char *env = std::getenv("TFSM_DEVICE")) device = std::atoi(env);
+        if (device < 0 || device >= ndev) return fail(TFSM_ERR_NO_DEVICE, "TFSM_DEVICE names no CUDA device");
+        std::unique_ptr<tfsm_cost_model> m(new tfsm_cost_model);
+        m->m.reset(new tfsm::CostModel(seed, device));
+        *out = m.release();
+        return TFSM_OK;
+    });
+}
+
+void tfsm_cost_model_free(tfsm_cost_model *m) { delete m; }
+
+int tfsm_cost_model_get_params(const tfsm_cost_model *m, float *params) {
+    return guarded([&]() -> int {
+        if (!m || !params) return fail(TFSM_ERR_ARG, "null argument");
+        const std::vector<float> p = m->m->params();
+        std::memcpy(params, p.data(), p.size() * sizeof(float));
+        return TFSM_OK;
+    });
+}
+
+int tfsm_cost_model_set_params(tfsm_cost_model *m, const float *params) {
+    return guarded([&]() -> int {
+        if (!m || !params) return fail(TFSM_ERR_ARG, "null argument");
+        m->m->set_params(params);
+        return TFSM_OK;
+    });
+}
+
+int tfsm_cost_model_predict(const tfsm_cost_model *m, const float *features, uint64_t n, float *costs) {
+    return guarded([&]() -> int {
+        if (!m || (n && (!features || !costs))) return fail(TFSM_ERR_ARG, "null argument");
+        m->m->predict(features, (size_t)n, costs);
+        return TFSM_OK;
+    });
+}
+
+int tfsm_cost_model_gradients(const tfsm_cost_model *m, const float *features, const float *costs, uint64_t n,
+                              float *grads) {
+    return guarded([&]() -> int {
+        if (!m || !features || !costs || !grads || n == 0) return fail(TFSM_ERR_ARG, "null argument or empty batch");
+        m->m->gradients(features, costs, (size_t)n, grads);
+        return TFSM_OK;
+    });
+}
+
+int tfsm_cost_model_train(tfsm_cost_model *m, const float *features, const float *costs, uint64_t n, int32_t epochs,
+                          int32_t batch, float lr, uint64_t seed, double *final_mse) {
+    return guarded([&]() -> int {
+        if (!m || !features || !costs || n == 0) return fail(TFSM_ERR_ARG, "null argument or no records");
+        if (epochs < 0 || batch < 16 || !(lr > 0)) return fail(TFSM_ERR_ARG, "epochs >= 0, batch >= 16, lr > 0");
+        const double mse = m->m->train(features, costs, (size_t)n, epochs, batch, lr, seed);
+        if (final_mse) *final_mse = mse;
+        return TFSM_OK;
+    });
+}
+
+int tfsm_set_order_policy(tfsm_graph *g, uint32_t policy, uint64_t seed, const tfsm_cost_model *model) {
+    return guarded([&]() -> int {
+        if (!g) return fail(TFSM_ERR_ARG, "null argument");
+        if (policy > 2) return fail(TFSM_ERR_ARG, "order policy must be 0 (GQL), 1 (random) or 2 (cost model)");
+        if (policy == 2 && !model) return fail(TFSM_ERR_ARG, "order policy 2 needs a cost model");
+        std::lock_guard<std::mutex> lk(g->mu);
+        g->opt.order_policy = policy;
+        g->opt.order_seed = seed;
+        g->opt.cost_model = policy == 2 ? model->m.get() : nullptr;
+        return TFSM_OK;
+    });
+}
+
+int tfsm_record_orders(tfsm_graph *g, int32_t enable) {
+    return guarded([&]() -> int {
+        if (!g) return fail(TFSM_ERR_ARG, "null argument");
+        std::lock_guard<std::mutex> lk(g->mu);
+        g->recording = enable != 0;
+        return TFSM_OK;
+    });
+}
+
+int tfsm_take_records(tfsm_graph *g, float *features, float *costs, uint64_t cap, uint64_t *n) {
+    return guarded([&]() -> int {
+        if (!g || !n) return fail(TFSM_ERR_ARG, "null argument");
+        std::lock_guard<std::mutex> lk(g->mu);
+        constexpr size_t W = TFSM_COST_FEATURES + 1;
+        const uint64_t have = g->records.size() / W;
+        if (!features) {
+            *n = have;
+            return TFSM_OK;
+        }
+        if (!costs) return fail(TFSM_ERR_ARG, "null argument");
+        const uint64_t k = std::min(have, cap);
+        for (uint64_t i = 0; i < k; ++i) {
+            std::memcpy(features + i * TFSM_COST_FEATURES, &g->records[i * W], TFSM_COST_FEATURES * sizeof(float));
+            costs[i] = g->records[i * W + TFSM_COST_FEATURES];
+        }
+        g->records.erase(g->records.begin(), g->records.begin() + (ptrdiff_t)(k * W));
+        *n = k;
+        return TFSM_OK;
+    });
+}

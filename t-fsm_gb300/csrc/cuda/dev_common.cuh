@@ -70,6 +70,8 @@ struct PatStatus {
     unsigned long long steps;         // candidate chunks evaluated by the search
     unsigned long long bytes;         // algorithmic bytes read by the search (logical loads)
     unsigned long long max_steps;     // longest single search (chunk evaluations)
+    unsigned long long steps_u[kMaxN];  // chunk evaluations spent on u's candidates (incl. splits)
+    uint32_t searches_u[kMaxN];         // searches started for u's candidates
 };
 
 enum : uint32_t { kRunning = 0, kFrequent = 1, kInfrequent = 2 };

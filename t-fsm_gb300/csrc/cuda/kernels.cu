@@ -765,6 +765,8 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
             atomicAdd(&ps.steps, n_steps);
             atomicAdd(&ps.bytes, n_bytes);
             atomicMax(&ps.max_steps, max_steps);
+            atomicAdd(&ps.steps_u[u], n_steps);
+            atomicAdd(&ps.searches_u[u], (uint32_t)n_search);
         }
         if (abandon) {
             if (lane == 0) atomicAdd(&counters[kDeferred], 1u);
@@ -843,6 +845,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_split(Graph g, const PatD
                 atomicAdd(&ps.steps, (unsigned long long)steps);
                 atomicAdd(&ps.bytes, wb);
                 atomicMax(&ps.max_steps, (unsigned long long)steps);
+                atomicAdd(&ps.steps_u[u], (unsigned long long)steps);
             }
             searched = r != kCancel;
         }

@@ -14,13 +14,17 @@
 #include <chrono>
 #include <cstdlib>
 #include <cstring>
+#include <array>
+#include <cmath>
 #include <map>
 #include <mutex>
+#include <random>
 #include <numeric>
 
 #include "cuda/dev_common.cuh"
 #include "cuda/kernels.h"
 #include "engine.hpp"
+#include "costmodel/features.hpp"
 #include "host/lg_fast.hpp"
 
 namespace tfsm {
@@ -116,6 +120,7 @@ struct GpuEngine::Impl {
     DevBuf<uint8_t> elab;
     std::map<int, int> vdense, edense;
     std::vector<uint32_t> lstart;  // host copy, n_labels + 1
+    std::vector<float> label_mean_deg;  // per dense label: mean degree of its vertices
     uint32_t n = 0;
     uint64_t m2 = 0;
     cudaStream_t stream = nullptr;
@@ -161,6 +166,13 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     for (uint32_t v = 0; v < lg.n; ++v) to_int[v] = fillv[(size_t)dl[v]]++;
     std::vector<uint32_t> from_int(lg.n);
     for (uint32_t v = 0; v < lg.n; ++v) from_int[to_int[v]] = v;
+    {
+        std::vector<double> dsum((size_t)NL, 0.0);
+        for (uint32_t v = 0; v < lg.n; ++v) dsum[(size_t)dl[v]] += lg.degree(v);
+        I.label_mean_deg.assign((size_t)NL, 0.f);
+        for (int L = 0; L < NL; ++L)
+            if (cnt[(size_t)L + 1]) I.label_mean_deg[(size_t)L] = (float)(dsum[(size_t)L] / cnt[(size_t)L + 1]);
+    }
     // CSR in internal ids, each list sorted by (internal id, edge label): row x is v's list mapped
     // through to_int and re-sorted (ids of one label keep their order, labels are regrouped).
     std::vector<uint32_t> off((size_t)lg.n + 1, 0);
@@ -498,6 +510,72 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
             if (D.rep[u] == u) gql_plan(*pats[p], s.dom_size, u, D.order[u], D.bn[u]);
     }
     if (!any_search) return;
+
+    // ---- matching orders other than GQL (cost model / random for logging); record features ----
+    struct Planned {
+        uint32_t p;
+        int u;
+        std::array<float, costmodel::kFeatures> f;
+    };
+    std::vector<Planned> planned;
+    if (opt.order_policy != 0 || opt.records) {
+        const auto t_ord = std::chrono::steady_clock::now();
+        std::mt19937_64 rng(opt.order_seed * 0x9E3779B97F4A7C15ull + times_.search_calls + 1);
+        auto set_order = [](PatDesc &D, int u, const costmodel::Order &o) {
+            for (int i = 0; i < D.n; ++i) {
+                D.order[u][i] = o[(size_t)i];
+                D.bn[u][i] = costmodel::backward_mask(D, o, i);
+            }
+        };
+        std::vector<float> X;                                       // model inputs, all candidates
+        std::vector<std::pair<size_t, size_t>> span;                // per planned entry: [first, count)
+        std::vector<std::vector<costmodel::Order>> cands;
+        for (size_t p = 0; p < P; ++p) {
+            if (!need_search[p]) continue;
+            PatDesc &D = L.hdescs[p];
+            for (int u = 0; u < D.n; ++u) {
+                if (D.rep[u] != u) continue;
+                costmodel::Order gq{};
+                for (int i = 0; i < D.n; ++i) gq[(size_t)i] = D.order[u][i];
+                std::vector<costmodel::Order> cand{gq};  // the GQL order first: it wins ties
+                if (opt.order_policy != 0) {
+                    std::vector<costmodel::Order> all;
+                    costmodel::enumerate_orders(D, u, 128, all);
+                    for (auto &o : all)
+                        if (o != gq) cand.push_back(o);
+                }
+                if (opt.order_policy == 1) set_order(D, u, cand[rng() % cand.size()]);
+                if (opt.order_policy == 2 && opt.cost_model) {
+                    span.emplace_back(X.size() / costmodel::kFeatures, cand.size());
+                    for (auto &o : cand) {
+                        std::array<float, costmodel::kFeatures> f;
+                        costmodel::order_features(D, I.hstatus[p].dom_size, tau, I.label_mean_deg.data(), o, f.data());
+                        X.insert(X.end(), f.begin(), f.end());
+                    }
+                    cands.push_back(std::move(cand));
+                }
+                planned.push_back({(uint32_t)p, u, {}});
+            }
+        }
+        if (opt.order_policy == 2 && opt.cost_model && !X.empty()) {
+            std::vector<float> y(X.size() / costmodel::kFeatures);
+            opt.cost_model->predict(X.data(), y.size(), y.data());
+            for (size_t k = 0; k < planned.size(); ++k) {
+                size_t best = 0;
+                for (size_t j = 1; j < span[k].second; ++j)
+                    if (y[span[k].first + j] < y[span[k].first + best]) best = j;
+                set_order(L.hdescs[planned[k].p], planned[k].u, cands[k][best]);
+            }
+        }
+        for (auto &pl : planned) {
+            const PatDesc &D = L.hdescs[pl.p];
+            costmodel::Order o{};
+            for (int i = 0; i < D.n; ++i) o[(size_t)i] = D.order[pl.u][i];
+            costmodel::order_features(D, I.hstatus[pl.p].dom_size, tau, I.label_mean_deg.data(), o, pl.f.data());
+        }
+        times_.order_ms +=
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_ord).count();
+    }
     TFSM_CK(cudaMemcpyAsync(L.descs.p, L.hdescs.data(), P * sizeof(PatDesc), cudaMemcpyHostToDevice, I.stream));
     times_.h2d_bytes += P * sizeof(PatDesc);
 
@@ -632,6 +710,15 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
                                       " index " + std::to_string(rec[2]) + " bound " + std::to_string(rec[3]) +
                                       " (" + std::to_string(rec[0]) + " violations)");
     }
+
+    if (opt.records)
+        for (auto &pl : planned) {
+            const PatStatus &s = I.hstatus[pl.p];
+            if (!s.searches_u[pl.u]) continue;  // nothing was searched with this order
+            opt.records->insert(opt.records->end(), pl.f.begin(), pl.f.end());
+            opt.records->push_back(
+                (float)std::log2(1.0 + (double)s.steps_u[pl.u] / (double)s.searches_u[pl.u]));
+        }
 
     for (size_t p = 0; p < P; ++p) {
         if (!need_search[p]) continue;

@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 
+#include "costmodel/mlp.hpp"
 #include "host/lg_graph.hpp"
 #include "host/pattern.hpp"
 
@@ -41,6 +42,15 @@ struct EngineOptions {
     uint32_t refine_rounds = 2;        // arc-consistency passes for patterns that need search
     uint32_t max_batch = 4096;         // miner: patterns per engine call
     double time_limit_s = 0;           // miner: stop between engine calls after this long (0: none)
+    // Matching order of each searched pattern vertex (never changes a result):
+    //   0: GQL order (fewest candidates next), 1: a random connected order (seeded; used to log
+    //   training records), 2: the order with the lowest cost predicted by `cost_model`
+    uint32_t order_policy = 0;
+    uint64_t order_seed = 0;
+    const CostModel *cost_model = nullptr;
+    // when set, one record per searched pattern vertex is appended: 32 features of the order used
+    // (costmodel/features.hpp) and log2(1 + chunk evaluations per search) measured for it
+    std::vector<float> *records = nullptr;
 };
 
 struct KernelTimes {                   // accumulated device time (CUDA events), milliseconds
@@ -54,6 +64,7 @@ struct KernelTimes {                   // accumulated device time (CUDA events),
     static constexpr int kRoundSlots = 65;      // split rounds + one
     uint64_t split_groups = 0;                  // searches handed to the split rounds
     uint64_t deferred = 0;                      // searches left for another pass (buffers full)
+    double order_ms = 0;                        // host + cost-model time spent choosing orders
     uint64_t search_passes = 0;
     uint64_t split_tasks[kRoundSlots] = {};     // tasks written for each split round
 };

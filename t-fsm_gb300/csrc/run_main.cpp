@@ -2,7 +2,7 @@
 //
 //   run -file G.lg -freq TAU [-thread T] [-maxNodes N] [-plain] [-exact] [-out PATH]
 //       [-step-budget B] [-split-slice S] [-chunk-words W] [-refine-rounds R] [-max-batch M]
-//       [-split-rounds K] [-round-budget B] [-time-limit SECONDS]
+//       [-split-rounds K] [-round-budget B] [-time-limit SECONDS] [-random-orders SEED]
 //
 // Frequent patterns go to ./grami_results.txt (or -out PATH) in the serial build's format
 // (serial/grami.h:622-635); timing and counts are printed as the parallel build prints them.
@@ -58,6 +58,8 @@ int main(int argc, char **argv) {
     if (opt(argc, argv, "-round-budget")) o.round_budget = (uint32_t)std::atoi(opt(argc, argv, "-round-budget"));
     if (opt(argc, argv, "-time-limit")) o.time_limit_s = std::atof(opt(argc, argv, "-time-limit"));
     rc = tfsm_set_options(g, &o);
+    if (rc == TFSM_OK && opt(argc, argv, "-random-orders"))  // random matching orders: same results
+        rc = tfsm_set_order_policy(g, 1, (uint64_t)std::atoll(opt(argc, argv, "-random-orders")), nullptr);
     if (rc != TFSM_OK) {
         std::fprintf(stderr, "error %d: %s\n", rc, tfsm_last_error());
         tfsm_graph_free(g);

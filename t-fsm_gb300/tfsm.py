@@ -40,8 +40,22 @@ EXPORTED = (
     "tfsm_get_options",
     "tfsm_set_options",
     "tfsm_evaluate_support_noalloc",
+    "tfsm_cost_model_create",
+    "tfsm_cost_model_free",
+    "tfsm_cost_model_get_params",
+    "tfsm_cost_model_set_params",
+    "tfsm_cost_model_predict",
+    "tfsm_cost_model_gradients",
+    "tfsm_cost_model_train",
+    "tfsm_set_order_policy",
+    "tfsm_record_orders",
+    "tfsm_take_records",
     "tfsm_last_error",
 )
+
+COST_FEATURES = 32
+COST_PARAMS = 6337
+ORDER_GQL, ORDER_RANDOM, ORDER_MODEL = 0, 1, 2
 
 
 class TfsmError(RuntimeError):
@@ -114,10 +128,23 @@ def lib() -> C.CDLL:
         L.tfsm_set_options.argtypes = [C.c_void_p, C.POINTER(OptionsC)]
         L.tfsm_evaluate_support_noalloc.argtypes = [C.c_void_p, C.POINTER(PatternC), C.c_int32, C.c_uint32,
                                                     C.POINTER(ResultC)]
+        fp = C.POINTER(C.c_float)
+        L.tfsm_cost_model_create.argtypes = [C.c_uint64, C.POINTER(C.c_void_p)]
+        L.tfsm_cost_model_free.argtypes = [C.c_void_p]
+        L.tfsm_cost_model_free.restype = None
+        L.tfsm_cost_model_get_params.argtypes = [C.c_void_p, fp]
+        L.tfsm_cost_model_set_params.argtypes = [C.c_void_p, fp]
+        L.tfsm_cost_model_predict.argtypes = [C.c_void_p, fp, C.c_uint64, fp]
+        L.tfsm_cost_model_gradients.argtypes = [C.c_void_p, fp, fp, C.c_uint64, fp]
+        L.tfsm_cost_model_train.argtypes = [C.c_void_p, fp, fp, C.c_uint64, C.c_int32, C.c_int32, C.c_float,
+                                            C.c_uint64, C.POINTER(C.c_double)]
+        L.tfsm_set_order_policy.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64, C.c_void_p]
+        L.tfsm_record_orders.argtypes = [C.c_void_p, C.c_int32]
+        L.tfsm_take_records.argtypes = [C.c_void_p, fp, fp, C.c_uint64, C.POINTER(C.c_uint64)]
         L.tfsm_last_error.argtypes = []
         L.tfsm_last_error.restype = C.c_char_p
         for f in EXPORTED:
-            if f not in ("tfsm_graph_free", "tfsm_last_error"):
+            if f not in ("tfsm_graph_free", "tfsm_last_error", "tfsm_cost_model_free"):
                 getattr(L, f).restype = C.c_int
         _lib = L
     return _lib
@@ -228,6 +255,25 @@ class Graph:
         o = OptionsC(**cur)
         _check(lib().tfsm_set_options(self._h, C.byref(o)))
 
+    def set_order_policy(self, policy: int, seed: int = 0, model: "CostModel | None" = None) -> None:
+        self._model = model  # kept alive while the handle may use it
+        _check(lib().tfsm_set_order_policy(self._h, policy, seed, model._h if model else None))
+
+    def record_orders(self, enable: bool = True) -> None:
+        _check(lib().tfsm_record_orders(self._h, 1 if enable else 0))
+
+    def take_records(self):
+        """(features [n x 32] float32, costs [n] float32) recorded so far; clears them."""
+        import numpy as np
+
+        n = C.c_uint64(0)
+        _check(lib().tfsm_take_records(self._h, None, None, 0, C.byref(n)))
+        f = np.zeros((n.value, COST_FEATURES), dtype=np.float32)
+        c = np.zeros(n.value, dtype=np.float32)
+        got = C.c_uint64(0)
+        _check(lib().tfsm_take_records(self._h, _fptr(f), _fptr(c), n.value, C.byref(got)))
+        return f[: got.value], c[: got.value]
+
     def mine(self, max_nodes: int = -1, flags: int = 0, results_path: str | Path | None = None,
              tau: int | None = None) -> dict:
         st = MineStatsC()
@@ -235,6 +281,71 @@ class Graph:
         _check(lib().tfsm_mine(self._h, int(self.tau if tau is None else tau), int(max_nodes), int(flags), p,
                                C.byref(st)))
         return {f: getattr(st, f) for f, _ in MineStatsC._fields_}
+
+
+def _fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class CostModel:
+    """The learned matching-order cost model (32-64-64-1 MLP, BF16 weights, trained on the GPU)."""
+
+    def __init__(self, seed: int = 0):
+        h = C.c_void_p()
+        _check(lib().tfsm_cost_model_create(seed, C.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().tfsm_cost_model_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self):
+        import numpy as np
+
+        p = np.zeros(COST_PARAMS, dtype=np.float32)
+        _check(lib().tfsm_cost_model_get_params(self._h, _fptr(p)))
+        return p
+
+    def set_params(self, p) -> None:
+        import numpy as np
+
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.shape == (COST_PARAMS,)
+        _check(lib().tfsm_cost_model_set_params(self._h, _fptr(p)))
+
+    def predict(self, x):
+        import numpy as np
+
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, COST_FEATURES)
+        y = np.zeros(len(x), dtype=np.float32)
+        _check(lib().tfsm_cost_model_predict(self._h, _fptr(x), len(x), _fptr(y)))
+        return y
+
+    def gradients(self, x, t):
+        import numpy as np
+
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, COST_FEATURES)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        g = np.zeros(COST_PARAMS, dtype=np.float32)
+        _check(lib().tfsm_cost_model_gradients(self._h, _fptr(x), _fptr(t), len(x), _fptr(g)))
+        return g
+
+    def train(self, x, t, epochs: int = 20, batch: int = 256, lr: float = 1e-3, seed: int = 0) -> float:
+        import numpy as np
+
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, COST_FEATURES)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        mse = C.c_double(0)
+        _check(lib().tfsm_cost_model_train(self._h, _fptr(x), _fptr(t), len(x), epochs, batch, lr, seed,
+                                           C.byref(mse)))
+        return mse.value
 
 
 def read_results(path: str | Path) -> list[str]:

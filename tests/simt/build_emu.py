@@ -23,7 +23,7 @@ def build(kind: str = "asan") -> Path:
     out_dir.mkdir(exist_ok=True)
     exe = out_dir / f"run_emu_{kind}"
     srcs = [CSRC / "cuda" / "kernels.cu", CSRC / "engine.cu", CSRC / "noalloc.cu", CSRC / "miner.cpp",
-            CSRC / "capi.cpp", CSRC / "run_main.cpp"]
+            CSRC / "capi.cpp", CSRC / "run_main.cpp", HERE / "costmodel_stub.cpp"]
     deps = srcs + list(CSRC.rglob("*.h*")) + list(CSRC.rglob("*.cuh")) + [HERE / "cuda_runtime.h"]
     if exe.exists() and all(d.stat().st_mtime <= exe.stat().st_mtime for d in deps):
         return exe

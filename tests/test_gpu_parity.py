@@ -207,3 +207,19 @@ def test_split_buffers_full_keep_results(built, case_graph, case, tmp_path):
                         "32", "-out", str(out)], capture_output=True, text=True, timeout=300, env=env)
     assert r.returncode == 0, r.stderr
     assert set(read_results(out)) == golden_pattern_set(case)
+
+
+@pytest.mark.parametrize("case", ["cfg1", "el3", "clique", "quirk_elabels"])
+@pytest.mark.parametrize("seed", [1, 2])
+def test_random_matching_orders_keep_results(tfsm, case_graph, case, seed, tmp_path):
+    """Any connected matching order finds the same embeddings: pattern set and exact supports."""
+    c = CASES[case]
+    with tfsm.Graph.load(case_graph(case), c["tau"]) as g:
+        g.set_order_policy(tfsm.ORDER_RANDOM, seed=seed)
+        pats, _ = mine_set(tfsm, g, case, tmp_path)
+        assert pats == golden_pattern_set(case)
+        want = golden_mni(case)
+        if want:
+            keys = list(want)[:200]
+            res = g.evaluate([tfsm.parse_key(k) for k in keys], flags=tfsm.FLAG_EXACT)
+            assert [r.mni for r in res] == [want[k] for k in keys]
