@@ -236,6 +236,43 @@ def reference_arm(args, w, world, rank):
     return 0
 
 
+def mlp_arm(args, w, g, tfsm, one_step, batched_results: Path) -> dict:
+    import numpy as np
+
+    feats, costs = [], []
+    for k in range(3):
+        wk = dict(w, gen=dict(w["gen"], seed=w["gen"]["seed"] + 10 + k))
+        with tfsm.Graph.load(make_graph(wk), w["tau"]) as gt:
+            gt.set_order_policy(tfsm.ORDER_RANDOM, seed=k + 1)
+            gt.record_orders(True)
+            gt.mine(max_nodes=w["max_nodes"], flags=tfsm.FLAG_PLAIN)
+            f, c = gt.take_records()
+            feats.append(f)
+            costs.append(c)
+    x, t = np.concatenate(feats), np.concatenate(costs)
+    model = tfsm.CostModel(seed=1)
+    t0 = time.perf_counter()
+    mse = model.train(x, t, epochs=60, batch=64, lr=2e-3, seed=2)
+    train_s = time.perf_counter() - t0
+    g.set_order_policy(tfsm.ORDER_MODEL, model=model)
+    try:
+        outm = Path(tempfile.mktemp(suffix=".m.txt"))
+        g.mine(max_nodes=w["max_nodes"], results_path=outm)
+        identical = set(tfsm.read_results(outm)) == set(tfsm.read_results(batched_results))
+        for _ in range(args.warmup):
+            one_step(0)
+        runs = [one_step(0) for _ in range(args.steps)]
+    finally:
+        g.set_order_policy(tfsm.ORDER_GQL)
+    ms = sum(r[0] for r in runs) / len(runs)
+    st = runs[0][2]
+    model.close()
+    return {"value": st["evaluations"] * 1e3 / ms, "ms_per_step": ms, "identical_output": identical,
+            "search_ms_per_step": sum(r[2]["search_ms"] for r in runs) / len(runs),
+            "steps_per_run": st["steps"], "training_records": int(len(x)), "train_mse": mse,
+            "train_s": train_s, "training_graphs": "workload shape, seeds +10..+12, plain miner, random orders"}
+
+
 def gpu_arm(args, w, world, rank):
     import torch
 
@@ -287,6 +324,10 @@ def gpu_arm(args, w, world, rank):
     pms = [one_step(tfsm.FLAG_PLAIN)[0] for _ in range(max(1, args.steps // 2))]
     plain_ms = max_over_ranks(world, sum(pms) / len(pms))
 
+    # batched + learned matching orders: a cost model trained on records that the plain miner logs
+    # (random connected orders) on three training graphs of the workload's shape (other seeds)
+    mlp = mlp_arm(args, w, g, tfsm, one_step, outb)
+
     # roofline of the dominant kernel (the search): algorithmic bytes / device time
     s_ms = sum(st["search_ms"] for st in stats)
     s_bytes = sum(st["search_bytes"] for st in stats)
@@ -335,6 +376,7 @@ def gpu_arm(args, w, world, rank):
             "plain": {"value": evals * 1e3 / plain_ms, "ms_per_step": plain_ms,
                       "engine_calls": stats[0]["evaluations"]},
             "batched_over_plain": plain_ms / step_ms, "identical_output": identical,
+            "batched_mlp": mlp,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "kernel": "k_search (+k_split)",
                          "peak_kind": peak_kind,

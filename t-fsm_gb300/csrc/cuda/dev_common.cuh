@@ -64,7 +64,7 @@ struct PatStatus {
     uint32_t fail_cnt[kMaxN];
     uint32_t done_mask;     // representatives whose found count reached tau
     uint32_t state;         // 0 running, 1 frequent, 2 infrequent
-    uint32_t changed;       // set by a refinement pass that removed a candidate
+    uint32_t changed;       // bit r: refinement round r removed a candidate
     uint32_t pad;
     unsigned long long searches;      // candidate checks started
     unsigned long long steps;         // candidate chunks evaluated by the search

@@ -164,10 +164,14 @@ __global__ void __launch_bounds__(256) k_domain_init(Graph g, const PatDesc *__r
 // ------------------------------------------------------------------------------------------------
 constexpr uint32_t kLaneScan = 16;  // k_refine: longest label range a single lane scans
 
+// One arc-consistency round `round` (< 32).  A pattern takes part while every domain can still
+// reach tau (any non-empty domain in exact mode) and, after the first round, while the previous
+// round removed something from it (bit round - 1 of `changed`); a removal sets bit `round`.
 __global__ void __launch_bounds__(256) k_refine(Graph g, const PatDesc *__restrict__ descs, PatStatus *__restrict__ st,
                                                 const uint32_t *__restrict__ item_pu,
                                                 const uint64_t *__restrict__ prefix, uint32_t n_items,
-                                                uint32_t *__restrict__ dom, uint64_t chk_words) {
+                                                uint32_t *__restrict__ dom, uint64_t chk_words, int round,
+                                                uint32_t tau, int exact) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -180,6 +184,16 @@ __global__ void __launch_bounds__(256) k_refine(Graph g, const PatDesc *__restri
         const PatDesc &D = descs[p];
         const uint32_t word = (uint32_t)(gw - prefix[item]);
         if (!TFSM_IN(34, D.off[u] + word, chk_words)) continue;
+        int skip = 0;
+        if (lane == 0) {
+            const PatStatus &ps = st[p];
+            skip = round > 0 && !((__ldcg(&ps.changed) >> (round - 1)) & 1u);
+            for (int w = 0; w < D.n && !skip; ++w) {
+                const uint32_t ds = __ldcg(&ps.dom_size[w]);
+                skip = exact ? ds == 0 : ds < tau;
+            }
+        }
+        if (__shfl_sync(0xffffffffu, skip, 0)) continue;
         uint32_t *wp = dom + D.off[u] + word;
         // other warps clear bits of this pool concurrently: one read, broadcast, keeps the warp's
         // control flow (and its collectives) uniform
@@ -254,7 +268,7 @@ __global__ void __launch_bounds__(256) k_refine(Graph g, const PatDesc *__restri
         if (keep != w0 && lane == 0) {
             atomicAnd(wp, keep);
             atomicSub(&st[p].dom_size[u], (uint32_t)__popc(w0 & ~keep));
-            atomicOr(&st[p].changed, 1u);
+            atomicOr(&st[p].changed, 1u << round);
         }
     }
 }
@@ -931,12 +945,14 @@ cudaError_t launch_domain_init(const Graph &g, const PatDesc *descs, PatStatus *
 
 cudaError_t launch_refine(const Graph &g, const PatDesc *descs, PatStatus *st, const uint32_t *item_pu,
                           const uint64_t *prefix, uint32_t n_items, uint64_t total_words, uint32_t *dom,
-                          uint64_t chk_words, cudaStream_t s) {
+                          uint64_t chk_words, int round, uint32_t tau, bool exact, cudaStream_t s) {
     if (n_items == 0 || total_words == 0) return cudaSuccess;
+    if (round < 0 || round >= 32) return cudaErrorInvalidValue;
     uint64_t blocks = (total_words * 32 + 255) / 256;
     const uint64_t cap = (uint64_t)num_sms() * 8 * 4;
     if (blocks > cap) blocks = cap;
-    TFSM_LAUNCH(k_refine, (unsigned)blocks, 256, s, g, descs, st, item_pu, prefix, n_items, dom, chk_words);
+    TFSM_LAUNCH(k_refine, (unsigned)blocks, 256, s, g, descs, st, item_pu, prefix, n_items, dom, chk_words, round,
+                tau, exact ? 1 : 0);
 #ifdef TFSM_BOUNDS_CHECK
     if (cudaStreamSynchronize(s) != cudaSuccess) return cudaGetLastError();
 #endif

@@ -15,9 +15,11 @@ cudaError_t launch_domain_init(const Graph &g, const PatDesc *descs, PatStatus *
                                uint32_t *found, uint32_t *failed, const uint32_t *pdom, const uint32_t *pfailed,
                                uint64_t chk_words, uint64_t chk_pwords, cudaStream_t s);
 
+// Arc-consistency round `round` (0..31) over the items' words; see k_refine for which patterns
+// take part.
 cudaError_t launch_refine(const Graph &g, const PatDesc *descs, PatStatus *st, const uint32_t *item_pu,
                           const uint64_t *prefix, uint32_t n_items, uint64_t total_words, uint32_t *dom,
-                          uint64_t chk_words, cudaStream_t s);
+                          uint64_t chk_words, int round, uint32_t tau, bool exact, cudaStream_t s);
 
 // The search pass: k_search over `prm.n_items` items.  `counters` (kNumCounters x u32) must be
 // zero on entry; `splits` holds two buffers of prm.split_cap tasks each.

@@ -99,6 +99,58 @@ struct DevBuf {
 using dev::PatDesc;
 using dev::PatStatus;
 
+// An event record inside a captured launch sequence: captured as an event-record node (plain
+// records inside a capture only order streams), so that it can time the graph's kernels.
+inline cudaError_t record_in_sequence(cudaEvent_t e, cudaStream_t s) {
+#if defined(TFSM_SIMT_EMULATION) || defined(TFSM_BOUNDS_CHECK)
+    return cudaEventRecord(e, s);
+#else
+    return cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+#endif
+}
+
+// Records the launches of `enqueue` on stream `s` as a CUDA graph and runs it.  `exec` keeps the
+// instantiated graph between calls: a sequence of the same shape (same kernels, new arguments)
+// is applied with cudaGraphExecUpdate instead of a new instantiation.  The checked build (which
+// synchronises inside its launchers) and the CPU emulation launch directly.
+template <class F>
+void run_captured(cudaStream_t s, cudaGraphExec_t &exec, F enqueue) {
+#if defined(TFSM_SIMT_EMULATION) || defined(TFSM_BOUNDS_CHECK)
+    (void)exec;
+    (void)s;
+    enqueue();
+#else
+    TFSM_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaGraph_t graph = nullptr;
+    try {
+        enqueue();
+    } catch (...) {
+        cudaStreamEndCapture(s, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        throw;
+    }
+    TFSM_CK(cudaStreamEndCapture(s, &graph));
+    if (exec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(exec, graph, &info) != cudaSuccess) {
+            (void)cudaGetLastError();
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
+        }
+    }
+    if (!exec) {
+        const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+        if (e != cudaSuccess) {
+            exec = nullptr;
+            cudaGraphDestroy(graph);
+            TFSM_CK(e);
+        }
+    }
+    cudaGraphDestroy(graph);
+    TFSM_CK(cudaGraphLaunch(exec, s));
+#endif
+}
+
 }  // namespace
 
 struct Level::Impl {
@@ -124,7 +176,9 @@ struct GpuEngine::Impl {
     uint32_t n = 0;
     uint64_t m2 = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_mid = nullptr;
+    // instantiated launch sequences, updated in place while their shape stays the same
+    cudaGraphExec_t exec_init = nullptr, exec_search = nullptr;
     // per-call scratch
     DevBuf<PatStatus> status;
     DevBuf<uint32_t> item_pu;
@@ -210,6 +264,7 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     TFSM_CK(cudaStreamCreateWithFlags(&I.stream, cudaStreamNonBlocking));
     TFSM_CK(cudaEventCreate(&I.ev0));
     TFSM_CK(cudaEventCreate(&I.ev1));
+    TFSM_CK(cudaEventCreate(&I.ev_mid));
     I.row_off.ensure(off.size());
     I.col.ensure(col.size());
     I.elab.ensure(el.size());
@@ -255,8 +310,11 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
 GpuEngine::~GpuEngine() {
     if (impl_) {
         if (impl_->stream) cudaStreamSynchronize(impl_->stream);
+        if (impl_->exec_init) cudaGraphExecDestroy(impl_->exec_init);
+        if (impl_->exec_search) cudaGraphExecDestroy(impl_->exec_search);
         if (impl_->ev0) cudaEventDestroy(impl_->ev0);
         if (impl_->ev1) cudaEventDestroy(impl_->ev1);
+        if (impl_->ev_mid) cudaEventDestroy(impl_->ev_mid);
         if (impl_->stream) cudaStreamDestroy(impl_->stream);
     }
 }
@@ -432,22 +490,43 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         return ms;
     };
 
+    // ---- domain init and the first arc-consistency rounds: one launch sequence (a CUDA graph),
+    // then one status read.  k_refine itself skips patterns that can no longer reach tau or that
+    // the previous round left unchanged.
     std::vector<char> active(P, 0);
     for (size_t p = 0; p < P; ++p) active[p] = !trivial[p];
     build_items(active);
+    const int fixed_refine = (int)std::min<uint32_t>(std::max<uint32_t>(1, opt.refine_rounds), 32);
     if (!item_pu.empty()) {
-        TFSM_CK(cudaEventRecord(I.ev0, I.stream));
-        TFSM_CK(dev::launch_domain_init(I.g, L.descs.p, I.status.p, I.item_pu.p, I.prefix.p, (uint32_t)item_pu.size(),
-                                        prefix.back(), L.dom.p, L.found.p, L.failed.p, pdom, pfailed, total,
-                                        prev ? prev->impl->words : 0, I.stream));
-        times_.init_ms += time_and_read_status();
+        const uint32_t n_it = (uint32_t)item_pu.size();
+        const uint64_t words = prefix.back();
+        run_captured(I.stream, I.exec_init, [&]() {
+            TFSM_CK(record_in_sequence(I.ev0, I.stream));
+            TFSM_CK(dev::launch_domain_init(I.g, L.descs.p, I.status.p, I.item_pu.p, I.prefix.p, n_it, words, L.dom.p,
+                                            L.found.p, L.failed.p, pdom, pfailed, total,
+                                            prev ? prev->impl->words : 0, I.stream));
+            TFSM_CK(record_in_sequence(I.ev_mid, I.stream));
+            for (int r = 0; r < fixed_refine; ++r)
+                TFSM_CK(dev::launch_refine(I.g, L.descs.p, I.status.p, I.item_pu.p, I.prefix.p, n_it, words, L.dom.p,
+                                           total, r, tau, opt.exact, I.stream));
+            TFSM_CK(record_in_sequence(I.ev1, I.stream));
+        });
+        read_status();
+        float ms = 0;
+        TFSM_CK(cudaEventElapsedTime(&ms, I.ev0, I.ev_mid));
+        times_.init_ms += ms;
+        TFSM_CK(cudaEventElapsedTime(&ms, I.ev_mid, I.ev1));
+        times_.refine_ms += ms;
         times_.init_launches++;
-        times_.init_words += prefix.back();
+        times_.init_words += words;
+        times_.refine_launches += (uint64_t)fixed_refine;
+        times_.refine_words += words * (uint64_t)fixed_refine;
     } else {
         read_status();
     }
 
-    // ---- arc-consistency rounds ----
+    // ---- express patterns (distinct labels, acyclic) continue to the arc-consistency fixpoint,
+    // whose domains are their MNI domains; one not settled after 32 rounds is searched instead.
     auto viable = [&](size_t p) {
         const PatDesc &D = L.hdescs[p];
         for (int u = 0; u < D.n; ++u) {
@@ -456,27 +535,23 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         }
         return true;
     };
-    for (uint32_t round = 0;; ++round) {
-        for (size_t p = 0; p < P; ++p) {
-            bool a = !trivial[p] && viable(p);
-            if (round > 0) a = a && I.hstatus[p].changed != 0;
-            if (!express[p] && round >= opt.refine_rounds) a = false;
-            if (round >= 64) a = false;
-            active[p] = a;
-        }
+    int last_round = fixed_refine - 1;
+    for (int round = fixed_refine; round < 32; ++round) {
+        for (size_t p = 0; p < P; ++p)
+            active[p] = !trivial[p] && express[p] && viable(p) && ((I.hstatus[p].changed >> (round - 1)) & 1u);
         if (std::find(active.begin(), active.end(), 1) == active.end()) break;
-        for (size_t p = 0; p < P; ++p) I.hstatus[p].changed = 0;
-        TFSM_CK(cudaMemcpyAsync(I.status.p, I.hstatus.data(), P * sizeof(PatStatus), cudaMemcpyHostToDevice,
-                                I.stream));
-        times_.h2d_bytes += P * sizeof(PatStatus);
         build_items(active);
         TFSM_CK(cudaEventRecord(I.ev0, I.stream));
         TFSM_CK(dev::launch_refine(I.g, L.descs.p, I.status.p, I.item_pu.p, I.prefix.p, (uint32_t)item_pu.size(),
-                                   prefix.back(), L.dom.p, total, I.stream));
+                                   prefix.back(), L.dom.p, total, round, tau, opt.exact, I.stream));
         times_.refine_ms += time_and_read_status();
         times_.refine_launches++;
         times_.refine_words += prefix.back();
+        last_round = round;
     }
+    if (last_round == 31)
+        for (size_t p = 0; p < P; ++p)
+            if (express[p] && ((I.hstatus[p].changed >> 31) & 1u)) express[p] = 0;
 
     // ---- decisions from domain sizes; plans for the rest ----
     std::vector<char> need_search(P, 0);
@@ -629,7 +704,6 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     TFSM_CK(cudaMemcpyAsync(I.items.p, items.data(), items.size() * sizeof(dev::SearchItem), cudaMemcpyHostToDevice,
                             I.stream));
     times_.h2d_bytes += items.size() * sizeof(dev::SearchItem);
-    TFSM_CK(cudaMemsetAsync(I.counters.p, 0, dev::kNumCounters * sizeof(uint32_t), I.stream));
     dev::SearchParams prm;
     prm.tau = tau;
     prm.exact = opt.exact ? 1 : 0;
@@ -654,19 +728,27 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     uint32_t hcnt[dev::kNumCounters];
     constexpr int kMaxPasses = 16;
     for (int pass = 0; pass < kMaxPasses; ++pass) {
-        if (pass > 0) TFSM_CK(cudaMemsetAsync(I.counters.p, 0, dev::kNumCounters * sizeof(uint32_t), I.stream));
         prm.defer = pass + 1 < kMaxPasses ? 1u : 0u;
-        TFSM_CK(dev::launch_search(I.g, L.descs.p, I.status.p, I.items.p, prm, I.counters.p, L.dom.p, L.found.p,
-                                   L.failed.p, I.splits.p, I.groups.p, I.stream));
-        launches += items.empty() ? 0 : 1;
-        if (prm.step_budget && !items.empty()) {
-            const int fixed = (int)std::min<uint32_t>(std::max<uint32_t>(1, opt.split_rounds), dev::kMaxRounds);
-            int r = 0;
-            for (; r < fixed; ++r) {
+        const bool split = prm.step_budget && !items.empty();
+        const int fixed = split ? (int)std::min<uint32_t>(std::max<uint32_t>(1, opt.split_rounds), dev::kMaxRounds) : 0;
+        // the search pass and the first split rounds: one launch sequence
+        if (items.empty()) {  // every candidate decided already: nothing to launch
+            TFSM_CK(cudaEventRecord(I.ev1, I.stream));
+            read_status();
+            std::memset(hcnt, 0, sizeof(hcnt));
+            break;
+        }
+        run_captured(I.stream, I.exec_search, [&]() {
+            TFSM_CK(cudaMemsetAsync(I.counters.p, 0, dev::kNumCounters * sizeof(uint32_t), I.stream));
+            TFSM_CK(dev::launch_search(I.g, L.descs.p, I.status.p, I.items.p, prm, I.counters.p, L.dom.p, L.found.p,
+                                       L.failed.p, I.splits.p, I.groups.p, I.stream));
+            for (int r = 0; r < fixed; ++r)
                 TFSM_CK(dev::launch_split_round(I.g, L.descs.p, I.status.p, prm, I.counters.p, r, prm.round_budget,
                                                 L.dom.p, L.found.p, L.failed.p, I.splits.p, I.groups.p, I.stream));
-                ++launches;
-            }
+        });
+        launches += (items.empty() ? 0 : 1) + (uint64_t)fixed;
+        if (split) {
+            int r = fixed;
             for (; r < dev::kMaxRounds; ++r) {
                 uint32_t pending = 0;
                 TFSM_CK(cudaMemcpyAsync(&pending, I.counters.p + 2 + r, sizeof(pending), cudaMemcpyDeviceToHost,

@@ -253,26 +253,30 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     PatStatus st;
     NA_CK(cudaMemcpyAsync(&st, d_status, sizeof(st), cudaMemcpyDeviceToHost, s));
     NA_CK(cudaStreamSynchronize(s));
-    const uint32_t rounds_cap = D.express ? 64u : 2u;
-    for (uint32_t round = 0; round < rounds_cap; ++round) {
+    // arc consistency: two rounds, express patterns to the fixpoint (32 rounds at most; one not
+    // settled by then is searched instead)
+    const int rounds_cap = D.express ? 32 : 2;
+    bool settled = true;
+    for (int round = 0; round < rounds_cap; ++round) {
         bool viable = true;
         for (int u = 0; u < n; ++u) viable = viable && (exact ? st.dom_size[u] > 0 : st.dom_size[u] >= tau);
-        if (!viable || (round > 0 && !st.changed)) break;
-        st.changed = 0;
-        NA_CK(cudaMemcpyAsync(d_status, &st, sizeof(st), cudaMemcpyHostToDevice, s));
-        NA_CK(dev::launch_refine(g, d_desc, d_status, d_item_pu, d_prefix, (uint32_t)n, words, d_dom, words, s));
+        if (!viable || (round > 0 && !((st.changed >> (round - 1)) & 1u))) break;
+        NA_CK(dev::launch_refine(g, d_desc, d_status, d_item_pu, d_prefix, (uint32_t)n, words, d_dom, words, round, tau,
+                                 exact, s));
         NA_CK(cudaMemcpyAsync(&st, d_status, sizeof(st), cudaMemcpyDeviceToHost, s));
         NA_CK(cudaStreamSynchronize(s));
+        settled = !((st.changed >> round) & 1u);
     }
+    const bool express = D.express && settled;
     uint32_t mn = UINT32_MAX;
     for (int u = 0; u < n; ++u) mn = mn < st.dom_size[u] ? mn : st.dom_size[u];
     out->status = TFSM_OK;
-    if (D.express || (exact ? mn == 0 : mn < tau)) {
+    if (express || (exact ? mn == 0 : mn < tau)) {
         out->decided_by_filter = 1;
-        if (D.express && mn > 0)
+        if (express && mn > 0)
             for (int u = 0; u < n; ++u) out->mni[u] = st.dom_size[u];
-        out->support = D.express && mn > 0 ? mn : 0;
-        out->frequent = D.express && mn >= tau && mn > 0;
+        out->support = express && mn > 0 ? mn : 0;
+        out->frequent = express && mn >= tau && mn > 0;
         return TFSM_OK;
     }
     // ---- search ----

@@ -347,6 +347,9 @@ inline cudaError_t cudaEventElapsedTime(float *ms, cudaEvent_t a, cudaEvent_t b)
     *ms = std::chrono::duration<float, std::milli>(b->t - a->t).count();
     return cudaSuccess;
 }
+// CUDA graphs: the emulated engine launches directly, only the handle type and its release exist
+typedef struct EmuGraphExec *cudaGraphExec_t;
+inline cudaError_t cudaGraphExecDestroy(cudaGraphExec_t) { return cudaSuccess; }
 inline cudaError_t cudaEventDestroy(cudaEvent_t e) {
     delete e;
     return cudaSuccess;
