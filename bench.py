@@ -273,6 +273,30 @@ def mlp_arm(args, w, g, tfsm, one_step, batched_results: Path) -> dict:
             "train_s": train_s, "training_graphs": "workload shape, seeds +10..+12, plain miner, random orders"}
 
 
+def tuned_arm(args, w, g, tfsm, one_step, batched_results: Path) -> dict:
+    """Batched path with the knobs the autotuner picks per level for this workload."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("autotune", PKG / "autotune.py")
+    at = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(at)
+    t0 = time.perf_counter()
+    best = at.tune(g, w["max_nodes"], repeats=2)
+    tune_s = time.perf_counter() - t0
+    try:
+        outt = Path(tempfile.mktemp(suffix=".t.txt"))
+        g.mine(max_nodes=w["max_nodes"], results_path=outt)
+        identical = set(tfsm.read_results(outt)) == set(tfsm.read_results(batched_results))
+        for _ in range(args.warmup):
+            one_step(0)
+        runs = [one_step(0) for _ in range(args.steps)]
+    finally:
+        g.set_level_options(0, None)
+    ms = sum(r[0] for r in runs) / len(runs)
+    return {"value": runs[0][2]["evaluations"] * 1e3 / ms, "ms_per_step": ms, "identical_output": identical,
+            "tune_s": tune_s, "levels": {str(k): v for k, v in best.items()}}
+
+
 def gpu_arm(args, w, world, rank):
     import torch
 
@@ -327,6 +351,7 @@ def gpu_arm(args, w, world, rank):
     # batched + learned matching orders: a cost model trained on records that the plain miner logs
     # (random connected orders) on three training graphs of the workload's shape (other seeds)
     mlp = mlp_arm(args, w, g, tfsm, one_step, outb)
+    tuned = tuned_arm(args, w, g, tfsm, one_step, outb)
 
     # roofline of the dominant kernel (the search): algorithmic bytes / device time
     s_ms = sum(st["search_ms"] for st in stats)
@@ -377,6 +402,7 @@ def gpu_arm(args, w, world, rank):
                       "engine_calls": stats[0]["evaluations"]},
             "batched_over_plain": plain_ms / step_ms, "identical_output": identical,
             "batched_mlp": mlp,
+            "batched_autotuned": tuned,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "kernel": "k_search (+k_split)",
                          "peak_kind": peak_kind,

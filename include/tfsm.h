@@ -19,6 +19,8 @@
 extern "C" {
 #endif
 
+#define TFSM_MAX_LEVELS 32 /* growth levels reported and tunable separately */
+
 #define TFSM_OK 0
 #define TFSM_ERR_ARG 1        /* invalid argument (null pointer, bad size, malformed pattern) */
 #define TFSM_ERR_IO 2         /* graph file cannot be opened */
@@ -83,6 +85,8 @@ typedef struct {
     uint64_t searches, steps, by_filter, engine_calls;
     int32_t levels;
     int32_t complete;      /* 0 when the time limit stopped the run early */
+    double level_ms[TFSM_MAX_LEVELS]; /* host wall time of the engine calls of each level (index =
+                                         pattern edges; 0 unused) */
 } tfsm_mine_stats;
 
 /* Load a .lg graph and prune it for threshold `tau` (label frequency, edge-label frequency and
@@ -141,6 +145,11 @@ typedef struct {
 
 int tfsm_get_options(const tfsm_graph *g, tfsm_options *opt);
 int tfsm_set_options(tfsm_graph *g, const tfsm_options *opt);
+
+/* Options for the engine calls of one growth level only (patterns with `level` edges,
+ * 1 <= level < TFSM_MAX_LEVELS), e.g. from the autotuner; opt == NULL clears that level, level 0
+ * clears every level.  Levels without their own options use tfsm_set_options'. */
+int tfsm_set_level_options(tfsm_graph *g, int32_t level, const tfsm_options *opt);
 
 /* Allocation-free variant of tfsm_evaluate_support (no counterpart in the reference).
  * For callers that must not allocate device memory during the call — for example code under a

@@ -23,6 +23,7 @@ struct tfsm_graph {
     int tau = 0;
     double load_ms = 0;
     bool recording = false;
+    std::vector<std::pair<bool, tfsm_options>> level_opt;  // tfsm_set_level_options, by level
     mutable std::vector<float> records;  // tfsm_record_orders: 33 floats per record
     std::mutex mu;
 };
@@ -108,6 +109,26 @@ void fill_result(const tfsm::EvalResult &r, int n, tfsm_result *out) {
     for (int i = 0; i < n && i < TFSM_MAX_PATTERN_VERTICES; ++i) out->mni[i] = r.mni[(size_t)i];
     out->searches = r.searches;
     out->steps = r.steps;
+}
+
+const char *const kKnobRules =
+    "split_slice must be >= 32; chunk_words, refine_rounds, max_batch and round_budget >= 1; split_rounds in 1..64; "
+    "time_limit_s >= 0";
+
+bool knobs_valid(const tfsm_options &o) {
+    return o.split_slice >= 32 && o.chunk_words >= 1 && o.refine_rounds >= 1 && o.max_batch >= 1 &&
+           o.split_rounds >= 1 && o.split_rounds <= 64 && o.round_budget >= 1 && o.time_limit_s >= 0;
+}
+
+// The speed-only knobs of `o` (not the time limit, which belongs to the whole run).
+void apply_knobs(const tfsm_options &o, tfsm::EngineOptions &e) {
+    e.step_budget = o.step_budget;
+    e.split_slice = o.split_slice;
+    e.chunk_words = o.chunk_words;
+    e.refine_rounds = o.refine_rounds;
+    e.max_batch = o.max_batch;
+    e.split_rounds = o.split_rounds;
+    e.round_budget = o.round_budget;
 }
 
 tfsm::EngineOptions engine_options(const tfsm_graph *g, uint32_t flags) {
@@ -234,6 +255,13 @@ int tfsm_mine(tfsm_graph *g, int32_t tau, int32_t max_nodes, uint32_t flags, con
         opt.max_nodes = max_nodes;
         opt.batched = (flags & TFSM_FLAG_PLAIN) == 0;
         opt.engine = engine_options(g, flags);
+        for (size_t l = 0; l < g->level_opt.size(); ++l) {
+            if (!g->level_opt[l].first) continue;
+            if (opt.level_engine.size() <= l) opt.level_engine.resize(l + 1);
+            tfsm::EngineOptions e = opt.engine;
+            apply_knobs(g->level_opt[l].second, e);
+            opt.level_engine[l] = {true, e};
+        }
         std::vector<tfsm::MinedPattern> pats;
         tfsm::MineStats st;
         g->eng->reset_times();
@@ -265,6 +293,7 @@ int tfsm_mine(tfsm_graph *g, int32_t tau, int32_t max_nodes, uint32_t flags, con
             stats->engine_calls = st.engine_calls;
             stats->levels = st.levels;
             stats->complete = st.complete ? 1 : 0;
+            for (size_t l = 0; l < st.level_ms.size() && l < TFSM_MAX_LEVELS; ++l) stats->level_ms[l] = st.level_ms[l];
         }
         return TFSM_OK;
     });
@@ -289,20 +318,26 @@ int tfsm_get_options(const tfsm_graph *g, tfsm_options *o) {
 int tfsm_set_options(tfsm_graph *g, const tfsm_options *o) {
     return guarded([&]() -> int {
         if (!g || !o) return fail(TFSM_ERR_ARG, "null argument");
-        if (o->split_slice < 32 || o->chunk_words < 1 || o->refine_rounds < 1 || o->max_batch < 1 ||
-            o->split_rounds < 1 || o->split_rounds > 64 || o->round_budget < 1 || !(o->time_limit_s >= 0))
-            return fail(TFSM_ERR_ARG,
-                        "split_slice must be >= 32; chunk_words, refine_rounds, max_batch and round_budget >= 1; "
-                        "split_rounds in 1..64; time_limit_s >= 0");
+        if (!knobs_valid(*o)) return fail(TFSM_ERR_ARG, kKnobRules);
         std::lock_guard<std::mutex> lk(g->mu);
-        g->opt.step_budget = o->step_budget;
-        g->opt.split_slice = o->split_slice;
-        g->opt.chunk_words = o->chunk_words;
-        g->opt.refine_rounds = o->refine_rounds;
-        g->opt.max_batch = o->max_batch;
+        apply_knobs(*o, g->opt);
         g->opt.time_limit_s = o->time_limit_s;
-        g->opt.split_rounds = o->split_rounds;
-        g->opt.round_budget = o->round_budget;
+        return TFSM_OK;
+    });
+}
+
+int tfsm_set_level_options(tfsm_graph *g, int32_t level, const tfsm_options *o) {
+    return guarded([&]() -> int {
+        if (!g) return fail(TFSM_ERR_ARG, "null argument");
+        if (level < 0 || level >= TFSM_MAX_LEVELS) return fail(TFSM_ERR_ARG, "level must be in 0..TFSM_MAX_LEVELS-1");
+        if (o && !knobs_valid(*o)) return fail(TFSM_ERR_ARG, kKnobRules);
+        std::lock_guard<std::mutex> lk(g->mu);
+        if (level == 0) {
+            g->level_opt.clear();
+            return TFSM_OK;
+        }
+        if (g->level_opt.size() <= (size_t)level) g->level_opt.resize((size_t)level + 1);
+        g->level_opt[(size_t)level] = o ? std::make_pair(true, *o) : std::make_pair(false, tfsm_options{});
         return TFSM_OK;
     });
 }

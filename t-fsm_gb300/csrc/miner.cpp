@@ -136,8 +136,11 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
     auto evaluate_level = [&](std::vector<Node> &nodes, const std::vector<int> &parent_of,
                               const std::vector<Node> *parents) {
         if (nodes.empty()) return;
+        const int lvl_no = st.levels + 1;
+        const EngineOptions &eo = opt.engine_for(lvl_no);
+        const double wall_before = eng.times().engine_ms;
         if (opt.batched) {
-            const size_t step = std::max<size_t>(1, opt.engine.max_batch);
+            const size_t step = std::max<size_t>(1, eo.max_batch);
             auto parent_level = [&](size_t i) -> const Level * {
                 return (parents && parent_of[i] >= 0) ? (*parents)[(size_t)parent_of[i]].lvl : nullptr;
             };
@@ -160,7 +163,7 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                 std::vector<EvalResult> res;
                 const KernelTimes before = eng.times();
                 const double search_before = before.search_ms;
-                eng.evaluate(pats, par, prev, tau, opt.engine, *cur_levels.back(), res);
+                eng.evaluate(pats, par, prev, tau, eo, *cur_levels.back(), res);
                 st.engine_calls++;
                 st.evaluations += b1 - b0;
                 if (verbose) {
@@ -215,7 +218,7 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                 }
                 cur_levels.emplace_back(new Level);
                 std::vector<EvalResult> res;
-                eng.evaluate(pats, par, prev, tau, opt.engine, *cur_levels.back(), res);
+                eng.evaluate(pats, par, prev, tau, eo, *cur_levels.back(), res);
                 st.engine_calls++;
                 nodes[i].res = std::move(res[0]);
                 nodes[i].lvl = cur_levels.back().get();
@@ -227,6 +230,8 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
             st.steps += nd.res.steps;
             st.by_filter += nd.res.by_filter ? 1 : 0;
         }
+        if ((size_t)lvl_no >= st.level_ms.size()) st.level_ms.resize((size_t)lvl_no + 1, 0.0);
+        st.level_ms[(size_t)lvl_no] += eng.times().engine_ms - wall_before;
     };
 
     // level 1: the frequent 1-edge patterns (frequent by construction of the pair table,

@@ -23,6 +23,13 @@ struct MineOptions {
     bool batched = true;
     int host_threads = 0;  // threads for extension + canonical checks (0: hardware concurrency)
     EngineOptions engine;
+    // per growth level (index = pattern edges): options for that level's engine calls, when set
+    std::vector<std::pair<bool, EngineOptions>> level_engine;
+    const EngineOptions &engine_for(int level) const {
+        return level >= 0 && (size_t)level < level_engine.size() && level_engine[(size_t)level].first
+                   ? level_engine[(size_t)level].second
+                   : engine;
+    }
 };
 
 struct MinedPattern {
@@ -41,6 +48,7 @@ struct MineStats {
     uint64_t engine_calls = 0;
     int levels = 0;
     bool complete = true;           // false when the time limit stopped the run
+    std::vector<double> level_ms;   // engine wall time per level (index = pattern edges)
 };
 
 // Mines all frequent patterns; `out` lists them level by level in generation order.

@@ -24,6 +24,7 @@ TFSM_ERR_NO_DEVICE = 9
 TFSM_ERR_CUDA = 10
 TFSM_ERR_INTERNAL = 11
 MAX_PATTERN_VERTICES = 16
+MAX_LEVELS = 32
 
 FLAG_EXACT = 1
 FLAG_PLAIN = 2
@@ -39,6 +40,7 @@ EXPORTED = (
     "tfsm_mine",
     "tfsm_get_options",
     "tfsm_set_options",
+    "tfsm_set_level_options",
     "tfsm_evaluate_support_noalloc",
     "tfsm_cost_model_create",
     "tfsm_cost_model_free",
@@ -99,7 +101,7 @@ class MineStatsC(C.Structure):
                 ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
                 ("evaluations", C.c_uint64), ("frequent", C.c_uint64), ("searches", C.c_uint64),
                 ("steps", C.c_uint64), ("by_filter", C.c_uint64), ("engine_calls", C.c_uint64),
-                ("levels", C.c_int32), ("complete", C.c_int32)]
+                ("levels", C.c_int32), ("complete", C.c_int32), ("level_ms", C.c_double * MAX_LEVELS)]
 
 
 _lib = None
@@ -126,6 +128,7 @@ def lib() -> C.CDLL:
         L.tfsm_mine.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_uint32, C.c_char_p, C.POINTER(MineStatsC)]
         L.tfsm_get_options.argtypes = [C.c_void_p, C.POINTER(OptionsC)]
         L.tfsm_set_options.argtypes = [C.c_void_p, C.POINTER(OptionsC)]
+        L.tfsm_set_level_options.argtypes = [C.c_void_p, C.c_int32, C.POINTER(OptionsC)]
         L.tfsm_evaluate_support_noalloc.argtypes = [C.c_void_p, C.POINTER(PatternC), C.c_int32, C.c_uint32,
                                                     C.POINTER(ResultC)]
         fp = C.POINTER(C.c_float)
@@ -255,6 +258,17 @@ class Graph:
         o = OptionsC(**cur)
         _check(lib().tfsm_set_options(self._h, C.byref(o)))
 
+    def set_level_options(self, level: int, options: dict | None) -> None:
+        """Knobs for the engine calls of one growth level (patterns with `level` edges); None clears
+        the level, level 0 clears all.  Missing keys take the handle's current options."""
+        if options is None:
+            _check(lib().tfsm_set_level_options(self._h, level, None))
+            return
+        cur = self.options()
+        cur.update(options)
+        o = OptionsC(**cur)
+        _check(lib().tfsm_set_level_options(self._h, level, C.byref(o)))
+
     def set_order_policy(self, policy: int, seed: int = 0, model: "CostModel | None" = None) -> None:
         self._model = model  # kept alive while the handle may use it
         _check(lib().tfsm_set_order_policy(self._h, policy, seed, model._h if model else None))
@@ -280,7 +294,7 @@ class Graph:
         p = str(results_path).encode() if results_path else None
         _check(lib().tfsm_mine(self._h, int(self.tau if tau is None else tau), int(max_nodes), int(flags), p,
                                C.byref(st)))
-        return {f: getattr(st, f) for f, _ in MineStatsC._fields_}
+        return {f: (list(getattr(st, f)) if f == "level_ms" else getattr(st, f)) for f, _ in MineStatsC._fields_}
 
 
 def _fptr(a):
