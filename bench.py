@@ -301,6 +301,10 @@ def gpu_arm(args, w, world, rank):
     import torch
 
     tfsm = binding()
+    # the plain path is the reference's miner loop around the drop-in evaluation: one engine call
+    # per candidate, fixed (GQL) matching order, no sub-pattern pruning (the reference searches
+    # every candidate)
+    PLAIN = tfsm.FLAG_PLAIN | tfsm.FLAG_NO_SUBPATTERN_PRUNING
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     graph = make_graph(w)
@@ -322,7 +326,7 @@ def gpu_arm(args, w, world, rank):
     # identical output of the batched and plain paths
     outb, outp = Path(tempfile.mktemp(suffix=".b.txt")), Path(tempfile.mktemp(suffix=".p.txt"))
     g.mine(max_nodes=w["max_nodes"], results_path=outb)
-    g.mine(max_nodes=w["max_nodes"], flags=tfsm.FLAG_PLAIN, results_path=outp)
+    g.mine(max_nodes=w["max_nodes"], flags=PLAIN, results_path=outp)
     identical = set(tfsm.read_results(outb)) == set(tfsm.read_results(outp))
 
     for _ in range(args.warmup):
@@ -344,8 +348,9 @@ def gpu_arm(args, w, world, rank):
 
     # plain path, same workload
     for _ in range(max(1, args.warmup // 2)):
-        one_step(tfsm.FLAG_PLAIN)
-    pms = [one_step(tfsm.FLAG_PLAIN)[0] for _ in range(max(1, args.steps // 2))]
+        one_step(PLAIN)
+    pruns = [one_step(PLAIN) for _ in range(max(1, args.steps // 2))]
+    pms = [r[0] for r in pruns]
     plain_ms = max_over_ranks(world, sum(pms) / len(pms))
 
     # batched + learned matching orders: a cost model trained on records that the plain miner logs
@@ -398,8 +403,11 @@ def gpu_arm(args, w, world, rank):
                        "graph_vertices": info["n_vertices"], "graph_edges": info["n_edges"]},
             "wall_clock_mine_s": step_ms / 1e3,
             "frequent_patterns": stats[0]["frequent"], "support_evaluations": evals,
+            "decided_by_subpattern": stats[0]["pruned"], "decided_by_filters": stats[0]["by_filter"],
             "plain": {"value": evals * 1e3 / plain_ms, "ms_per_step": plain_ms,
-                      "engine_calls": stats[0]["evaluations"]},
+                      "engine_calls": pruns[0][2]["engine_calls"],
+                      "path": "reference miner loop + drop-in evaluation: one engine call per candidate, GQL order, "
+                              "no sub-pattern pruning"},
             "batched_over_plain": plain_ms / step_ms, "identical_output": identical,
             "batched_mlp": mlp,
             "batched_autotuned": tuned,

@@ -37,6 +37,8 @@ extern "C" {
 #define TFSM_FLAG_EXACT 1u    /* exact MNI per vertex: no early exit at tau */
 #define TFSM_FLAG_PLAIN 2u    /* tfsm_mine: one engine call per candidate pattern (unbatched) */
 #define TFSM_FLAG_NO_SPLIT 4u /* disable splitting of long searches (hub tasks) */
+#define TFSM_FLAG_NO_SUBPATTERN_PRUNING 8u /* tfsm_mine: search every candidate, even one with an
+                                              infrequent one-edge-smaller sub-pattern */
 
 typedef struct tfsm_graph tfsm_graph;
 
@@ -87,6 +89,8 @@ typedef struct {
     int32_t complete;      /* 0 when the time limit stopped the run early */
     double level_ms[TFSM_MAX_LEVELS]; /* host wall time of the engine calls of each level (index =
                                          pattern edges; 0 unused) */
+    uint64_t pruned;       /* candidates decided infrequent by an infrequent sub-pattern (counted in
+                              evaluations and by_filter; no engine call) */
 } tfsm_mine_stats;
 
 /* Load a .lg graph and prune it for threshold `tau` (label frequency, edge-label frequency and

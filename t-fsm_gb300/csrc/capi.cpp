@@ -254,6 +254,7 @@ int tfsm_mine(tfsm_graph *g, int32_t tau, int32_t max_nodes, uint32_t flags, con
         opt.tau = tau;
         opt.max_nodes = max_nodes;
         opt.batched = (flags & TFSM_FLAG_PLAIN) == 0;
+        opt.subpattern_pruning = (flags & TFSM_FLAG_NO_SUBPATTERN_PRUNING) == 0;
         opt.engine = engine_options(g, flags);
         for (size_t l = 0; l < g->level_opt.size(); ++l) {
             if (!g->level_opt[l].first) continue;
@@ -294,6 +295,7 @@ int tfsm_mine(tfsm_graph *g, int32_t tau, int32_t max_nodes, uint32_t flags, con
             stats->levels = st.levels;
             stats->complete = st.complete ? 1 : 0;
             for (size_t l = 0; l < st.level_ms.size() && l < TFSM_MAX_LEVELS; ++l) stats->level_ms[l] = st.level_ms[l];
+            stats->pruned = st.pruned;
         }
         return TFSM_OK;
     });

@@ -1,0 +1,147 @@
+// Sub-pattern (Apriori) pruning for the miner.
+//
+// MNI support is anti-monotone: an embedding of a pattern P contains an embedding of every
+// connected sub-pattern S of P, with the vertices of S mapped to the same data vertices, so
+// MNI(P) <= MNI(S).  Rightmost extension with the canonical check generates every frequent pattern
+// exactly once, level by level, so when one of P's connected sub-patterns with one edge less is not
+// among the previous level's frequent patterns, P is infrequent and needs no search (the miner
+// applies this only with a single frequent edge label: with several, the reference's canonical
+// check does not generate every frequent pattern, see miner.cpp).  The
+// reference reaches the same decision through its search and its push-down cache of per-vertex
+// non-candidates (parallel/decompose.h, parallel/comper.h:1582-1612); the mined set is unchanged.
+//
+// Sub-patterns are matched by an isomorphism-invariant key: vertices are ordered by an invariant
+// (label, degree, sorted (edge label, neighbour label) pairs), every ordering that keeps that
+// order is tried, and the smallest edge list wins.
+#pragma once
+
+#include <algorithm>
+#include <array>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "pattern.hpp"
+
+namespace tfsm {
+
+struct SmallGraph {
+    std::vector<int> label;                 // by vertex
+    std::vector<std::array<int, 3>> edges;  // (a, b, edge label)
+};
+
+// Isomorphism-invariant key (bytes of int32 values).
+inline std::string canonical_key(const SmallGraph &g) {
+    const int n = (int)g.label.size();
+    std::vector<std::vector<int>> inv((size_t)n);
+    for (int v = 0; v < n; ++v) inv[(size_t)v] = {g.label[(size_t)v], 0};
+    for (auto &e : g.edges) {
+        inv[(size_t)e[0]][1]++;
+        inv[(size_t)e[1]][1]++;
+    }
+    std::vector<std::vector<std::pair<int, int>>> nb((size_t)n);
+    for (auto &e : g.edges) {
+        nb[(size_t)e[0]].push_back({e[2], g.label[(size_t)e[1]]});
+        nb[(size_t)e[1]].push_back({e[2], g.label[(size_t)e[0]]});
+    }
+    for (int v = 0; v < n; ++v) {
+        std::sort(nb[(size_t)v].begin(), nb[(size_t)v].end());
+        for (auto &p : nb[(size_t)v]) {
+            inv[(size_t)v].push_back(p.first);
+            inv[(size_t)v].push_back(p.second);
+        }
+    }
+    std::vector<int> order((size_t)n);
+    for (int v = 0; v < n; ++v) order[(size_t)v] = v;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return inv[(size_t)a] < inv[(size_t)b]; });
+    // classes of equal invariants: [begin, end) ranges of `order`
+    std::vector<std::pair<int, int>> cls;
+    for (int i = 0; i < n;) {
+        int j = i + 1;
+        while (j < n && inv[(size_t)order[(size_t)j]] == inv[(size_t)order[(size_t)i]]) ++j;
+        cls.push_back({i, j});
+        i = j;
+    }
+    std::vector<int> pos((size_t)n);
+    std::vector<std::array<int, 3>> cur, best;
+    bool have = false;
+    for (;;) {
+        for (int i = 0; i < n; ++i) pos[(size_t)order[(size_t)i]] = i;
+        cur.clear();
+        for (auto &e : g.edges) {
+            const int a = pos[(size_t)e[0]], b = pos[(size_t)e[1]];
+            cur.push_back({std::min(a, b), std::max(a, b), e[2]});
+        }
+        std::sort(cur.begin(), cur.end());
+        if (!have || cur < best) {
+            best = cur;
+            have = true;
+        }
+        // next ordering: odometer over the classes' permutations
+        size_t k = 0;
+        for (; k < cls.size(); ++k) {
+            auto b = order.begin() + cls[k].first, e = order.begin() + cls[k].second;
+            if (std::next_permutation(b, e)) break;  // wrapped classes are back in ascending order
+        }
+        if (k == cls.size()) break;
+    }
+    std::vector<int32_t> key;
+    key.push_back(n);
+    for (int i = 0; i < n; ++i)
+        for (int x : inv[(size_t)order[(size_t)i]]) key.push_back(x);  // classes are in sorted order again
+    key.push_back(-1);
+    for (auto &e : best) key.insert(key.end(), {e[0], e[1], e[2]});
+    return std::string(reinterpret_cast<const char *>(key.data()), key.size() * sizeof(int32_t));
+}
+
+inline SmallGraph small_graph(const Pattern &p) {
+    SmallGraph g;
+    for (auto &v : p.vertices) g.label.push_back(v.label);
+    for (auto &c : p.codes) g.edges.push_back({c.from, c.to, c.edge_label});
+    return g;
+}
+
+// Keys of P's connected sub-patterns with one edge less (an edge to a degree-1 vertex goes with
+// that vertex; an edge whose removal disconnects the rest gives no connected sub-pattern).
+inline void one_edge_smaller_keys(const Pattern &p, std::vector<std::string> &keys) {
+    keys.clear();
+    const SmallGraph g = small_graph(p);
+    const int n = (int)g.label.size(), m = (int)g.edges.size();
+    if (m < 2) return;
+    std::vector<int> deg((size_t)n, 0);
+    for (auto &e : g.edges) {
+        deg[(size_t)e[0]]++;
+        deg[(size_t)e[1]]++;
+    }
+    for (int i = 0; i < m; ++i) {
+        const int a = g.edges[(size_t)i][0], b = g.edges[(size_t)i][1];
+        int drop = -1;
+        if (deg[(size_t)a] == 1) drop = a;
+        else if (deg[(size_t)b] == 1) drop = b;
+        SmallGraph s;
+        std::vector<int> remap((size_t)n, -1);
+        for (int v = 0; v < n; ++v)
+            if (v != drop) {
+                remap[(size_t)v] = (int)s.label.size();
+                s.label.push_back(g.label[(size_t)v]);
+            }
+        for (int j = 0; j < m; ++j)
+            if (j != i)
+                s.edges.push_back({remap[(size_t)g.edges[(size_t)j][0]], remap[(size_t)g.edges[(size_t)j][1]],
+                                   g.edges[(size_t)j][2]});
+        // connected?
+        const int ns = (int)s.label.size();
+        std::vector<int> comp((size_t)ns);
+        for (int v = 0; v < ns; ++v) comp[(size_t)v] = v;
+        auto find = [&](int x) {
+            while (comp[(size_t)x] != x) x = comp[(size_t)x] = comp[(size_t)comp[(size_t)x]];
+            return x;
+        };
+        for (auto &e : s.edges) comp[(size_t)find(e[0])] = find(e[1]);
+        bool connected = true;
+        for (int v = 1; v < ns && connected; ++v) connected = find(v) == find(0);
+        if (connected) keys.push_back(canonical_key(s));
+    }
+}
+
+}  // namespace tfsm

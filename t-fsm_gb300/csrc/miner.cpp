@@ -11,6 +11,9 @@
 #include <memory>
 #include <mutex>
 #include <thread>
+#include <unordered_set>
+
+#include "host/subpattern.hpp"
 
 namespace tfsm {
 
@@ -19,6 +22,7 @@ namespace {
 struct Node {
     Pattern pat;
     EvalResult res;
+    bool pruned = false;   // a sub-pattern with one edge less is infrequent: decided without search
     Level *lvl = nullptr;  // device memory holding this pattern's final domains
     int idx = 0;           // index inside lvl
 };
@@ -119,6 +123,11 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
     }
     const uint32_t tau = (uint32_t)std::max(opt.tau, 0);
     const bool verbose = std::getenv("TFSM_VERBOSE") != nullptr;  // per-engine-call summary on stderr
+    // Sub-pattern pruning needs every frequent pattern of a level to be generated.  With more than
+    // one frequent edge label the reference's canonical check orders forward edges by a relation
+    // that is not a strict weak ordering (parallel/canonical.h:40-44), and its mined sets are not
+    // closed under sub-patterns; the pruning is then off so that the output stays the reference's.
+    const bool prune_subpatterns = opt.subpattern_pruning && g.freq_elabels.size() <= 1;
 
     // Levels own device memory; a level is released once its children are evaluated.
     std::vector<std::unique_ptr<Level>> prev_levels, cur_levels;
@@ -139,23 +148,38 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
         const int lvl_no = st.levels + 1;
         const EngineOptions &eo = opt.engine_for(lvl_no);
         const double wall_before = eng.times().engine_ms;
+        // sub-pattern pruning decided some candidates already; the engine evaluates the rest
+        std::vector<size_t> todo;
+        for (size_t i = 0; i < nodes.size(); ++i) {
+            if (!nodes[i].pruned) {
+                todo.push_back(i);
+                continue;
+            }
+            nodes[i].res = EvalResult();
+            nodes[i].res.mni.assign((size_t)nodes[i].pat.size(), 0);
+            nodes[i].res.by_filter = true;
+            st.evaluations++;
+            st.pruned++;
+        }
         if (opt.batched) {
             const size_t step = std::max<size_t>(1, eo.max_batch);
-            auto parent_level = [&](size_t i) -> const Level * {
+            auto parent_level = [&](size_t k) -> const Level * {
+                const size_t i = todo[k];
                 return (parents && parent_of[i] >= 0) ? (*parents)[(size_t)parent_of[i]].lvl : nullptr;
             };
             size_t b0 = 0;
-            while (b0 < nodes.size()) {
+            while (b0 < todo.size()) {
                 if (out_of_time()) {
-                    nodes.resize(b0);
+                    nodes.resize(todo[b0]);
                     break;
                 }
                 const Level *prev = parent_level(b0);
                 size_t b1 = b0 + 1;
-                while (b1 < nodes.size() && b1 - b0 < step && parent_level(b1) == prev) ++b1;
+                while (b1 < todo.size() && b1 - b0 < step && parent_level(b1) == prev) ++b1;
                 std::vector<const Pattern *> pats;
                 std::vector<int> par;
-                for (size_t i = b0; i < b1; ++i) {
+                for (size_t k = b0; k < b1; ++k) {
+                    const size_t i = todo[k];
                     pats.push_back(&nodes[i].pat);
                     par.push_back(prev ? (*parents)[(size_t)parent_of[i]].idx : -1);
                 }
@@ -194,15 +218,16 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                         std::fprintf(stderr, "\n");
                     }
                 }
-                for (size_t i = b0; i < b1; ++i) {
-                    nodes[i].res = std::move(res[i - b0]);
+                for (size_t k = b0; k < b1; ++k) {
+                    const size_t i = todo[k];
+                    nodes[i].res = std::move(res[k - b0]);
                     nodes[i].lvl = cur_levels.back().get();
-                    nodes[i].idx = (int)(i - b0);
+                    nodes[i].idx = (int)(k - b0);
                 }
                 b0 = b1;
             }
         } else {
-            for (size_t i = 0; i < nodes.size(); ++i) {
+            for (size_t i : todo) {
                 if (out_of_time()) {
                     nodes.resize(i);
                     break;
@@ -263,6 +288,35 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                 next.push_back(std::move(nd));
                 parent_of.push_back((int)i);
             }
+        if (prune_subpatterns && !next.empty()) {
+            // keys of this level's frequent patterns, then the one-edge-smaller sub-patterns of
+            // every child (both on the host pool)
+            std::vector<std::string> fkeys(level.size());
+            {
+                std::atomic<size_t> k(0);
+                const std::function<void()> work = [&]() {
+                    for (size_t i; (i = k.fetch_add(1)) < level.size();)
+                        if (level[i].res.frequent) fkeys[i] = canonical_key(small_graph(level[i].pat));
+                };
+                pool.run(work);
+            }
+            std::unordered_set<std::string> freq;
+            for (size_t i = 0; i < level.size(); ++i)
+                if (level[i].res.frequent) freq.insert(std::move(fkeys[i]));
+            std::atomic<size_t> k(0);
+            const std::function<void()> work = [&]() {
+                std::vector<std::string> keys;
+                for (size_t i; (i = k.fetch_add(1)) < next.size();) {
+                    one_edge_smaller_keys(next[i].pat, keys);
+                    for (auto &key : keys)
+                        if (!freq.count(key)) {
+                            next[i].pruned = true;
+                            break;
+                        }
+                }
+            };
+            pool.run(work);
+        }
         st.extend_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - te).count();
         if (next.empty()) break;
         prev_levels = std::move(cur_levels);

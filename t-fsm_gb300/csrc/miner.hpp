@@ -22,6 +22,7 @@ struct MineOptions {
     int max_nodes = -1;
     bool batched = true;
     int host_threads = 0;  // threads for extension + canonical checks (0: hardware concurrency)
+    bool subpattern_pruning = true;  // Apriori: a child with an infrequent one-edge-smaller sub-pattern is infrequent
     EngineOptions engine;
     // per growth level (index = pattern edges): options for that level's engine calls, when set
     std::vector<std::pair<bool, EngineOptions>> level_engine;
@@ -45,6 +46,7 @@ struct MineStats {
     uint64_t searches = 0;
     uint64_t steps = 0;
     uint64_t by_filter = 0;         // decided without search
+    uint64_t pruned = 0;            // of these: by an infrequent sub-pattern (no engine call)
     uint64_t engine_calls = 0;
     int levels = 0;
     bool complete = true;           // false when the time limit stopped the run

@@ -2,7 +2,7 @@
 //
 //   run -file G.lg -freq TAU [-thread T] [-maxNodes N] [-plain] [-exact] [-out PATH]
 //       [-step-budget B] [-split-slice S] [-chunk-words W] [-refine-rounds R] [-max-batch M]
-//       [-split-rounds K] [-round-budget B] [-time-limit SECONDS] [-random-orders SEED]
+//       [-split-rounds K] [-round-budget B] [-time-limit SECONDS] [-random-orders SEED] [-no-prune]
 //
 // Frequent patterns go to ./grami_results.txt (or -out PATH) in the serial build's format
 // (serial/grami.h:622-635); timing and counts are printed as the parallel build prints them.
@@ -40,6 +40,7 @@ int main(int argc, char **argv) {
     uint32_t flags = 0;
     if (flag(argc, argv, "-plain")) flags |= TFSM_FLAG_PLAIN;
     if (flag(argc, argv, "-exact")) flags |= TFSM_FLAG_EXACT;
+    if (flag(argc, argv, "-no-prune")) flags |= TFSM_FLAG_NO_SUBPATTERN_PRUNING;
 
     tfsm_graph *g = nullptr;
     int rc = tfsm_graph_load(file, tau, &g);
@@ -78,9 +79,10 @@ int main(int argc, char **argv) {
     std::printf("[INFO] # Frequent Patterns: %llu\n", (unsigned long long)st.frequent);
     std::printf("[INFO] # Support Evaluations: %llu (%.0f /s)\n", (unsigned long long)st.evaluations,
                 st.mine_ms > 0 ? st.evaluations / (st.mine_ms / 1e3) : 0.0);
-    std::printf("[INFO] # Searches: %llu, # Chunk steps: %llu, decided by filters: %llu, engine calls: %llu\n",
+    std::printf("[INFO] # Searches: %llu, # Chunk steps: %llu, decided by filters: %llu (by sub-patterns: %llu), "
+                "engine calls: %llu\n",
                 (unsigned long long)st.searches, (unsigned long long)st.steps, (unsigned long long)st.by_filter,
-                (unsigned long long)st.engine_calls);
+                (unsigned long long)st.pruned, (unsigned long long)st.engine_calls);
     if (!st.complete) std::printf("[INFO] TIME LIMIT REACHED: the run is incomplete\n");
     std::printf("[TIME] Device: init %.3f ms (%llu), refine %.3f ms (%llu), search %.3f ms (%llu), host extend %.3f ms\n",
                 st.init_ms, (unsigned long long)st.init_launches, st.refine_ms, (unsigned long long)st.refine_launches,

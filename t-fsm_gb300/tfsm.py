@@ -29,6 +29,7 @@ MAX_LEVELS = 32
 FLAG_EXACT = 1
 FLAG_PLAIN = 2
 FLAG_NO_SPLIT = 4
+FLAG_NO_SUBPATTERN_PRUNING = 8
 
 EXPORTED = (
     "tfsm_graph_load",
@@ -101,7 +102,8 @@ class MineStatsC(C.Structure):
                 ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
                 ("evaluations", C.c_uint64), ("frequent", C.c_uint64), ("searches", C.c_uint64),
                 ("steps", C.c_uint64), ("by_filter", C.c_uint64), ("engine_calls", C.c_uint64),
-                ("levels", C.c_int32), ("complete", C.c_int32), ("level_ms", C.c_double * MAX_LEVELS)]
+                ("levels", C.c_int32), ("complete", C.c_int32), ("level_ms", C.c_double * MAX_LEVELS),
+                ("pruned", C.c_uint64)]
 
 
 _lib = None

@@ -55,7 +55,7 @@ def test_mining_batched_matches_reference(tfsm, graphs, case, tmp_path):
 def test_mining_plain_matches_reference(tfsm, graphs, case, tmp_path):
     pats, st = mine_set(tfsm, graphs(case), case, tmp_path, flags=tfsm.FLAG_PLAIN)
     assert pats == golden_pattern_set(case)
-    assert st["engine_calls"] == st["evaluations"]
+    assert st["engine_calls"] == st["evaluations"] - st["pruned"]  # one engine call per searched candidate
 
 
 SPLIT_OPTS = [dict(step_budget=1, split_slice=32, round_budget=1),   # splits again in every round
@@ -223,3 +223,17 @@ def test_random_matching_orders_keep_results(tfsm, case_graph, case, seed, tmp_p
             keys = list(want)[:200]
             res = g.evaluate([tfsm.parse_key(k) for k in keys], flags=tfsm.FLAG_EXACT)
             assert [r.mni for r in res] == [want[k] for k in keys]
+
+
+@pytest.mark.parametrize("case", ["cfg1", "clique", "cfg2_t9000", "el3"])
+def test_subpattern_pruning_keeps_results(tfsm, graphs, case, tmp_path):
+    """With and without sub-pattern pruning: the reference's pattern set (pruning is active on
+    single-edge-label graphs only)."""
+    g = graphs(case)
+    a, sa = mine_set(tfsm, g, case, tmp_path)
+    b, sb = mine_set(tfsm, g, case, tmp_path, flags=tfsm.FLAG_NO_SUBPATTERN_PRUNING)
+    assert a == b == golden_pattern_set(case)
+    assert sa["evaluations"] == sb["evaluations"]
+    assert sb["pruned"] == 0
+    if case in ("cfg1", "cfg2_t9000"):
+        assert sa["pruned"] > 0

@@ -72,3 +72,12 @@ def test_fast_parser_multi_chunk_file(checker, tmp_path):
     f.write_text("\n".join(lines) + "\n")
     r = subprocess.run([str(checker), str(f), "50", "16"], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and "line 250001" in r.stdout, r.stdout + r.stderr
+
+
+def test_subpattern_key_is_an_isomorphism_invariant(tmp_path):
+    """canonical_key (sub-pattern pruning): equal for relabelled copies, one key per class."""
+    exe = tmp_path / "subpattern_check"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", str(ROOT / "t-fsm_gb300" / "csrc"),
+                    str(ROOT / "tests" / "native" / "subpattern_check.cpp"), "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
