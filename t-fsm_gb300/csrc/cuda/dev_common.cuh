@@ -85,6 +85,17 @@ struct SearchItem {
     uint32_t word_hi;
 };
 
+// Bits of a 32-candidate word that belong to part `part` of 2^log2 interleaved parts.
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline uint32_t part_mask(uint32_t part, uint32_t log2) {
+    uint32_t m = 0;
+    const uint32_t step = 1u << log2;
+    for (uint32_t b = part; b < 32; b += step) m |= 1u << b;
+    return m;
+}
+
 // Split task: an unexplored part of one (u, v) search — the candidates at positions [lo, hi) of the
 // anchor list at `depth`, below the partial embedding prefix[0..depth-1] (data vertices of the
 // pattern vertices order[0..depth-1] of u's matching order).  A search that exceeds its step budget
@@ -135,6 +146,8 @@ struct SearchParams {
                              //    split_cap - split_slack): the rounds' tasks can outnumber it
     uint32_t group_cap;      // capacity of the split-group buffer
     uint32_t round_budget;   // step budget of every split round but round kMaxRounds - 1
+    uint32_t parts_log2;     // every item is claimed 2^parts_log2 times, claim k searching the bits b of
+                             //    its words with b % 2^parts_log2 == k (small calls: more warps busy)
     uint32_t defer;          // 1: a search whose remainder finds no room is left undecided for the
                              //    next pass; 0: it finishes in place without a budget
     uint32_t n_pats;         // patterns of the batch

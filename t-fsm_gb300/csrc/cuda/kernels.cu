@@ -695,8 +695,9 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
         uint32_t it = 0;
         if (lane == 0) it = atomicAdd(&counters[0], 1u);
         it = __shfl_sync(0xffffffffu, it, 0);
-        if (it >= prm.n_items) break;
-        const SearchItem item = items[it];
+        if (it >= (prm.n_items << prm.parts_log2)) break;
+        const SearchItem item = items[it >> prm.parts_log2];
+        const uint32_t pmask = part_mask(it & ((1u << prm.parts_log2) - 1), prm.parts_log2);
         const uint32_t p = item.pat;
         const int u = item.u;
         if (!TFSM_IN(12, p, prm.n_pats) || !TFSM_IN(20, u, kMaxN)) continue;
@@ -708,7 +709,8 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
             if (pattern_stops(ps, u, exact, lane)) break;
             const uint32_t o = P.off[u] + word;
             if (!TFSM_IN(13, o, prm.words)) break;
-            uint32_t cand = warp_word(dom + o, lane) & ~warp_word(found + o, lane) & ~warp_word(failed + o, lane);
+            uint32_t cand = warp_word(dom + o, lane) & ~warp_word(found + o, lane) & ~warp_word(failed + o, lane) &
+                            pmask;
             while (cand) {
                 const int b = __ffs(cand) - 1;
                 cand &= cand - 1;
@@ -967,7 +969,7 @@ cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, c
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search, kSearchWarps * 32, 0);
     if (per_sm <= 0) per_sm = 1;
     uint64_t blocks = (uint64_t)num_sms() * (uint64_t)per_sm;
-    const uint64_t need = (prm.n_items + kSearchWarps - 1) / kSearchWarps;
+    const uint64_t need = (((uint64_t)prm.n_items << prm.parts_log2) + kSearchWarps - 1) / kSearchWarps;
     if (blocks > need) blocks = need;
     TFSM_LAUNCH(k_search, (unsigned)blocks, kSearchWarps * 32, s, g, descs, st, items, prm, counters, dom, found,
                 failed, splits, groups);
@@ -979,6 +981,13 @@ cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, c
     }
 #endif
     return e;
+}
+
+uint32_t resident_search_warps() {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search, kSearchWarps * 32, 0);
+    if (per_sm <= 0) per_sm = 1;
+    return (uint32_t)(num_sms() * per_sm * kSearchWarps);
 }
 
 cudaError_t launch_split_round(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchParams &prm,

@@ -34,6 +34,9 @@ cudaError_t launch_split_round(const Graph &g, const PatDesc *descs, PatStatus *
                                uint32_t *counters, int round, uint32_t budget, const uint32_t *dom, uint32_t *found,
                                uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s);
 
+// Warps of k_search resident on the device at once (SMs x blocks per SM x warps per block).
+uint32_t resident_search_warps();
+
 // Checked builds (-DTFSM_BOUNDS_CHECK): the first out-of-bounds access the search kernels
 // detected (count, site, index, bound); false when none or when checks are compiled out.
 bool read_bounds_check(unsigned long long rec[4]);

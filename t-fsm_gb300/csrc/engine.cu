@@ -662,6 +662,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     // chunks of all patterns are interleaved so that every pattern progresses and early exit cuts
     // the rest.
     std::vector<dev::SearchItem> items;
+    uint32_t parts_log2 = 0;
     {
         struct Q {
             uint32_t p, u, w, words;
@@ -681,6 +682,14 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
             }
         }
         const uint32_t cw = std::max<uint32_t>(1, opt.chunk_words);
+        // Calls with few words (a level of a few patterns) split every item into interleaved parts
+        // of its 32 candidates, so that enough warps search in parallel: about four items per
+        // resident warp of the search kernel (152 SMs x 40 warps on GB300).
+        uint64_t n_plain = 0;
+        for (auto &qs : ranks)
+            for (Q &q : qs) n_plain += (q.words + cw - 1) / cw;
+        const uint64_t want = 4ull * (uint64_t)dev::resident_search_warps();
+        while (parts_log2 < 5 && (n_plain << parts_log2) < want) ++parts_log2;
         for (auto &qs : ranks) {
             bool more = true;
             while (more) {
@@ -715,6 +724,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     prm.search_fill = prm.split_cap / 2;
     prm.group_cap = (uint32_t)I.groups.n;
     prm.round_budget = std::max<uint32_t>(1, opt.round_budget);
+    prm.parts_log2 = parts_log2;
     prm.defer = 0;
     prm.n_pats = (uint32_t)P;
     prm.words = total;
