@@ -96,6 +96,28 @@ struct DevBuf {
     }
 };
 
+// Page-locked host staging buffer (grows, never shrinks): copies from it are true DMA transfers.
+template <class T>
+struct PinnedBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf &) = delete;
+    PinnedBuf &operator=(const PinnedBuf &) = delete;
+    ~PinnedBuf() {
+        if (p) cudaFreeHost(p);
+    }
+    void ensure(size_t k) {
+        if (k <= n && p) return;
+        const size_t want = std::max<size_t>(k + k / 2, 1024);
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        TFSM_CK(cudaHostAlloc((void **)&p, want * sizeof(T), cudaHostAllocDefault));
+        n = want;
+    }
+};
+
 using dev::PatDesc;
 using dev::PatStatus;
 
@@ -184,6 +206,7 @@ struct GpuEngine::Impl {
     DevBuf<uint32_t> item_pu;
     DevBuf<uint64_t> prefix;
     DevBuf<dev::SearchItem> items;
+    PinnedBuf<dev::SearchItem> hitems;  // staging of the search items (rewritten each call)
     DevBuf<uint32_t> counters;
     DevBuf<dev::SplitTask> splits;
     DevBuf<dev::SplitGroup> groups;
@@ -304,6 +327,8 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     }
     I.splits.ensure(2 * task_cap);
     I.groups.ensure(group_cap);
+    // search-item staging for about 64 full-label domains (at most 1 M items, 16 MB)
+    I.hitems.ensure(std::min<size_t>(1u << 20, ((size_t)lg.n / 32 + 1) * 64));
     upload_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
@@ -377,6 +402,13 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
             acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         }
     } wall{times_.engine_ms};
+    // host wall time per phase: descriptors, init+refine, plans, items, search, results
+    auto tphase = std::chrono::steady_clock::now();
+    auto phase = [&](int k) {
+        const auto now = std::chrono::steady_clock::now();
+        times_.phase_ms[k] += std::chrono::duration<double, std::milli>(now - tphase).count();
+        tphase = now;
+    };
     const size_t P = pats.size();
     res.assign(P, EvalResult());
     if (!out.impl) out.impl.reset(new Level::Impl);
@@ -490,6 +522,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         return ms;
     };
 
+    phase(0);
     // ---- domain init and the first arc-consistency rounds: one launch sequence (a CUDA graph),
     // then one status read.  k_refine itself skips patterns that can no longer reach tau or that
     // the previous round left unchanged.
@@ -553,6 +586,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         for (size_t p = 0; p < P; ++p)
             if (express[p] && ((I.hstatus[p].changed >> 31) & 1u)) express[p] = 0;
 
+    phase(1);
     // ---- decisions from domain sizes; plans for the rest ----
     std::vector<char> need_search(P, 0);
     bool any_search = false;
@@ -654,6 +688,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     TFSM_CK(cudaMemcpyAsync(L.descs.p, L.hdescs.data(), P * sizeof(PatDesc), cudaMemcpyHostToDevice, I.stream));
     times_.h2d_bytes += P * sizeof(PatDesc);
 
+    phase(2);
     // ---- search items ----
     // Vertex-major, as the reference evaluates one pattern vertex after another
     // (parallel/comper.h:1181-1239): every pattern first searches its representative with the
@@ -661,7 +696,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     // candidates are by then largely marked found by the earlier embeddings.  Within one rank the
     // chunks of all patterns are interleaved so that every pattern progresses and early exit cuts
     // the rest.
-    std::vector<dev::SearchItem> items;
+    size_t n_items = 0;  // search items, written into the pinned staging buffer I.hitems
     uint32_t parts_log2 = 0;
     {
         struct Q {
@@ -690,6 +725,8 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
             for (Q &q : qs) n_plain += (q.words + cw - 1) / cw;
         const uint64_t want = 4ull * (uint64_t)dev::resident_search_warps();
         while (parts_log2 < 5 && (n_plain << parts_log2) < want) ++parts_log2;
+        I.hitems.ensure((size_t)n_plain);
+        dev::SearchItem *out = I.hitems.p;
         for (auto &qs : ranks) {
             bool more = true;
             while (more) {
@@ -703,20 +740,20 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
                     it.word_lo = q.w;
                     it.word_hi = std::min(q.words, q.w + cw);
                     q.w = it.word_hi;
-                    items.push_back(it);
+                    out[n_items++] = it;
                     more = true;
                 }
             }
         }
     }
-    I.items.ensure(items.size());
-    TFSM_CK(cudaMemcpyAsync(I.items.p, items.data(), items.size() * sizeof(dev::SearchItem), cudaMemcpyHostToDevice,
+    I.items.ensure(n_items);
+    TFSM_CK(cudaMemcpyAsync(I.items.p, I.hitems.p, n_items * sizeof(dev::SearchItem), cudaMemcpyHostToDevice,
                             I.stream));
-    times_.h2d_bytes += items.size() * sizeof(dev::SearchItem);
+    times_.h2d_bytes += n_items * sizeof(dev::SearchItem);
     dev::SearchParams prm;
     prm.tau = tau;
     prm.exact = opt.exact ? 1 : 0;
-    prm.n_items = (uint32_t)items.size();
+    prm.n_items = (uint32_t)n_items;
     prm.step_budget = opt.step_budget;
     prm.split_slice = std::max<uint32_t>(32, opt.split_slice);
     prm.split_cap = (uint32_t)(I.splits.n / 2);
@@ -728,6 +765,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     prm.defer = 0;
     prm.n_pats = (uint32_t)P;
     prm.words = total;
+    phase(3);
     // A search pass, then split rounds: `split_rounds` of them unconditionally (one launch
     // sequence, no host round trip), then one at a time while the previous round left tasks.
     // Searches whose remainder found no room in the split buffers were left undecided: another
@@ -739,10 +777,10 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     constexpr int kMaxPasses = 16;
     for (int pass = 0; pass < kMaxPasses; ++pass) {
         prm.defer = pass + 1 < kMaxPasses ? 1u : 0u;
-        const bool split = prm.step_budget && !items.empty();
+        const bool split = prm.step_budget && n_items != 0;
         const int fixed = split ? (int)std::min<uint32_t>(std::max<uint32_t>(1, opt.split_rounds), dev::kMaxRounds) : 0;
         // the search pass and the first split rounds: one launch sequence
-        if (items.empty()) {  // every candidate decided already: nothing to launch
+        if (n_items == 0) {  // every candidate decided already: nothing to launch
             TFSM_CK(cudaEventRecord(I.ev1, I.stream));
             read_status();
             std::memset(hcnt, 0, sizeof(hcnt));
@@ -756,7 +794,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
                 TFSM_CK(dev::launch_split_round(I.g, L.descs.p, I.status.p, prm, I.counters.p, r, prm.round_budget,
                                                 L.dom.p, L.found.p, L.failed.p, I.splits.p, I.groups.p, I.stream));
         });
-        launches += (items.empty() ? 0 : 1) + (uint64_t)fixed;
+        launches += (n_items == 0 ? 0 : 1) + (uint64_t)fixed;
         if (split) {
             int r = fixed;
             for (; r < dev::kMaxRounds; ++r) {
@@ -803,6 +841,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
                                       " (" + std::to_string(rec[0]) + " violations)");
     }
 
+    phase(4);
     if (opt.records)
         for (auto &pl : planned) {
             const PatStatus &s = I.hstatus[pl.p];
@@ -832,6 +871,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         if (opt.exact) r.frequent = mn >= tau;
         else r.frequent = s.state == dev::kFrequent || (s.state == dev::kRunning && all_reps);
     }
+    phase(5);
 }
 
 }  // namespace tfsm

@@ -205,6 +205,10 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                                  eng.times().search_ms - search_before, (unsigned long long)srch,
                                  (unsigned long long)mx);
                     const KernelTimes &now = eng.times();
+                    std::fprintf(stderr, "          host phases ms: desc %.3f init+refine %.3f plans %.3f items %.3f search %.3f results %.3f\n",
+                                 now.phase_ms[0] - before.phase_ms[0], now.phase_ms[1] - before.phase_ms[1],
+                                 now.phase_ms[2] - before.phase_ms[2], now.phase_ms[3] - before.phase_ms[3],
+                                 now.phase_ms[4] - before.phase_ms[4], now.phase_ms[5] - before.phase_ms[5]);
                     if (now.split_groups > before.split_groups) {
                         std::fprintf(stderr, "          split: %llu searches, %llu passes, %llu deferred, tasks per round",
                                      (unsigned long long)(now.split_groups - before.split_groups),

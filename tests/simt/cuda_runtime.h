@@ -347,6 +347,16 @@ inline cudaError_t cudaEventElapsedTime(float *ms, cudaEvent_t a, cudaEvent_t b)
     *ms = std::chrono::duration<float, std::milli>(b->t - a->t).count();
     return cudaSuccess;
 }
+// page-locked host memory: plain host memory here
+#define cudaHostAllocDefault 0u
+inline cudaError_t cudaHostAlloc(void **p, size_t bytes, unsigned) {
+    *p = std::malloc(bytes ? bytes : 1);
+    return *p ? cudaSuccess : cudaErrorMemoryAllocation;
+}
+inline cudaError_t cudaFreeHost(void *p) {
+    std::free(p);
+    return cudaSuccess;
+}
 // CUDA graphs: the emulated engine launches directly, only the handle type and its release exist
 typedef struct EmuGraphExec *cudaGraphExec_t;
 inline cudaError_t cudaGraphExecDestroy(cudaGraphExec_t) { return cudaSuccess; }
