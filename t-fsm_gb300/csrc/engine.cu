@@ -239,8 +239,27 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     for (uint32_t v = 0; v < lg.n; ++v) cnt[(size_t)(dl[v] = vidx(lg.vlabel[v])) + 1]++;
     I.lstart.assign((size_t)NL + 1, 0);
     for (int L = 0; L < NL; ++L) I.lstart[(size_t)L + 1] = I.lstart[(size_t)L] + cnt[(size_t)L + 1];
-    std::vector<uint32_t> to_int(lg.n), fillv(I.lstart.begin(), I.lstart.end() - 1);
-    for (uint32_t v = 0; v < lg.n; ++v) to_int[v] = fillv[(size_t)dl[v]]++;
+    // Inside a label, vertices are ranked by descending degree (ties: pruned order) and the ranks
+    // fill the label's bitmap words column by column: bit 0 of every word holds the top ranks, bit
+    // 1 the next ones, and so on.  Warps take words in parallel and bits in order, so the search
+    // meets well-connected candidates first (they usually complete an embedding quickly: a
+    // frequent pattern reaches tau with fewer exhaustive failures), while every word keeps a mix of
+    // degrees for the per-word refinement.  Any order gives the same results.
+    std::vector<std::vector<std::pair<uint32_t, uint32_t>>> members((size_t)NL);  // (-degree, v)
+    for (int L = 0; L < NL; ++L) members[(size_t)L].reserve(cnt[(size_t)L + 1]);
+    for (uint32_t v = 0; v < lg.n; ++v) members[(size_t)dl[v]].push_back({~lg.degree(v), v});
+    std::vector<uint32_t> to_int(lg.n);
+    for (int L = 0; L < NL; ++L) {
+        auto &mv = members[(size_t)L];
+        std::sort(mv.begin(), mv.end());  // descending degree, then ascending pruned id
+        const uint32_t c = (uint32_t)mv.size(), words = (c + 31) / 32;
+        uint32_t r = 0;
+        for (uint32_t bit = 0; bit < 32 && r < c; ++bit)
+            for (uint32_t w = 0; w < words && r < c; ++w) {
+                const uint32_t local = w * 32 + bit;
+                if (local < c) to_int[mv[r++].second] = I.lstart[(size_t)L] + local;
+            }
+    }
     std::vector<uint32_t> from_int(lg.n);
     for (uint32_t v = 0; v < lg.n; ++v) from_int[to_int[v]] = v;
     {
