@@ -3,7 +3,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
@@ -142,8 +144,13 @@ tfsm::EngineOptions engine_options(const tfsm_graph *g, uint32_t flags) {
 int finish_graph(std::unique_ptr<tfsm_graph> &g, int tau, std::chrono::steady_clock::time_point t0,
                  tfsm_graph **out) {
     g->tau = tau;
+    const auto t_prune = std::chrono::steady_clock::now();
     g->eng.reset(new tfsm::GpuEngine(g->lg, 0));
     g->load_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (std::getenv("TFSM_VERBOSE"))
+        std::fprintf(stderr, "[load] parse + prune %.3f ms, engine %.3f ms (%s)\n",
+                     std::chrono::duration<double, std::milli>(t_prune - t0).count(), g->eng->upload_ms(),
+                     g->eng->load_breakdown().c_str());
     *out = g.release();
     return TFSM_OK;
 }
@@ -170,15 +177,15 @@ int tfsm_graph_from_edges(uint32_t n_vertices, const int32_t *vlabels, uint64_t 
             return fail(TFSM_ERR_ARG, "null argument");
         *out = nullptr;
         auto t0 = std::chrono::steady_clock::now();
-        tfsm::RawLg raw;
-        raw.vlabel.assign(vlabels, vlabels + n_vertices);
-        raw.edges.reserve((size_t)n_edges);
-        for (uint64_t i = 0; i < n_edges; ++i) {
-            if (src[i] >= n_vertices || dst[i] >= n_vertices) return fail(TFSM_ERR_FORMAT, "edge endpoint out of range");
-            raw.edges.emplace_back(src[i], dst[i], elabels[i]);
-        }
+        std::atomic<bool> bad(false);
+        tfsm::fast::parallel_ranges((size_t)n_edges, tfsm::fast::default_threads(), [&](int, size_t k0, size_t k1) {
+            for (size_t k = k0; k < k1 && !bad.load(std::memory_order_relaxed); ++k)
+                if (src[k] >= n_vertices || dst[k] >= n_vertices) bad.store(true);
+        });
+        if (bad) return fail(TFSM_ERR_FORMAT, "edge endpoint out of range");
+        const std::vector<int> vl(vlabels, vlabels + n_vertices);
         std::unique_ptr<tfsm_graph> g(new tfsm_graph);
-        g->lg = tfsm::build_pruned_fast(raw, tau);
+        g->lg = tfsm::build_pruned_edges(vl, tfsm::EdgeArrays{src, dst, elabels, (size_t)n_edges}, tau);
         return finish_graph(g, tau, t0, out);
     });
 }

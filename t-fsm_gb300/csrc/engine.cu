@@ -16,6 +16,7 @@
 #include <cstring>
 #include <array>
 #include <cmath>
+#include <cstdio>
 #include <map>
 #include <mutex>
 #include <random>
@@ -231,6 +232,16 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     if (I.edense.size() > 250) throw EngineError(5, "more than 250 frequent edge labels");
     const int NL = (int)lg.freq_vlabels.size();
     if (NL > 250) throw EngineError(5, "more than 250 frequent vertex labels");
+    auto tck = std::chrono::steady_clock::now();
+    auto checkpoint = [&](const char *what) {
+        const auto now = std::chrono::steady_clock::now();
+        char buf[64];
+        std::snprintf(buf, sizeof(buf), "%s%s %.2f", load_breakdown_.empty() ? "" : ", ", what,
+                      std::chrono::duration<double, std::milli>(now - tck).count());
+        load_breakdown_ += buf;
+        tck = now;
+    };
+    checkpoint("device");
     const fast::LabelIndex vidx(lg.freq_vlabels), eidx(lg.freq_elabels);
     const int threads = fast::default_threads();
     // label-grouped renumbering: internal id = label_start[L] + rank within the label
@@ -301,6 +312,7 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
             }
         }
     });
+    checkpoint("csr+labels");
     I.n = lg.n;
     I.m2 = off[lg.n];
     TFSM_CK(cudaStreamCreateWithFlags(&I.stream, cudaStreamNonBlocking));
@@ -322,6 +334,7 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     TFSM_CK(cudaMemcpyAsync(I.label_start.p, I.lstart.data(), I.lstart.size() * 4, cudaMemcpyHostToDevice,
                             I.stream));
     TFSM_CK(cudaStreamSynchronize(I.stream));
+    checkpoint("upload");
     I.g.n = lg.n;
     I.g.m2 = I.m2;
     I.g.n_labels = NL;
@@ -348,6 +361,7 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     I.groups.ensure(group_cap);
     // search-item staging for about 64 full-label domains (at most 1 M items, 16 MB)
     I.hitems.ensure(std::min<size_t>(1u << 20, ((size_t)lg.n / 32 + 1) * 64));
+    checkpoint("buffers");
     upload_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 

@@ -97,6 +97,7 @@ public:
     void reset_times() { times_ = KernelTimes(); }
     uint64_t graph_bytes() const;
     double upload_ms() const { return upload_ms_; }
+    const std::string &load_breakdown() const { return load_breakdown_; }  // engine construction phases
     int dense_label(int label) const;  // -1 when the label is not frequent
     uint32_t n_vertices() const;
     // Read-only views used by the allocation-free entry point (noalloc.cu).
@@ -111,6 +112,7 @@ private:
     std::unique_ptr<Impl> impl_;
     KernelTimes times_;
     double upload_ms_ = 0;
+    std::string load_breakdown_;
 };
 
 }  // namespace tfsm

@@ -12,7 +12,10 @@
 
 #include <algorithm>
 #include <atomic>
+#include <condition_variable>
 #include <cstdint>
+#include <functional>
+#include <mutex>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -27,6 +30,74 @@ namespace fast {
 
 inline int default_threads() { return (int)std::max(1u, std::min(64u, std::thread::hardware_concurrency())); }
 
+// Process-wide workers for the loader's parallel passes (creating a thread per core for each
+// pass costs about as much as a pass on a 1 M-edge graph).  One job at a time: callers are
+// serialised on `job_mu`; a job runs `tasks` calls of `fn(task)` spread over the workers and the
+// caller.
+class Workers {
+  public:
+    static Workers &get() {
+        static Workers w(default_threads() - 1);
+        return w;
+    }
+    void run(size_t tasks, const std::function<void(size_t)> &fn) {
+        std::lock_guard<std::mutex> job(job_mu_);
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            fn_ = &fn;
+            tasks_ = tasks;
+            next_.store(0);
+            done_ = 0;
+            ++gen_;
+        }
+        cv_.notify_all();
+        drain();
+        std::unique_lock<std::mutex> lk(mu_);
+        done_cv_.wait(lk, [&]() { return done_ == tasks_; });
+        fn_ = nullptr;
+    }
+    ~Workers() {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            quit_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : th_) t.join();
+    }
+
+  private:
+    explicit Workers(int n) {
+        for (int i = 0; i < n; ++i) th_.emplace_back([this]() { loop(); });
+    }
+    void drain() {
+        for (size_t k; (k = next_.fetch_add(1)) < tasks_;) {
+            (*fn_)(k);
+            std::lock_guard<std::mutex> lk(mu_);
+            if (++done_ == tasks_) done_cv_.notify_all();
+        }
+    }
+    void loop() {
+        uint64_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&]() { return quit_ || gen_ != seen; });
+                if (quit_) return;
+                seen = gen_;
+            }
+            drain();
+        }
+    }
+    std::vector<std::thread> th_;
+    std::mutex job_mu_, mu_;
+    std::condition_variable cv_, done_cv_;
+    const std::function<void(size_t)> *fn_ = nullptr;
+    std::atomic<size_t> next_{0};
+    size_t tasks_ = 0, done_ = 0;
+    uint64_t gen_ = 0;
+    bool quit_ = false;
+};
+
 // Runs fn(t, begin, end) over [0, n) split into `threads` contiguous ranges.
 template <class F>
 void parallel_ranges(size_t n, int threads, F fn) {
@@ -35,9 +106,8 @@ void parallel_ranges(size_t n, int threads, F fn) {
         fn(0, (size_t)0, n);
         return;
     }
-    std::vector<std::thread> th;
-    for (size_t k = 0; k < t; ++k) th.emplace_back([&, k]() { fn((int)k, n * k / t, n * (k + 1) / t); });
-    for (auto &x : th) x.join();
+    const std::function<void(size_t)> task = [&](size_t k) { fn((int)k, n * k / t, n * (k + 1) / t); };
+    Workers::get().run(t, task);
 }
 
 // int label -> dense index among `labels` (ascending, distinct); -1 when absent.
@@ -179,27 +249,48 @@ inline RawLg parse_lg_text_fast(const char *data, size_t size, int threads = fas
     return raw;
 }
 
-// Same LgGraph as build_pruned(raw, tau).
-inline LgGraph build_pruned_fast(const RawLg &raw, int tau, int threads = fast::default_threads()) {
+// Edges of the input, read in place: (a, b, label) of edge k in input order.
+struct EdgeTuples {
+    const std::vector<std::tuple<uint32_t, uint32_t, int>> &e;
+    size_t size() const { return e.size(); }
+    uint32_t a(size_t k) const { return std::get<0>(e[k]); }
+    uint32_t b(size_t k) const { return std::get<1>(e[k]); }
+    int l(size_t k) const { return std::get<2>(e[k]); }
+};
+struct EdgeArrays {
+    const uint32_t *src, *dst;
+    const int32_t *lab;
+    size_t m;
+    size_t size() const { return m; }
+    uint32_t a(size_t k) const { return src[k]; }
+    uint32_t b(size_t k) const { return dst[k]; }
+    int l(size_t k) const { return lab[k]; }
+};
+
+// Same LgGraph as build_pruned on the same vertex labels and edges (endpoints already checked).
+template <class Edges>
+LgGraph build_pruned_edges(const std::vector<int> &vlabel_in, const Edges &edges, int tau,
+                           int threads = fast::default_threads()) {
     LgGraph g;
-    const size_t N = raw.vlabel.size();
+    const size_t N = vlabel_in.size(), M = edges.size();
+    if (M >= (1ull << 32)) throw LgError(5, "more than 2^32 - 1 edges");
     g.input_vertices = N;
-    g.input_edges = raw.edges.size();
+    g.input_edges = M;
     const uint64_t need = (uint64_t)std::max(tau, 0);
     // ---- label frequencies ----
-    const std::vector<int> vlabels = fast::distinct(raw.vlabel);
+    const std::vector<int> vlabels = fast::distinct(vlabel_in);
     const fast::LabelIndex vidx(vlabels);
     std::vector<uint64_t> vcount(vlabels.size(), 0);
     std::vector<int> vdense_in(N);  // dense index among all input labels
-    for (size_t i = 0; i < N; ++i) vcount[(size_t)(vdense_in[i] = vidx(raw.vlabel[i]))]++;
+    for (size_t i = 0; i < N; ++i) vcount[(size_t)(vdense_in[i] = vidx(vlabel_in[i]))]++;
     std::vector<int> elabels_all;
     {
         std::vector<int> seen;
         // few distinct edge labels in practice: collect them without sorting 2m values
         int last = 0;
         bool have = false;
-        for (auto &e : raw.edges) {
-            const int l = std::get<2>(e);
+        for (size_t k = 0; k < M; ++k) {
+            const int l = edges.l(k);
             if (have && l == last) continue;
             have = true;
             last = l;
@@ -209,8 +300,16 @@ inline LgGraph build_pruned_fast(const RawLg &raw, int tau, int threads = fast::
         elabels_all = fast::distinct(seen);
     }
     const fast::LabelIndex eidx_all(elabels_all);
+    const int T = std::max(1, threads);
+    std::vector<std::vector<uint64_t>> ecount_t((size_t)T);
+    fast::parallel_ranges(M, T, [&](int t, size_t k0, size_t k1) {
+        auto &c = ecount_t[(size_t)t];
+        c.assign(elabels_all.size(), 0);
+        for (size_t k = k0; k < k1; ++k) c[(size_t)eidx_all(edges.l(k))]++;
+    });
     std::vector<uint64_t> ecount(elabels_all.size(), 0);
-    for (auto &e : raw.edges) ecount[(size_t)eidx_all(std::get<2>(e))]++;
+    for (auto &c : ecount_t)
+        for (size_t i = 0; i < c.size(); ++i) ecount[i] += c[i];
     std::vector<char> vfreq(vlabels.size(), 0), efreq(elabels_all.size(), 0);
     for (size_t k = 0; k < vlabels.size(); ++k)
         if (vcount[k] >= need) {
@@ -227,56 +326,59 @@ inline LgGraph build_pruned_fast(const RawLg &raw, int tau, int threads = fast::
     for (size_t i = 0; i < N; ++i)
         if (vfreq[(size_t)vdense_in[i]]) {
             id_map[i] = g.n++;
-            g.vlabel.push_back(raw.vlabel[i]);
+            g.vlabel.push_back(vlabel_in[i]);
         }
-    // ---- CSR of kept edges (both directions, input order), then sorted by neighbour id ----
-    std::vector<uint64_t> deg((size_t)g.n + 1, 0);
-    std::vector<char> ekeep(raw.edges.size());
-    for (size_t k = 0; k < raw.edges.size(); ++k) {
-        const auto &e = raw.edges[k];
-        const uint32_t a = std::get<0>(e), b = std::get<1>(e);
-        const bool keep = id_map[a] != UINT32_MAX && id_map[b] != UINT32_MAX &&
-                          efreq[(size_t)eidx_all(std::get<2>(e))];
-        ekeep[k] = keep;
-        if (keep) {
-            deg[id_map[a]]++;
-            deg[id_map[b]]++;
-            g.m++;
+    // ---- CSR of kept edges (both directions), filled in parallel, then every list sorted by
+    // (neighbour id, input edge index): the reference's order (neighbour ascending, parallel edges
+    // in input order) whatever order the threads filled it in ----
+    std::vector<uint32_t> deg((size_t)g.n + 1, 0);
+    std::vector<char> ekeep(M);
+    std::vector<uint64_t> kept_t((size_t)T, 0);
+    fast::parallel_ranges(M, T, [&](int t, size_t k0, size_t k1) {
+        uint64_t kept = 0;
+        for (size_t k = k0; k < k1; ++k) {
+            const uint32_t x = id_map[edges.a(k)], y = id_map[edges.b(k)];
+            const bool keep = x != UINT32_MAX && y != UINT32_MAX && efreq[(size_t)eidx_all(edges.l(k))];
+            ekeep[k] = keep;
+            if (keep) {
+                __atomic_fetch_add(&deg[x], 1u, __ATOMIC_RELAXED);
+                __atomic_fetch_add(&deg[y], 1u, __ATOMIC_RELAXED);
+                ++kept;
+            }
         }
-    }
+        kept_t[(size_t)t] = kept;
+    });
+    for (uint64_t c : kept_t) g.m += c;
     g.offs.assign((size_t)g.n + 1, 0);
     for (uint32_t v = 0; v < g.n; ++v) g.offs[v + 1] = g.offs[v] + deg[v];
     g.nbr.assign(g.offs[g.n], 0);
     g.elab.assign(g.offs[g.n], 0);
+    std::vector<uint32_t> src_edge(g.offs[g.n]);  // input edge of each entry
     {
-        std::vector<uint64_t> fill(g.offs.begin(), g.offs.end() - 1);
-        for (size_t k = 0; k < raw.edges.size(); ++k) {
-            if (!ekeep[k]) continue;
-            const auto &e = raw.edges[k];
-            const uint32_t x = id_map[std::get<0>(e)], y = id_map[std::get<1>(e)];
-            const int l = std::get<2>(e);
-            g.nbr[fill[x]] = y;
-            g.elab[fill[x]++] = l;
-            g.nbr[fill[y]] = x;
-            g.elab[fill[y]++] = l;
-        }
+        std::vector<uint64_t> cursor(g.offs.begin(), g.offs.end() - 1);
+        fast::parallel_ranges(M, T, [&](int, size_t k0, size_t k1) {
+            for (size_t k = k0; k < k1; ++k) {
+                if (!ekeep[k]) continue;
+                const uint32_t x = id_map[edges.a(k)], y = id_map[edges.b(k)];
+                const uint64_t px = __atomic_fetch_add(&cursor[x], 1ull, __ATOMIC_RELAXED);
+                g.nbr[px] = y;
+                src_edge[px] = (uint32_t)k;
+                const uint64_t py = __atomic_fetch_add(&cursor[y], 1ull, __ATOMIC_RELAXED);
+                g.nbr[py] = x;
+                src_edge[py] = (uint32_t)k;
+            }
+        });
     }
-    // stable sort by neighbour id: key = (neighbour, position) is unique, so a plain sort is stable
-    fast::parallel_ranges(g.n, threads, [&](int, size_t b0, size_t b1) {
+    fast::parallel_ranges(g.n, T, [&](int, size_t b0, size_t b1) {
         std::vector<uint64_t> key;
-        std::vector<int> lab;
         for (size_t v = b0; v < b1; ++v) {
             const uint64_t b = g.offs[v], e = g.offs[v + 1];
-            bool sorted = true;
-            for (uint64_t i = b + 1; i < e && sorted; ++i) sorted = g.nbr[i - 1] <= g.nbr[i];
-            if (sorted) continue;
             key.clear();
-            lab.assign(g.elab.begin() + (ptrdiff_t)b, g.elab.begin() + (ptrdiff_t)e);
-            for (uint64_t i = b; i < e; ++i) key.push_back(((uint64_t)g.nbr[i] << 32) | (uint64_t)(i - b));
+            for (uint64_t i = b; i < e; ++i) key.push_back(((uint64_t)g.nbr[i] << 32) | (uint64_t)src_edge[i]);
             std::sort(key.begin(), key.end());
             for (uint64_t i = b; i < e; ++i) {
                 g.nbr[i] = (uint32_t)(key[i - b] >> 32);
-                g.elab[i] = lab[(size_t)(key[i - b] & 0xffffffffu)];
+                g.elab[i] = edges.l((size_t)(key[i - b] & 0xffffffffu));
             }
         }
     });
@@ -287,7 +389,6 @@ inline LgGraph build_pruned_fast(const RawLg &raw, int tau, int threads = fast::
     const fast::LabelIndex fv(g.freq_vlabels), fe(g.freq_elabels);
     const size_t NL = g.freq_vlabels.size(), NE = g.freq_elabels.size();
     const size_t cells = NL * NE * NL;
-    const int T = std::max(1, threads);
     std::vector<std::vector<uint32_t>> cnt_a((size_t)T), cnt_b((size_t)T);
     std::vector<std::unordered_map<uint64_t, std::pair<uint32_t, uint32_t>>> cnt_h((size_t)T);
     const bool dense = cells <= (1u << 22);
@@ -353,6 +454,11 @@ inline LgGraph build_pruned_fast(const RawLg &raw, int tau, int threads = fast::
             g.edge_pairs.push_back({g.freq_vlabels[la], g.freq_elabels[el], g.freq_vlabels[lb], ca, cb});
     }
     return g;
+}
+
+// Same LgGraph as build_pruned(raw, tau).
+inline LgGraph build_pruned_fast(const RawLg &raw, int tau, int threads = fast::default_threads()) {
+    return build_pruned_edges(raw.vlabel, EdgeTuples{raw.edges}, tau, threads);
 }
 
 inline LgGraph load_lg_fast(const std::string &path, int tau, int threads = fast::default_threads()) {

@@ -55,8 +55,21 @@ int main(int argc, char **argv) {
             raw.edges.emplace_back(a, b, wide ? el * 7919 : el);
             if (rng() % 20 == 0) raw.edges.emplace_back(b, a, wide ? (el + 1) * 7919 : el + 1);  // parallel edge
         }
+        const LgGraph ref = build_pruned(raw, tau);
         for (int threads : {1, 3, 16})
-            if (compare(build_pruned(raw, tau), build_pruned_fast(raw, tau, threads))) return 1;
+            if (compare(ref, build_pruned_fast(raw, tau, threads))) return 1;
+        // the host-array form (tfsm_graph_from_edges) reads the caller's arrays in place
+        std::vector<uint32_t> src, dst;
+        std::vector<int32_t> lab;
+        for (auto &e : raw.edges) {
+            src.push_back(std::get<0>(e));
+            dst.push_back(std::get<1>(e));
+            lab.push_back(std::get<2>(e));
+        }
+        for (int threads : {1, 16})
+            if (compare(ref, build_pruned_edges(raw.vlabel, EdgeArrays{src.data(), dst.data(), lab.data(), src.size()},
+                                                tau, threads)))
+                return 1;
         return 0;
     }
     if (argc < 3) {
