@@ -13,6 +13,7 @@
 #include <thread>
 #include <unordered_set>
 
+#include "host/lg_fast.hpp"
 #include "host/subpattern.hpp"
 
 namespace tfsm {
@@ -27,64 +28,22 @@ struct Node {
     int idx = 0;           // index inside lvl
 };
 
-// Workers kept for the whole mining run: a level's extension is a few milliseconds of work, of
-// the same order as creating and joining a thread per core for it.
+// Runs `work` on `threads` host threads (the caller's and the loader's persistent workers):
+// creating a thread per core for every level would cost as much as the level's extension.
 class Pool {
   public:
-    explicit Pool(int n) {
-        for (int i = 0; i + 1 < n; ++i) th_.emplace_back([this]() { loop(); });
-    }
-    ~Pool() {
-        {
-            std::lock_guard<std::mutex> lk(mu_);
-            quit_ = true;
-        }
-        cv_.notify_all();
-        for (auto &t : th_) t.join();
-    }
-    // Runs fn on every worker and the calling thread; returns when all calls have returned.
-    void run(const std::function<void()> &fn) {
-        if (th_.empty()) {
-            fn();
+    explicit Pool(int threads) : threads_(std::max(1, threads)) {}
+    void run(const std::function<void()> &work) {
+        if (threads_ == 1) {
+            work();
             return;
         }
-        {
-            std::lock_guard<std::mutex> lk(mu_);
-            fn_ = &fn;
-            busy_ = (int)th_.size();
-            ++gen_;
-        }
-        cv_.notify_all();
-        fn();
-        std::unique_lock<std::mutex> lk(mu_);
-        done_.wait(lk, [this]() { return busy_ == 0; });
-        fn_ = nullptr;
+        const std::function<void(size_t)> task = [&](size_t) { work(); };
+        fast::Workers::get().run((size_t)threads_, task);
     }
 
   private:
-    void loop() {
-        uint64_t seen = 0;
-        for (;;) {
-            const std::function<void()> *fn;
-            {
-                std::unique_lock<std::mutex> lk(mu_);
-                cv_.wait(lk, [&]() { return quit_ || gen_ != seen; });
-                if (quit_) return;
-                seen = gen_;
-                fn = fn_;
-            }
-            (*fn)();
-            std::lock_guard<std::mutex> lk(mu_);
-            if (--busy_ == 0) done_.notify_one();
-        }
-    }
-    std::vector<std::thread> th_;
-    std::mutex mu_;
-    std::condition_variable cv_, done_;
-    const std::function<void()> *fn_ = nullptr;
-    int busy_ = 0;
-    uint64_t gen_ = 0;
-    bool quit_ = false;
+    int threads_;
 };
 
 // Extends every frequent node (rightmost extension + canonical check), in parallel over parents.
