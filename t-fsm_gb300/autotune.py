@@ -21,10 +21,10 @@ from typing import Callable
 SPACE = [
     ("chunk_words", [1, 2]),
     ("step_budget", [16, 8, 32, 64]),
-    ("round_budget", [16, 8, 32]),
+    ("round_budget", [32, 16, 64]),
     ("split_slice", [64, 32, 128]),
-    ("refine_rounds", [2, 1, 3]),
-    ("split_rounds", [4, 2, 8]),
+    ("refine_rounds", [1, 2]),
+    ("split_rounds", [2, 4]),
 ]
 
 

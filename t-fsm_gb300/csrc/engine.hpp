@@ -36,10 +36,10 @@ struct EngineOptions {
     bool exact = false;                // evaluate every candidate (exact MNI), no early exit
     uint32_t step_budget = 16;         // chunk evaluations before a search is split (0: never)
     uint32_t split_slice = 64;         // anchor positions per split task
-    uint32_t round_budget = 16;        // step budget of a split task (the 64th round has none)
-    uint32_t split_rounds = 4;         // split rounds launched without checking for remaining tasks
+    uint32_t round_budget = 32;        // step budget of a split task (the 64th round has none)
+    uint32_t split_rounds = 2;         // split rounds launched without checking for remaining tasks
     uint32_t chunk_words = 1;          // bitmap words per search work item (x32 candidates)
-    uint32_t refine_rounds = 2;        // arc-consistency passes for patterns that need search
+    uint32_t refine_rounds = 1;        // arc-consistency passes for patterns that need search
     uint32_t max_batch = 4096;         // miner: patterns per engine call
     double time_limit_s = 0;           // miner: stop between engine calls after this long (0: none)
     // Matching order of each searched pattern vertex (never changes a result):
