@@ -266,15 +266,15 @@ def mlp_arm(args, w, g, tfsm, one_step, batched_results: Path) -> dict:
         g.set_order_policy(tfsm.ORDER_GQL)
     ms = sum(r[0] for r in runs) / len(runs)
     st = runs[0][2]
-    model.close()
-    return {"value": st["evaluations"] * 1e3 / ms, "ms_per_step": ms, "identical_output": identical,
+    return model, {"value": st["evaluations"] * 1e3 / ms, "ms_per_step": ms, "identical_output": identical,
             "search_ms_per_step": sum(r[2]["search_ms"] for r in runs) / len(runs),
             "steps_per_run": st["steps"], "training_records": int(len(x)), "train_mse": mse,
             "train_s": train_s, "training_graphs": "workload shape, seeds +10..+12, plain miner, random orders"}
 
 
-def tuned_arm(args, w, g, tfsm, one_step, batched_results: Path) -> dict:
-    """Batched path with the knobs the autotuner picks per level for this workload."""
+def tuned_arm(args, w, g, tfsm, one_step, batched_results: Path, model) -> dict:
+    """Batched path with the knobs the autotuner picks per level for this workload; then the
+    same with the learned matching orders as well."""
     import importlib.util
 
     spec = importlib.util.spec_from_file_location("autotune", PKG / "autotune.py")
@@ -290,11 +290,23 @@ def tuned_arm(args, w, g, tfsm, one_step, batched_results: Path) -> dict:
         for _ in range(args.warmup):
             one_step(0)
         runs = [one_step(0) for _ in range(args.steps)]
+        g.set_order_policy(tfsm.ORDER_MODEL, model=model)
+        outb = Path(tempfile.mktemp(suffix=".tm.txt"))
+        g.mine(max_nodes=w["max_nodes"], results_path=outb)
+        identical_both = set(tfsm.read_results(outb)) == set(tfsm.read_results(batched_results))
+        for _ in range(args.warmup):
+            one_step(0)
+        runs_both = [one_step(0) for _ in range(args.steps)]
     finally:
         g.set_level_options(0, None)
+        g.set_order_policy(tfsm.ORDER_GQL)
     ms = sum(r[0] for r in runs) / len(runs)
-    return {"value": runs[0][2]["evaluations"] * 1e3 / ms, "ms_per_step": ms, "identical_output": identical,
-            "tune_s": tune_s, "levels": {str(k): v for k, v in best.items()}}
+    ms_both = sum(r[0] for r in runs_both) / len(runs_both)
+    evals = runs[0][2]["evaluations"]
+    return {"value": evals * 1e3 / ms, "ms_per_step": ms, "identical_output": identical,
+            "tune_s": tune_s, "levels": {str(k): v for k, v in best.items()},
+            "with_learned_orders": {"value": evals * 1e3 / ms_both, "ms_per_step": ms_both,
+                                    "identical_output": identical_both}}
 
 
 def gpu_arm(args, w, world, rank):
@@ -355,8 +367,11 @@ def gpu_arm(args, w, world, rank):
 
     # batched + learned matching orders: a cost model trained on records that the plain miner logs
     # (random connected orders) on three training graphs of the workload's shape (other seeds)
-    mlp = mlp_arm(args, w, g, tfsm, one_step, outb)
-    tuned = tuned_arm(args, w, g, tfsm, one_step, outb)
+    model, mlp = mlp_arm(args, w, g, tfsm, one_step, outb)
+    try:
+        tuned = tuned_arm(args, w, g, tfsm, one_step, outb, model)
+    finally:
+        model.close()
 
     # roofline of the dominant kernel (the search): algorithmic bytes / device time
     s_ms = sum(st["search_ms"] for st in stats)
@@ -428,7 +443,9 @@ def gpu_arm(args, w, world, rank):
         }
         print(json.dumps(line), flush=True)
     g.close()
-    return 0 if identical else 1
+    same = (identical and mlp["identical_output"] and tuned["identical_output"]
+            and tuned["with_learned_orders"]["identical_output"])
+    return 0 if same else 1
 
 
 def main() -> int:
