@@ -144,7 +144,8 @@ typedef struct {
                                the run is then reported incomplete */
     uint32_t round_budget;  /* chunk evaluations of a split task before its own remainder is split
                                again (>= 1) */
-    uint32_t reserved;
+    uint32_t search_lanes;  /* lanes per search: 8 (default: four searches per warp, for calls with
+                               several patterns of at most 8 vertices) or 32; 0 means 32 */
 } tfsm_options;
 
 int tfsm_get_options(const tfsm_graph *g, tfsm_options *opt);

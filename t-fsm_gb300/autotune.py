@@ -19,6 +19,7 @@ from typing import Callable
 
 # candidate values per knob, in the order they are tuned; the first is the engine default
 SPACE = [
+    ("search_lanes", [8, 32]),
     ("chunk_words", [1, 2]),
     ("step_budget", [16, 8, 32, 64]),
     ("round_budget", [32, 16, 64]),

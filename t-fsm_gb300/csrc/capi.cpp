@@ -115,11 +115,12 @@ void fill_result(const tfsm::EvalResult &r, int n, tfsm_result *out) {
 
 const char *const kKnobRules =
     "split_slice must be >= 32; chunk_words, refine_rounds, max_batch and round_budget >= 1; split_rounds in 1..64; "
-    "time_limit_s >= 0";
+    "time_limit_s >= 0; search_lanes 8 or 32";
 
 bool knobs_valid(const tfsm_options &o) {
     return o.split_slice >= 32 && o.chunk_words >= 1 && o.refine_rounds >= 1 && o.max_batch >= 1 &&
-           o.split_rounds >= 1 && o.split_rounds <= 64 && o.round_budget >= 1 && o.time_limit_s >= 0;
+           o.split_rounds >= 1 && o.split_rounds <= 64 && o.round_budget >= 1 && o.time_limit_s >= 0 &&
+           (o.search_lanes == 0 || o.search_lanes == 8 || o.search_lanes == 32);
 }
 
 // The speed-only knobs of `o` (not the time limit, which belongs to the whole run).
@@ -131,6 +132,7 @@ void apply_knobs(const tfsm_options &o, tfsm::EngineOptions &e) {
     e.max_batch = o.max_batch;
     e.split_rounds = o.split_rounds;
     e.round_budget = o.round_budget;
+    e.search_lanes = o.search_lanes == 0 ? 32 : o.search_lanes;
 }
 
 tfsm::EngineOptions engine_options(const tfsm_graph *g, uint32_t flags) {
@@ -319,7 +321,7 @@ int tfsm_get_options(const tfsm_graph *g, tfsm_options *o) {
         o->split_rounds = g->opt.split_rounds;
         o->time_limit_s = g->opt.time_limit_s;
         o->round_budget = g->opt.round_budget;
-        o->reserved = 0;
+        o->search_lanes = g->opt.search_lanes;
         return TFSM_OK;
     });
 }

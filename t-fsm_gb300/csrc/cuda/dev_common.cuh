@@ -146,6 +146,8 @@ struct SearchParams {
                              //    split_cap - split_slack): the rounds' tasks can outnumber it
     uint32_t group_cap;      // capacity of the split-group buffer
     uint32_t round_budget;   // step budget of every split round but round kMaxRounds - 1
+    uint32_t team_lanes;     // lanes per search: 32, or 8 (four searches per warp; patterns of at
+                             //    most 8 vertices)
     uint32_t parts_log2;     // every item is claimed 2^parts_log2 times, claim k searching the bits b of
                              //    its words with b % 2^parts_log2 == k (small calls: more warps busy)
     uint32_t defer;          // 1: a search whose remainder finds no room is left undecided for the

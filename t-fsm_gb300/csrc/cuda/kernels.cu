@@ -279,31 +279,73 @@ __global__ void __launch_bounds__(256) k_refine(Graph g, const PatDesc *__restri
 // ------------------------------------------------------------------------------------------------
 namespace {
 
-struct WarpPlan {
-    uint32_t off[kMaxN];
-    uint32_t lstart[kMaxN];
-    uint32_t lend[kMaxN];
-    uint32_t orbit[kMaxN];
-    uint32_t bn[kMaxN];       // by depth
-    uint8_t order[kMaxN];     // by depth
-    uint8_t lab[kMaxN];       // dense label by pattern vertex
-    uint8_t el[kMaxN][kMaxN];
-    int32_t n;
-    uint32_t repmask;
-    uint32_t key;             // (pattern << 8 | start vertex) the plan was loaded for
-    uint64_t words;           // size of the level's bitmap pools (checked builds)
+// A team: the G lanes (32, 16 or 8) of a warp that run one search.  Small teams run several
+// independent searches per warp, which pays when label ranges are short (most lanes of a
+// 32-candidate chunk would idle); every collective is masked to the team's lanes.
+template <int G>
+struct Team {
+    uint32_t lane;  // 0 .. G-1
+    uint32_t base;  // first warp lane of the team
+    uint32_t mask;  // the team's lanes in the warp
+    __device__ explicit Team(uint32_t warp_lane)
+        : lane(warp_lane & (G - 1)), base(warp_lane & ~(uint32_t)(G - 1)),
+          mask(G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (warp_lane & ~(uint32_t)(G - 1)))) {}
+    __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+    __device__ __forceinline__ uint32_t ballot(bool p) const {
+        const uint32_t b = __ballot_sync(mask, p);
+        return G == 32 ? b : (b >> base) & ((1u << G) - 1u);
+    }
+    template <class T>
+    __device__ __forceinline__ T bcast(T v, int src) const {
+        return __shfl_sync(mask, v, src, G);
+    }
+    template <class T>
+    __device__ __forceinline__ T xor_shfl(T v, int m) const {
+        return __shfl_xor_sync(mask, v, m, G);
+    }
+    __device__ __forceinline__ bool any(bool p) const { return __any_sync(mask, p); }
+    __device__ __forceinline__ uint32_t sum(uint32_t v) const { return __reduce_add_sync(mask, v); }
+    // leader reads a word that other teams may update; the team gets one value
+    __device__ __forceinline__ uint32_t word(const uint32_t *p) const {
+        uint32_t w = 0;
+        if (lane == 0) w = __ldcg(p);
+        return bcast(w, 0);
+    }
 };
 
-struct WarpState {
-    uint32_t emb[kMaxN];      // by pattern vertex
-    uint32_t pos[kMaxN];      // by depth: next unevaluated anchor position
-    uint32_t end[kMaxN];      // by depth: end of the anchor range
-    uint32_t base[kMaxN];     // by depth: first position of the chunk held in mask / rest
-    uint32_t mask[kMaxN];     // by depth: surviving candidates already known to be in w's MNI domain
-    uint32_t rest[kMaxN];     // by depth: the other surviving candidates (tried after `mask`)
-    uint8_t anchor[kMaxN];    // by depth: pattern vertex whose adjacency is scanned
-    uint32_t blo[kMaxN][kMaxN];  // [depth][backward neighbour b]: label range of order[depth]'s
-    uint32_t bhi[kMaxN][kMaxN];  //   label inside emb[b]'s adjacency
+// Largest pattern a team of G lanes searches (its per-depth state is sized for it).
+template <int G>
+struct TeamMaxN {
+    static constexpr int value = G == 32 ? kMaxN : 8;
+};
+
+template <int N>
+struct Plan {
+    uint32_t off[N];
+    uint32_t lstart[N];
+    uint32_t lend[N];
+    uint32_t orbit[N];
+    uint32_t bn[N];       // by depth
+    uint8_t order[N];     // by depth
+    uint8_t lab[N];       // dense label by pattern vertex
+    uint8_t el[N][N];
+    int32_t n;
+    uint32_t repmask;
+    uint32_t key;         // (pattern << 8 | start vertex) the plan was loaded for
+    uint64_t words;       // size of the level's bitmap pools (checked builds)
+};
+
+template <int N>
+struct State {
+    uint32_t emb[N];      // by pattern vertex
+    uint32_t pos[N];      // by depth: next unevaluated anchor position
+    uint32_t end[N];      // by depth: end of the anchor range
+    uint32_t base[N];     // by depth: first position of the chunk held in mask / rest
+    uint32_t mask[N];     // by depth: surviving candidates already known to be in w's MNI domain
+    uint32_t rest[N];     // by depth: the other surviving candidates (tried after `mask`)
+    uint8_t anchor[N];    // by depth: pattern vertex whose adjacency is scanned
+    uint32_t blo[N][N];   // [depth][backward neighbour b]: label range of order[depth]'s
+    uint32_t bhi[N][N];   //   label inside emb[b]'s adjacency
 };
 
 enum : int { kFail = 0, kFound = 1, kAbort = 2, kCancel = 3 };
@@ -324,22 +366,23 @@ constexpr uint32_t kCancelEvery = 16;
 // graphs (the extra ballot and found-word loads cost more than the reordering saves): off.
 constexpr bool kFoundFirst = false;
 
-__device__ __forceinline__ void load_plan(WarpPlan &P, const PatDesc &D, uint32_t p, int u, uint32_t lane,
+template <int G, int N>
+__device__ __forceinline__ void load_plan(const Team<G> &T, Plan<N> &P, const PatDesc &D, uint32_t p, int u,
                                           uint64_t words) {
     const uint32_t key = (p << 8) | (uint32_t)u;
-    if (P.key == key) return;  // all lanes read the same shared value
-    __syncwarp();
-    if (lane < (uint32_t)kMaxN) {
-        P.off[lane] = (uint32_t)D.off[lane];
-        P.lstart[lane] = D.lstart[lane];
-        P.lend[lane] = D.lstart[lane] + D.lsize[lane];
-        P.orbit[lane] = D.orbit_mask[lane];
-        P.bn[lane] = D.bn[u][lane];
-        P.order[lane] = D.order[u][lane];
-        P.lab[lane] = (uint8_t)D.lab[lane];
+    if (P.key == key) return;  // every lane of the team reads the same shared value
+    T.sync();
+    for (uint32_t i = T.lane; i < (uint32_t)N; i += G) {
+        P.off[i] = (uint32_t)D.off[i];
+        P.lstart[i] = D.lstart[i];
+        P.lend[i] = D.lstart[i] + D.lsize[i];
+        P.orbit[i] = D.orbit_mask[i];
+        P.bn[i] = D.bn[u][i];
+        P.order[i] = D.order[u][i];
+        P.lab[i] = (uint8_t)D.lab[i];
     }
-    for (uint32_t i = lane; i < (uint32_t)(kMaxN * kMaxN); i += 32) (&P.el[0][0])[i] = (&D.el[0][0])[i];
-    if (lane == 0) {
+    for (uint32_t i = T.lane; i < (uint32_t)(N * N); i += G) P.el[i / N][i % N] = D.el[i / N][i % N];
+    if (T.lane == 0) {
         P.n = D.n;
         uint32_t rm = 0;
         for (int k = 0; k < D.n; ++k)
@@ -348,12 +391,13 @@ __device__ __forceinline__ void load_plan(WarpPlan &P, const PatDesc &D, uint32_
         P.key = key;
         P.words = words;
     }
-    __syncwarp();
+    T.sync();
 }
 
 // Anchor of depth d: the backward neighbour whose label sub-range is the shortest.  Lane k
-// handles the k-th backward neighbour; a warp minimum picks the winner.
-__device__ __forceinline__ void setup_depth(const Graph &g, const WarpPlan &P, WarpState &S, int d, uint32_t lane,
+// handles the k-th backward neighbour; a team minimum picks the winner.
+template <int G, int N>
+__device__ __forceinline__ void setup_depth(const Team<G> &T, const Graph &g, const Plan<N> &P, State<N> &S, int d,
                                             uint32_t &bytes) {
     const int w = P.order[d];
     const uint32_t bnm = P.bn[d];
@@ -361,9 +405,9 @@ __device__ __forceinline__ void setup_depth(const Graph &g, const WarpPlan &P, W
     unsigned long long key = ~0ull;
     uint32_t lo = 0, hi = 0;
     int b = 0;
-    if ((int)lane < nb) {
+    if ((int)T.lane < nb) {
         uint32_t m = bnm;
-        for (uint32_t k = 0; k < lane; ++k) m &= m - 1;
+        for (uint32_t k = 0; k < T.lane; ++k) m &= m - 1;
         b = __ffs(m) - 1;
         const uint32_t y = S.emb[b];
         if (TFSM_IN(2, y, g.n)) {
@@ -374,31 +418,32 @@ __device__ __forceinline__ void setup_depth(const Graph &g, const WarpPlan &P, W
         }
         S.blo[d][b] = lo;  // lane k owns backward neighbour b's slot
         S.bhi[d][b] = hi;
-        key = ((unsigned long long)(hi - lo) << 32) | lane;
+        key = ((unsigned long long)(hi - lo) << 32) | T.lane;
     }
 #pragma unroll
-    for (int s = 16; s > 0; s >>= 1) {
-        const unsigned long long o = __shfl_xor_sync(0xffffffffu, key, s);
+    for (int s = G / 2; s > 0; s >>= 1) {
+        const unsigned long long o = T.xor_shfl(key, s);
         key = o < key ? o : key;
     }
-    const int win = (int)(key & 31ull);
-    lo = __shfl_sync(0xffffffffu, lo, win);
-    hi = __shfl_sync(0xffffffffu, hi, win);
-    b = __shfl_sync(0xffffffffu, b, win);
-    if (lane == 0) {
+    const int win = (int)(key & (unsigned long long)(G - 1));
+    lo = T.bcast(lo, win);
+    hi = T.bcast(hi, win);
+    b = T.bcast(b, win);
+    if (T.lane == 0) {
         S.pos[d] = lo;
         S.end[d] = hi;
         S.mask[d] = 0;
         S.rest[d] = 0;
         S.anchor[d] = (uint8_t)b;
     }
-    __syncwarp();
+    T.sync();
 }
 
 // Is adjacency position `idx` of the depth-d anchor a valid extension?  (one lane, one position)
 // `known` is set when x is already proven to be in w's MNI domain (a found embedding maps w to x).
 // A candidate proven to be in no embedding as w (its `failed` bit) is rejected: sound pruning.
-__device__ __forceinline__ bool check_candidate(const Graph &g, const WarpPlan &P, const WarpState &S,
+template <int N>
+__device__ __forceinline__ bool check_candidate(const Graph &g, const Plan<N> &P, const State<N> &S,
                                                 const uint32_t *__restrict__ dom, const uint32_t *found,
                                                 const uint32_t *failed, int d, uint32_t idx, uint32_t &x_out,
                                                 bool &known, uint32_t &bytes) {
@@ -447,26 +492,27 @@ __device__ __forceinline__ bool check_candidate(const Graph &g, const WarpPlan &
 // (S.emb[order[0..start-1]]).  With `slice`, depth `start` scans only anchor positions [lo, hi).
 // The search never backtracks above `start`.  Returns kAbort once `budget` chunk evaluations are
 // exceeded (budget 0: unlimited); `abort_depth` then says where it stopped.  Returns kCancel when
-// `cancel` says the search no longer matters.
-__device__ __forceinline__ int dfs(const Graph &g, const WarpPlan &P, WarpState &S, const uint32_t *__restrict__ dom,
-                                   const uint32_t *found, const uint32_t *failed, uint32_t lane, int start, bool slice,
-                                   uint32_t lo, uint32_t hi, uint32_t budget, const Cancel &cancel, uint32_t &steps,
-                                   int &abort_depth, uint32_t &bytes) {
+// `cancel` says the search no longer matters.  A chunk is G consecutive anchor positions.
+template <int G, int N>
+__device__ __forceinline__ int dfs(const Team<G> &T, const Graph &g, const Plan<N> &P, State<N> &S,
+                                   const uint32_t *__restrict__ dom, const uint32_t *found, const uint32_t *failed,
+                                   int start, bool slice, uint32_t lo, uint32_t hi, uint32_t budget,
+                                   const Cancel &cancel, uint32_t &steps, int &abort_depth, uint32_t &bytes) {
     const int n = P.n;
-    setup_depth(g, P, S, start, lane, bytes);
+    setup_depth(T, g, P, S, start, bytes);
     if (slice) {
-        if (lane == 0) {
+        if (T.lane == 0) {
             S.pos[start] = lo;
             S.end[start] = hi;
         }
-        __syncwarp();
+        T.sync();
     }
     int d = start;
     for (;;) {
         const uint32_t mk = S.mask[d], mr = S.rest[d];
         const uint32_t pos = S.pos[d], end = S.end[d];
         // every lane has read this depth's state before lane 0 may overwrite it below
-        __syncwarp();
+        T.sync();
         if ((mk | mr) == 0) {
             if (pos >= end) {
                 if (d == start) return kFail;
@@ -479,52 +525,52 @@ __device__ __forceinline__ int dfs(const Graph &g, const WarpPlan &P, WarpState 
             }
             if (steps && steps % kCancelEvery == 0) {
                 int c = 0;
-                if (lane == 0) {
+                if (T.lane == 0) {
                     c = (__ldcg(cancel.found_word) & cancel.bit) || __ldcg(&cancel.ps->state) != kRunning ||
                         (!cancel.exact && ((__ldcg(&cancel.ps->done_mask) >> cancel.u) & 1u));
                 }
-                if (__shfl_sync(0xffffffffu, c, 0)) return kCancel;
+                if (T.bcast(c, 0)) return kCancel;
             }
-            const uint32_t idx = pos + lane;
+            const uint32_t idx = pos + T.lane;
             uint32_t x = 0;
             bool known = false;
             const bool ok = idx < end && check_candidate(g, P, S, dom, found, failed, d, idx, x, known, bytes);
-            const uint32_t bal = __ballot_sync(0xffffffffu, ok);
-            const uint32_t pref = kFoundFirst ? __ballot_sync(0xffffffffu, ok && known) : 0u;
+            const uint32_t bal = T.ballot(ok);
+            const uint32_t pref = kFoundFirst ? T.ballot(ok && known) : 0u;
             ++steps;
             if (d == n - 1) {
                 if (bal) {
-                    if ((int)lane == __ffs(bal) - 1) S.emb[P.order[d]] = x;
-                    __syncwarp();
+                    if ((int)T.lane == __ffs(bal) - 1) S.emb[P.order[d]] = x;
+                    T.sync();
                     return kFound;
                 }
-                if (lane == 0) S.pos[d] = pos + 32;
-                __syncwarp();
+                if (T.lane == 0) S.pos[d] = pos + G;
+                T.sync();
                 continue;
             }
-            if (lane == 0) {
+            if (T.lane == 0) {
                 S.base[d] = pos;
-                S.pos[d] = pos + 32;
+                S.pos[d] = pos + G;
                 S.mask[d] = pref;
                 S.rest[d] = bal & ~pref;
             }
-            __syncwarp();
+            T.sync();
             continue;
         }
         // candidates known to be in w's MNI domain first: they usually complete an embedding
         const bool from_pref = mk != 0;
         const uint32_t m = from_pref ? mk : mr;
         const int i = __ffs(m) - 1;
-        if (lane == 0) {
+        if (T.lane == 0) {
             if (from_pref) S.mask[d] = m & (m - 1);
             else S.rest[d] = m & (m - 1);
             if (TFSM_IN(7, S.base[d] + i, g.m2)) S.emb[P.order[d]] = __ldg(g.col + S.base[d] + i);
         }
-        __syncwarp();
+        T.sync();
         bytes += 4;  // re-read of the chosen neighbour id
         if (!TFSM_IN(8, d + 1, n)) return kFail;
         ++d;
-        setup_depth(g, P, S, d, lane, bytes);
+        setup_depth(T, g, P, S, d, bytes);
     }
 }
 
@@ -532,7 +578,7 @@ __device__ __forceinline__ int dfs(const Graph &g, const WarpPlan &P, WarpState 
 // failure under contention); false when they do not all fit.  The counter may then pass `limit`
 // (readers clamp it to the buffer size); a failed claim [first, first + k) still owns its slots
 // that lie inside the buffer and must fill them (split tasks: with null tasks).  A counter already
-// at `limit` is not advanced, so it passes `limit` by at most one claim per running warp.
+// at `limit` is not advanced, so it passes `limit` by at most one claim per running team.
 __device__ __forceinline__ bool reserve(uint32_t *counter, uint32_t k, uint32_t limit, uint32_t &first) {
     if (__ldcg(counter) >= limit) {
         first = 0xffffffffu;
@@ -545,24 +591,26 @@ __device__ __forceinline__ bool reserve(uint32_t *counter, uint32_t k, uint32_t 
 // Unexplored anchor positions left at depth j of a search that stopped at depth `dabort`: the
 // not-yet-taken candidates of j's current chunk, then [pos[j], end[j]).  Candidates of a chunk are
 // taken lowest position first, so everything below the lowest pending one is explored.
-__device__ __forceinline__ void remainder_at(const WarpState &S, int j, int dabort, uint32_t &from, uint32_t &to) {
+template <int N>
+__device__ __forceinline__ void remainder_at(const State<N> &S, int j, int dabort, uint32_t &from, uint32_t &to) {
     to = S.end[j];
     const uint32_t m = S.mask[j] | S.rest[j];
     from = (j == dabort || m == 0) ? S.pos[j] : S.base[j] + (uint32_t)(__ffs(m) - 1);
     if (from > to) from = to;
 }
 
-// Warp-uniform claim of `k` slots below `limit`; the slots of a failed claim inside the buffer
+// Team-uniform claim of `k` slots below `limit`; the slots of a failed claim inside the buffer
 // (`cap`) become null tasks.
-__device__ __forceinline__ bool claim_tasks(SplitTask *out, uint32_t *out_count, uint32_t k, uint32_t limit,
-                                            uint32_t cap, uint32_t lane, uint32_t &t0) {
+template <int G>
+__device__ __forceinline__ bool claim_tasks(const Team<G> &T, SplitTask *out, uint32_t *out_count, uint32_t k,
+                                            uint32_t limit, uint32_t cap, uint32_t &t0) {
     int ok = 0;
-    if (lane == 0) ok = reserve(out_count, k, limit, t0) ? 1 : 0;
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    t0 = __shfl_sync(0xffffffffu, t0, 0);
+    if (T.lane == 0) ok = reserve(out_count, k, limit, t0) ? 1 : 0;
+    ok = T.bcast(ok, 0);
+    t0 = T.bcast(t0, 0);
     if (!ok && t0 < cap) {
         const uint32_t e = (uint64_t)t0 + k < cap ? t0 + k : cap;
-        for (uint32_t q = t0 + lane; q < e; q += 32) out[q].pat = kNullTask;
+        for (uint32_t q = t0 + T.lane; q < e; q += G) out[q].pat = kNullTask;
     }
     return ok != 0;
 }
@@ -571,9 +619,10 @@ __device__ __forceinline__ bool claim_tasks(SplitTask *out, uint32_t *out_count,
 // sliced (`slice` anchor positions each) below `limit`; when that does not fit, compact (one task
 // per depth, re-split by later rounds) below limit + slack.  Returns how many were written; 0 when
 // neither fits (then nothing is written).
-__device__ uint32_t emit_remainder(const WarpPlan &P, const WarpState &S, uint32_t p, int u, uint32_t v, int start,
-                                   int dabort, uint32_t group, uint32_t slice, SplitTask *out, uint32_t *out_count,
-                                   uint32_t cap, uint32_t limit, uint32_t slack, uint32_t lane, uint64_t m2) {
+template <int G, int N>
+__device__ uint32_t emit_remainder(const Team<G> &T, const Plan<N> &P, const State<N> &S, uint32_t p, int u,
+                                   uint32_t v, int start, int dabort, uint32_t group, uint32_t slice, SplitTask *out,
+                                   uint32_t *out_count, uint32_t cap, uint32_t limit, uint32_t slack, uint64_t m2) {
     uint32_t total = 0, depths = 0;
     for (int j = start; j <= dabort; ++j) {
         uint32_t f, t;
@@ -583,12 +632,12 @@ __device__ uint32_t emit_remainder(const WarpPlan &P, const WarpState &S, uint32
     }
     if (total == 0) return 0;
     uint32_t t0 = 0;
-    if (!claim_tasks(out, out_count, total, limit, cap, lane, t0)) {
-        if (!claim_tasks(out, out_count, depths, limit + slack, cap, lane, t0)) return 0;
+    if (!claim_tasks(T, out, out_count, total, limit, cap, t0)) {
+        if (!claim_tasks(T, out, out_count, depths, limit + slack, cap, t0)) return 0;
         slice = 0xffffffffu;  // compact: one task per non-empty depth
         total = depths;
     }
-    for (uint32_t k = lane; k < total; k += 32) {
+    for (uint32_t k = T.lane; k < total; k += G) {
         uint32_t acc = 0, f = 0, t = 0, c = 0;
         int j = start;
         for (; j <= dabort; ++j) {
@@ -606,18 +655,19 @@ __device__ uint32_t emit_remainder(const WarpPlan &P, const WarpState &S, uint32
         task.lo = f + (k - acc) * slice;  // k - acc is 0 when compact
         task.hi = t - task.lo > slice ? task.lo + slice : t;
         task.group = group;
-        for (int q = 0; q < kMaxN; ++q) task.prefix[q] = q < j ? S.emb[P.order[q]] : 0u;
+        for (int q = 0; q < kMaxN; ++q) task.prefix[q] = q < j && q < N ? S.emb[P.order[q]] : 0u;
         if (TFSM_IN(14, t0 + k, cap) && TFSM_IN(48, task.hi, m2 + 1)) out[t0 + k] = task;
     }
     return total;
 }
 
 // Add every vertex of the embedding in S (and its automorphic images) to the found bitmaps.
-__device__ __forceinline__ void mark_found(const WarpPlan &P, const WarpState &S, PatStatus &st,
-                                           uint32_t *__restrict__ found, uint32_t tau, bool exact, uint32_t lane) {
-    if ((int)lane < P.n) {
-        const uint32_t x = S.emb[lane];
-        uint32_t orb = P.orbit[lane];
+template <int G, int N>
+__device__ __forceinline__ void mark_found(const Team<G> &T, const Plan<N> &P, const State<N> &S, PatStatus &st,
+                                           uint32_t *__restrict__ found, uint32_t tau, bool exact) {
+    for (int q = (int)T.lane; q < P.n; q += G) {
+        const uint32_t x = S.emb[q];
+        uint32_t orb = P.orbit[q];
         while (orb) {
             const int k = __ffs(orb) - 1;
             orb &= orb - 1;
@@ -634,13 +684,15 @@ __device__ __forceinline__ void mark_found(const WarpPlan &P, const WarpState &S
             }
         }
     }
-    __syncwarp();
+    T.sync();
 }
 
 // v has no embedding as u (nor as any vertex automorphic to u).
-__device__ __forceinline__ void mark_failed(const WarpPlan &P, PatStatus &st, uint32_t *__restrict__ failed, int u,
-                                            uint32_t v, uint32_t tau, bool exact, uint32_t lane) {
-    if (lane == 0) {
+template <int G, int N>
+__device__ __forceinline__ void mark_failed(const Team<G> &T, const Plan<N> &P, PatStatus &st,
+                                            uint32_t *__restrict__ failed, int u, uint32_t v, uint32_t tau,
+                                            bool exact) {
+    if (T.lane == 0) {
         uint32_t orb = P.orbit[u];
         while (orb) {
             const int k = __ffs(orb) - 1;
@@ -655,24 +707,25 @@ __device__ __forceinline__ void mark_failed(const WarpPlan &P, PatStatus &st, ui
             }
         }
     }
-    __syncwarp();
+    T.sync();
 }
 
-// Warp-uniform: lane 0 reads the shared flags and broadcasts the decision.
-__device__ __forceinline__ bool pattern_stops(const PatStatus &st, int u, bool exact, uint32_t lane) {
+// Team-uniform: lane 0 reads the shared flags and broadcasts the decision.
+template <int G>
+__device__ __forceinline__ bool pattern_stops(const Team<G> &T, const PatStatus &st, int u, bool exact) {
     int stop = 0;
-    if (lane == 0) {
+    if (T.lane == 0) {
         stop = __ldcg(&st.state) != kRunning;
         if (!stop && !exact) stop = (__ldcg(&st.done_mask) >> u) & 1u;
     }
-    return __shfl_sync(0xffffffffu, stop, 0) != 0;
+    return T.bcast(stop, 0) != 0;
 }
-
 
 }  // namespace
 
 // The search pass.  Counters: see kNumCounters in dev_common.cuh.  Split tasks of round 0 go to
-// `splits` (the first buffer).
+// `splits` (the first buffer).  Each team of G lanes claims its own items.
+template <int G>
 __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const PatDesc *__restrict__ descs,
                                                               PatStatus *__restrict__ st,
                                                               const SearchItem *__restrict__ items, SearchParams prm,
@@ -682,76 +735,77 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
                                                               uint32_t *__restrict__ failed,
                                                               SplitTask *__restrict__ splits,
                                                               SplitGroup *__restrict__ groups) {
-    __shared__ WarpPlan plans[kSearchWarps];
-    __shared__ WarpState states[kSearchWarps];
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t wid = threadIdx.x >> 5;
-    WarpPlan &P = plans[wid];
-    WarpState &S = states[wid];
-    if (lane == 0) P.key = 0xffffffffu;
-    __syncwarp();
+    constexpr int N = TeamMaxN<G>::value;
+    constexpr int kTeams = kSearchWarps * 32 / G;
+    __shared__ Plan<N> plans[kTeams];
+    __shared__ State<N> states[kTeams];
+    const Team<G> T(threadIdx.x & 31);
+    Plan<N> &P = plans[threadIdx.x / G];
+    State<N> &S = states[threadIdx.x / G];
+    if (T.lane == 0) P.key = 0xffffffffu;
+    T.sync();
     const bool exact = prm.exact != 0;
     for (;;) {
         uint32_t it = 0;
-        if (lane == 0) it = atomicAdd(&counters[0], 1u);
-        it = __shfl_sync(0xffffffffu, it, 0);
+        if (T.lane == 0) it = atomicAdd(&counters[0], 1u);
+        it = T.bcast(it, 0);
         if (it >= (prm.n_items << prm.parts_log2)) break;
         const SearchItem item = items[it >> prm.parts_log2];
         const uint32_t pmask = part_mask(it & ((1u << prm.parts_log2) - 1), prm.parts_log2);
         const uint32_t p = item.pat;
         const int u = item.u;
-        if (!TFSM_IN(12, p, prm.n_pats) || !TFSM_IN(20, u, kMaxN)) continue;
-        load_plan(P, descs[p], p, u, lane, prm.words);
+        if (!TFSM_IN(12, p, prm.n_pats) || !TFSM_IN(20, u, N)) continue;
+        if (!TFSM_IN(22, descs[p].n, N + 1)) continue;
+        load_plan(T, P, descs[p], p, u, prm.words);
         PatStatus &ps = st[p];
         unsigned long long n_search = 0, n_steps = 0, n_bytes = 0, max_steps = 0;
         bool stop = false, abandon = false;
         for (uint32_t word = item.word_lo; word < item.word_hi && !stop; ++word) {
-            if (pattern_stops(ps, u, exact, lane)) break;
+            if (pattern_stops(T, ps, u, exact)) break;
             const uint32_t o = P.off[u] + word;
             if (!TFSM_IN(13, o, prm.words)) break;
-            uint32_t cand = warp_word(dom + o, lane) & ~warp_word(found + o, lane) & ~warp_word(failed + o, lane) &
-                            pmask;
+            uint32_t cand = T.word(dom + o) & ~T.word(found + o) & ~T.word(failed + o) & pmask;
             while (cand) {
                 const int b = __ffs(cand) - 1;
                 cand &= cand - 1;
-                if ((warp_word(found + o, lane) >> b) & 1u) continue;
-                if (pattern_stops(ps, u, exact, lane)) {
+                if ((T.word(found + o) >> b) & 1u) continue;
+                if (pattern_stops(T, ps, u, exact)) {
                     stop = true;
                     break;
                 }
                 if (prm.defer && prm.step_budget) {
-                    // the first split round's share of the buffer is full: this warp starts no
+                    // the first split round's share of the buffer is full: this team starts no
                     // more searches in this pass; the next pass takes up what is left
                     int full = 0;
-                    if (lane == 0) full = __ldcg(&counters[2]) >= prm.search_fill;
-                    if (__shfl_sync(0xffffffffu, full, 0)) {
+                    if (T.lane == 0) full = __ldcg(&counters[2]) >= prm.search_fill;
+                    if (T.bcast(full, 0)) {
                         abandon = stop = true;
                         break;
                     }
                 }
                 const uint32_t v = P.lstart[u] + word * 32 + b;
-                if (lane == 0) S.emb[u] = v;
-                __syncwarp();
+                if (T.lane == 0) S.emb[u] = v;
+                T.sync();
                 uint32_t steps = 0, bytes = 12;  // + domain, found and failed words of v
                 int adepth = 0;
                 ++n_search;
                 const Cancel cancel{found + o, 1u << b, &ps, u, exact};
-                int r = dfs(g, P, S, dom, found, failed, lane, 1, false, 0, 0, prm.step_budget, cancel, steps, adepth,
+                int r = dfs(T, g, P, S, dom, found, failed, 1, false, 0, 0, prm.step_budget, cancel, steps, adepth,
                             bytes);
                 if (r == kAbort) {
                     // Hub splitting: the unexplored remainder becomes tasks for the split rounds,
                     // grouped so that the last one to finish can decide v.
                     uint32_t g0 = 0;
                     int okg = 0;
-                    if (lane == 0)
+                    if (T.lane == 0)
                         okg = reserve(&counters[1], 1, prm.group_cap, g0) && TFSM_IN(15, g0, prm.group_cap) ? 1 : 0;
-                    okg = __shfl_sync(0xffffffffu, okg, 0);
-                    g0 = __shfl_sync(0xffffffffu, g0, 0);
+                    okg = T.bcast(okg, 0);
+                    g0 = T.bcast(g0, 0);
                     uint32_t added = 0;
                     if (okg)
-                        added = emit_remainder(P, S, p, u, v, 1, adepth, g0, prm.split_slice, splits, &counters[2],
-                                               prm.split_cap, prm.search_fill, prm.split_slack, lane, g.m2);
-                    if (lane == 0 && okg) {  // read only by the split rounds, which run after this kernel
+                        added = emit_remainder(T, P, S, p, u, v, 1, adepth, g0, prm.split_slice, splits, &counters[2],
+                                               prm.split_cap, prm.search_fill, prm.split_slack, g.m2);
+                    if (T.lane == 0 && okg) {  // read only by the split rounds, which run after this kernel
                         groups[g0].pat = p;
                         groups[g0].u = (uint16_t)u;
                         groups[g0].v = v;
@@ -759,24 +813,24 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
                         groups[g0].incomplete = 0;
                     }
                     if (added || prm.defer) {
-                        if (!added && lane == 0) atomicAdd(&counters[kDeferred], 1u);  // buffers full
+                        if (!added && T.lane == 0) atomicAdd(&counters[kDeferred], 1u);  // buffers full
                         n_steps += steps;
-                        n_bytes += __reduce_add_sync(0xffffffffu, bytes);
+                        n_bytes += T.sum(bytes);
                         continue;  // decided by the split rounds, or by the next pass
                     }
                     // buffers full, last pass: finish this search here without a budget
-                    if (lane == 0) S.emb[u] = v;
-                    __syncwarp();
-                    r = dfs(g, P, S, dom, found, failed, lane, 1, false, 0, 0, 0, cancel, steps, adepth, bytes);
+                    if (T.lane == 0) S.emb[u] = v;
+                    T.sync();
+                    r = dfs(T, g, P, S, dom, found, failed, 1, false, 0, 0, 0, cancel, steps, adepth, bytes);
                 }
                 n_steps += steps;
                 max_steps = steps > max_steps ? steps : max_steps;
-                n_bytes += __reduce_add_sync(0xffffffffu, bytes);
-                if (r == kFound) mark_found(P, S, ps, found, prm.tau, exact, lane);
-                else if (r == kFail) mark_failed(P, ps, failed, u, v, prm.tau, exact, lane);
+                n_bytes += T.sum(bytes);
+                if (r == kFound) mark_found(T, P, S, ps, found, prm.tau, exact);
+                else if (r == kFail) mark_failed(T, P, ps, failed, u, v, prm.tau, exact);
             }
         }
-        if (lane == 0 && n_search) {
+        if (T.lane == 0 && n_search) {
             atomicAdd(&ps.searches, n_search);
             atomicAdd(&ps.steps, n_steps);
             atomicAdd(&ps.bytes, n_bytes);
@@ -785,7 +839,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
             atomicAdd(&ps.searches_u[u], (uint32_t)n_search);
         }
         if (abandon) {
-            if (lane == 0) atomicAdd(&counters[kDeferred], 1u);
+            if (T.lane == 0) atomicAdd(&counters[kDeferred], 1u);
             return;
         }
     }
@@ -794,6 +848,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
 // One split round: processes the tasks of round `round` (in `in`), searching each below its
 // partial embedding; a task that exceeds `budget` (0: never, as in the last round) emits its own
 // unexplored remainder into `out` for the next round, inside the same group.
+template <int G>
 __global__ void __launch_bounds__(kSearchWarps * 32) k_split(Graph g, const PatDesc *__restrict__ descs,
                                                              PatStatus *__restrict__ st, SearchParams prm,
                                                              uint32_t *__restrict__ counters, int round,
@@ -803,61 +858,61 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_split(Graph g, const PatD
                                                              const SplitTask *__restrict__ in,
                                                              SplitTask *__restrict__ out,
                                                              SplitGroup *__restrict__ groups) {
-    __shared__ WarpPlan plans[kSearchWarps];
-    __shared__ WarpState states[kSearchWarps];
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t wid = threadIdx.x >> 5;
-    WarpPlan &P = plans[wid];
-    WarpState &S = states[wid];
-    if (lane == 0) P.key = 0xffffffffu;
-    __syncwarp();
+    constexpr int N = TeamMaxN<G>::value;
+    constexpr int kTeams = kSearchWarps * 32 / G;
+    __shared__ Plan<N> plans[kTeams];
+    __shared__ State<N> states[kTeams];
+    const Team<G> T(threadIdx.x & 31);
+    Plan<N> &P = plans[threadIdx.x / G];
+    State<N> &S = states[threadIdx.x / G];
+    if (T.lane == 0) P.key = 0xffffffffu;
+    T.sync();
     const bool exact = prm.exact != 0;
     const uint32_t n_tasks = min(counters[2 + round], prm.split_cap);
     for (;;) {
         uint32_t it = 0;
-        if (lane == 0) it = atomicAdd(&counters[kClaimBase + round], 1u);
-        it = __shfl_sync(0xffffffffu, it, 0);
+        if (T.lane == 0) it = atomicAdd(&counters[kClaimBase + round], 1u);
+        it = T.bcast(it, 0);
         if (it >= n_tasks) break;
         const SplitTask &t = in[it];  // fields read one by one; the prefix stays in memory
         const uint32_t p = t.pat;
         if (p == kNullTask) continue;  // a slot of a claim that did not fit
         const int u = t.u;
         const int depth = t.depth;
-        if (!TFSM_IN(16, p, prm.n_pats) || !TFSM_IN(17, t.group, prm.group_cap) || !TFSM_IN(21, u, kMaxN)) continue;
-        load_plan(P, descs[p], p, u, lane, prm.words);
+        if (!TFSM_IN(16, p, prm.n_pats) || !TFSM_IN(17, t.group, prm.group_cap) || !TFSM_IN(21, u, N)) continue;
+        if (!TFSM_IN(23, descs[p].n, N + 1)) continue;
+        load_plan(T, P, descs[p], p, u, prm.words);
         PatStatus &ps = st[p];
         SplitGroup &grp = groups[t.group];
         const uint32_t xl = t.v - P.lstart[u];
         const uint32_t o = P.off[u] + (xl >> 5);
         const uint32_t bit = 1u << (xl & 31);
         if (!TFSM_IN(18, o, prm.words) || !TFSM_IN(44, depth, P.n) || !TFSM_IN(45, t.lo, (uint64_t)t.hi + 1) ||
-            !TFSM_IN(47, t.hi, g.m2 + 1) || !TFSM_IN(46, depth, kMaxN))
+            !TFSM_IN(47, t.hi, g.m2 + 1) || !TFSM_IN(46, depth, N))
             continue;
         bool searched = false;
         uint32_t added = 0;
-        if (!pattern_stops(ps, u, exact, lane) && !(warp_word(found + o, lane) & bit)) {
-            if ((int)lane < depth) S.emb[P.order[lane]] = t.prefix[lane];
-            __syncwarp();
+        if (!pattern_stops(T, ps, u, exact) && !(T.word(found + o) & bit)) {
+            for (int q = (int)T.lane; q < depth; q += G) S.emb[P.order[q]] = t.prefix[q];
+            T.sync();
             uint32_t steps = 0, bytes = 12;
             int adepth = 0;
             const Cancel cancel{found + o, bit, &ps, u, exact};
-            int r = dfs(g, P, S, dom, found, failed, lane, depth, true, t.lo, t.hi, budget, cancel, steps, adepth,
-                        bytes);
+            int r = dfs(T, g, P, S, dom, found, failed, depth, true, t.lo, t.hi, budget, cancel, steps, adepth, bytes);
             if (r == kAbort) {
-                added = emit_remainder(P, S, p, u, t.v, depth, adepth, t.group, prm.split_slice, out,
+                added = emit_remainder(T, P, S, p, u, t.v, depth, adepth, t.group, prm.split_slice, out,
                                        &counters[2 + round + 1], prm.split_cap, prm.split_cap - prm.split_slack,
-                                       prm.split_slack, lane, g.m2);
+                                       prm.split_slack, g.m2);
                 if (!added && prm.defer) {  // no room: v stays undecided for the next pass
-                    if (lane == 0) atomicAdd(&counters[kDeferred], 1u);
+                    if (T.lane == 0) atomicAdd(&counters[kDeferred], 1u);
                     r = kCancel;
                 } else if (!added) {  // no room, last pass: finish the task here
-                    r = dfs(g, P, S, dom, found, failed, lane, depth, true, t.lo, t.hi, 0, cancel, steps, adepth,
-                            bytes);
+                    r = dfs(T, g, P, S, dom, found, failed, depth, true, t.lo, t.hi, 0, cancel, steps, adepth, bytes);
                 }
             }
-            if (r == kFound) mark_found(P, S, ps, found, prm.tau, exact, lane);
-            const unsigned long long wb = __reduce_add_sync(0xffffffffu, bytes);
-            if (lane == 0) {
+            if (r == kFound) mark_found(T, P, S, ps, found, prm.tau, exact);
+            const unsigned long long wb = T.sum(bytes);
+            if (T.lane == 0) {
                 atomicAdd(&ps.steps, (unsigned long long)steps);
                 atomicAdd(&ps.bytes, wb);
                 atomicMax(&ps.max_steps, (unsigned long long)steps);
@@ -865,7 +920,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_split(Graph g, const PatD
             }
             searched = r != kCancel;
         }
-        if (lane == 0) {
+        if (T.lane == 0) {
             if (!searched && !(__ldcg(found + o) & bit)) atomicOr(&grp.incomplete, 1u);
             if (added) atomicAdd(&grp.pending, added);  // before this task's own completion below
             __threadfence();
@@ -891,7 +946,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_split(Graph g, const PatD
                 }
             }
         }
-        __syncwarp();
+        T.sync();
     }
 }
 
@@ -961,19 +1016,48 @@ cudaError_t launch_refine(const Graph &g, const PatDesc *descs, PatStatus *st, c
     return cudaGetLastError();
 }
 
+namespace {
+
+template <int G>
+cudaError_t launch_search_t(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchItem *items,
+                            const SearchParams &prm, uint32_t *counters, const uint32_t *dom, uint32_t *found,
+                            uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<G>, kSearchWarps * 32, 0);
+    if (per_sm <= 0) per_sm = 1;
+    uint64_t blocks = (uint64_t)num_sms() * (uint64_t)per_sm;
+    const uint64_t teams = (uint64_t)kSearchWarps * 32 / G;
+    const uint64_t need = (((uint64_t)prm.n_items << prm.parts_log2) + teams - 1) / teams;
+    if (blocks > need) blocks = need;
+    TFSM_LAUNCH(k_search<G>, (unsigned)blocks, kSearchWarps * 32, s, g, descs, st, items, prm, counters, dom, found,
+                failed, splits, groups);
+    return cudaGetLastError();
+}
+
+template <int G>
+cudaError_t launch_split_t(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchParams &prm,
+                           uint32_t *counters, int round, uint32_t budget, const uint32_t *dom, uint32_t *found,
+                           uint32_t *failed, const SplitTask *in, SplitTask *out, SplitGroup *groups,
+                           cudaStream_t s) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_split<G>, kSearchWarps * 32, 0);
+    if (per_sm <= 0) per_sm = 1;
+    TFSM_LAUNCH(k_split<G>, (unsigned)(num_sms() * per_sm), kSearchWarps * 32, s, g, descs, st, prm, counters, round,
+                budget, dom, found, failed, in, out, groups);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
 cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchItem *items,
                           const SearchParams &prm, uint32_t *counters, const uint32_t *dom, uint32_t *found,
                           uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s) {
     if (prm.n_items == 0) return cudaSuccess;
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search, kSearchWarps * 32, 0);
-    if (per_sm <= 0) per_sm = 1;
-    uint64_t blocks = (uint64_t)num_sms() * (uint64_t)per_sm;
-    const uint64_t need = (((uint64_t)prm.n_items << prm.parts_log2) + kSearchWarps - 1) / kSearchWarps;
-    if (blocks > need) blocks = need;
-    TFSM_LAUNCH(k_search, (unsigned)blocks, kSearchWarps * 32, s, g, descs, st, items, prm, counters, dom, found,
-                failed, splits, groups);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e;
+    if (prm.team_lanes == 8) e = launch_search_t<8>(g, descs, st, items, prm, counters, dom, found, failed, splits, groups, s);
+    else if (prm.team_lanes == 32)
+        e = launch_search_t<32>(g, descs, st, items, prm, counters, dom, found, failed, splits, groups, s);
+    else return cudaErrorInvalidValue;
 #ifdef TFSM_BOUNDS_CHECK
     if (e == cudaSuccess && cudaStreamSynchronize(s) != cudaSuccess) {
         std::fprintf(stderr, "tfsm checked build: fault in k_search\n");
@@ -985,7 +1069,7 @@ cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, c
 
 uint32_t resident_search_warps() {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search, kSearchWarps * 32, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<32>, kSearchWarps * 32, 0);
     if (per_sm <= 0) per_sm = 1;
     return (uint32_t)(num_sms() * per_sm * kSearchWarps);
 }
@@ -994,15 +1078,15 @@ cudaError_t launch_split_round(const Graph &g, const PatDesc *descs, PatStatus *
                                uint32_t *counters, int round, uint32_t budget, const uint32_t *dom, uint32_t *found,
                                uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s) {
     if (round < 0 || round >= kMaxRounds) return cudaErrorInvalidValue;
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_split, kSearchWarps * 32, 0);
-    if (per_sm <= 0) per_sm = 1;
     const SplitTask *in = splits + (size_t)(round % 2) * prm.split_cap;
     SplitTask *out = splits + (size_t)((round + 1) % 2) * prm.split_cap;
     if (round + 1 == kMaxRounds) budget = 0;  // the last possible round completes every task
-    TFSM_LAUNCH(k_split, (unsigned)(num_sms() * per_sm), kSearchWarps * 32, s, g, descs, st, prm, counters, round,
-                budget, dom, found, failed, in, out, groups);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e;
+    if (prm.team_lanes == 8)
+        e = launch_split_t<8>(g, descs, st, prm, counters, round, budget, dom, found, failed, in, out, groups, s);
+    else if (prm.team_lanes == 32)
+        e = launch_split_t<32>(g, descs, st, prm, counters, round, budget, dom, found, failed, in, out, groups, s);
+    else return cudaErrorInvalidValue;
 #ifdef TFSM_BOUNDS_CHECK
     if (e == cudaSuccess && cudaStreamSynchronize(s) != cudaSuccess) {
         std::fprintf(stderr, "tfsm checked build: fault in k_split\n");

@@ -731,6 +731,18 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     // the rest.
     size_t n_items = 0;  // search items, written into the pinned staging buffer I.hitems
     uint32_t parts_log2 = 0;
+    // lanes per search: teams of 8 when asked for, when the call has several patterns to search
+    // (single-pattern calls measured faster with whole warps) and every one fits a team's state
+    uint32_t team_lanes = 32;
+    if (opt.search_lanes == 8) {
+        int max_n = 0, searched = 0;
+        for (size_t p = 0; p < P; ++p)
+            if (need_search[p]) {
+                max_n = std::max(max_n, L.hdescs[p].n);
+                ++searched;
+            }
+        if (max_n <= 8 && searched > 1) team_lanes = 8;
+    }
     {
         struct Q {
             uint32_t p, u, w, words;
@@ -756,7 +768,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         uint64_t n_plain = 0;
         for (auto &qs : ranks)
             for (Q &q : qs) n_plain += (q.words + cw - 1) / cw;
-        const uint64_t want = 4ull * (uint64_t)dev::resident_search_warps();
+        const uint64_t want = 4ull * (uint64_t)dev::resident_search_warps() * (32u / team_lanes);
         while (parts_log2 < 5 && (n_plain << parts_log2) < want) ++parts_log2;
         I.hitems.ensure((size_t)n_plain);
         dev::SearchItem *out = I.hitems.p;
@@ -795,6 +807,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     prm.group_cap = (uint32_t)I.groups.n;
     prm.round_budget = std::max<uint32_t>(1, opt.round_budget);
     prm.parts_log2 = parts_log2;
+    prm.team_lanes = team_lanes;
     prm.defer = 0;
     prm.n_pats = (uint32_t)P;
     prm.words = total;

@@ -39,6 +39,8 @@ struct EngineOptions {
     uint32_t round_budget = 32;        // step budget of a split task (the 64th round has none)
     uint32_t split_rounds = 2;         // split rounds launched without checking for remaining tasks
     uint32_t chunk_words = 1;          // bitmap words per search work item (x32 candidates)
+    uint32_t search_lanes = 8;         // lanes per search: 32, or 8 (four searches per warp, used for
+                                       //   calls with several patterns of at most 8 vertices)
     uint32_t refine_rounds = 1;        // arc-consistency passes for patterns that need search
     uint32_t max_batch = 4096;         // miner: patterns per engine call
     double time_limit_s = 0;           // miner: stop between engine calls after this long (0: none)

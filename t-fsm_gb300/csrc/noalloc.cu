@@ -316,6 +316,7 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     prm.exact = exact ? 1 : 0;
     prm.n_items = (uint32_t)n_items;
     prm.step_budget = 0;  // no hub splitting on this path
+    prm.team_lanes = 32;
     prm.split_slice = 32;
     prm.n_pats = 1;
     prm.words = words;

@@ -7,7 +7,8 @@
 // __shfl_sync, __shfl_xor_sync, __reduce_add_sync) are rendezvous on a std::barrier, which also
 // orders memory like bar.warp.sync.  __shared__ variables become static storage (one block at a
 // time).  Atomics are GCC __atomic builtins; __ldcg is a relaxed atomic load.  Device memory is
-// host memory.  Only full-warp masks are supported (the kernels use nothing else).
+// host memory.  Masks: the full warp, or an aligned group of 8 or 16 lanes (a team of lanes that
+// runs its own search); each group has its own rendezvous, so groups of a warp proceed independently.
 #pragma once
 
 #include <algorithm>
@@ -46,13 +47,14 @@ struct Barrier {
     std::atomic<unsigned> arrived{0};
     std::atomic<unsigned long long> generation{0};
     std::atomic<int> line[32];
+    unsigned count = 32;  // lanes that meet here
     Barrier() {
         for (auto &l : line) l.store(0);
     }
     void arrive_and_wait(unsigned lane, int at) {
         line[lane].store(at, std::memory_order_relaxed);
         const unsigned long long gen = generation.load(std::memory_order_acquire);
-        if (arrived.fetch_add(1, std::memory_order_acq_rel) == 31) {
+        if (arrived.fetch_add(1, std::memory_order_acq_rel) == count - 1) {
             arrived.store(0, std::memory_order_relaxed);
             generation.fetch_add(1, std::memory_order_acq_rel);
             return;
@@ -76,7 +78,22 @@ struct Barrier {
 
 struct Warp {
     Barrier bar;
+    Barrier g8[4], g16[2];  // aligned lane groups
     uint64_t vals[32];
+    Warp() {
+        for (auto &b : g8) b.count = 8;
+        for (auto &b : g16) b.count = 16;
+    }
+    Barrier &of(unsigned mask) {
+        if (mask == 0xffffffffu) return bar;
+        const unsigned base = (unsigned)__builtin_ctz(mask), size = (unsigned)__builtin_popcount(mask);
+        const bool aligned = (size == 8 || size == 16) && base % size == 0 && mask == (((1u << size) - 1) << base);
+        if (!aligned) {
+            std::fprintf(stderr, "emulation: unsupported collective mask %08x\n", mask);
+            std::abort();
+        }
+        return size == 8 ? g8[base / 8] : g16[base / 16];
+    }
 };
 
 inline thread_local dim3 tl_threadIdx, tl_blockIdx;
@@ -162,14 +179,16 @@ void launch(unsigned grid, unsigned block, F &&fn) {
 
 inline unsigned lane() { return tl_threadIdx.x & 31; }
 
-// all 32 lanes publish a value, then read the published values
+// the lanes of `mask` publish a value, then read the published values
 template <class R>
-R collective(uint64_t mine, R (*combine)(const uint64_t *, unsigned, uint64_t), uint64_t arg, int at) {
+R collective(unsigned mask, uint64_t mine, R (*combine)(const uint64_t *, unsigned, unsigned, uint64_t), uint64_t arg,
+             int at) {
     Warp &w = *tl_warp;
+    Barrier &b = w.of(mask);
     w.vals[lane()] = mine;
-    w.bar.arrive_and_wait(lane(), at);
-    R r = combine(w.vals, lane(), arg);
-    w.bar.arrive_and_wait(lane(), -at);
+    b.arrive_and_wait(lane(), at);
+    R r = combine(w.vals, lane(), mask, arg);
+    b.arrive_and_wait(lane(), -at);
     return r;
 }
 
@@ -180,17 +199,17 @@ R collective(uint64_t mine, R (*combine)(const uint64_t *, unsigned, uint64_t), 
 #define blockDim (tfsm_emu::g_blockDim)
 #define gridDim (tfsm_emu::g_gridDim)
 
-inline void __syncwarp(unsigned = 0xffffffffu, int at = __builtin_LINE()) {
-    tfsm_emu::tl_warp->bar.arrive_and_wait(tfsm_emu::lane(), at);
+inline void __syncwarp(unsigned mask = 0xffffffffu, int at = __builtin_LINE()) {
+    tfsm_emu::tl_warp->of(mask).arrive_and_wait(tfsm_emu::lane(), at);
 }
 
-inline unsigned __ballot_sync(unsigned, int pred, int at = __builtin_LINE()) {
+inline unsigned __ballot_sync(unsigned mask, int pred, int at = __builtin_LINE()) {
     return tfsm_emu::collective<unsigned>(
-        pred ? 1u : 0u,
-        [](const uint64_t *v, unsigned, uint64_t) -> unsigned {
+        mask, pred ? 1u : 0u,
+        [](const uint64_t *v, unsigned, unsigned m, uint64_t) -> unsigned {
             unsigned r = 0;
             for (unsigned l = 0; l < 32; ++l)
-                if (v[l]) r |= 1u << l;
+                if (((m >> l) & 1u) && v[l]) r |= 1u << l;
             return r;
         },
         0, at);
@@ -198,36 +217,49 @@ inline unsigned __ballot_sync(unsigned, int pred, int at = __builtin_LINE()) {
 
 inline int __any_sync(unsigned m, int pred, int at = __builtin_LINE()) { return __ballot_sync(m, pred, at) != 0; }
 
+// Source lanes follow CUDA: `src` (or lane ^ laneMask) inside the caller's segment of `width`
+// lanes.  The argument packs (width << 8 | src).
 template <class T>
-T __shfl_sync(unsigned, T v, int src, int at = __builtin_LINE()) {
+T __shfl_sync(unsigned mask, T v, int src, int width = 32, int at = __builtin_LINE()) {
     static_assert(sizeof(T) <= 8, "shuffle of at most 8 bytes");
     uint64_t bits = 0;
     std::memcpy(&bits, &v, sizeof(T));
     const uint64_t got = tfsm_emu::collective<uint64_t>(
-        bits, [](const uint64_t *vals, unsigned, uint64_t s) -> uint64_t { return vals[s & 31]; }, (uint64_t)src, at);
+        mask, bits,
+        [](const uint64_t *vals, unsigned ln, unsigned, uint64_t a) -> uint64_t {
+            const unsigned w = (unsigned)(a >> 8), s = (unsigned)(a & 0xff);
+            return vals[(ln & ~(w - 1)) + (s & (w - 1))];
+        },
+        ((uint64_t)width << 8) | (uint64_t)(src & 0xff), at);
     T r;
     std::memcpy(&r, &got, sizeof(T));
     return r;
 }
 
 template <class T>
-T __shfl_xor_sync(unsigned, T v, int mask, int at = __builtin_LINE()) {
+T __shfl_xor_sync(unsigned mask, T v, int lane_mask, int width = 32, int at = __builtin_LINE()) {
     uint64_t bits = 0;
     std::memcpy(&bits, &v, sizeof(T));
     const uint64_t got = tfsm_emu::collective<uint64_t>(
-        bits, [](const uint64_t *vals, unsigned ln, uint64_t m) -> uint64_t { return vals[(ln ^ m) & 31]; },
-        (uint64_t)mask, at);
+        mask, bits,
+        [](const uint64_t *vals, unsigned ln, unsigned, uint64_t a) -> uint64_t {
+            const unsigned w = (unsigned)(a >> 8), m = (unsigned)(a & 0xff);
+            const unsigned t = ln ^ m;
+            return vals[((t & ~(w - 1)) == (ln & ~(w - 1))) ? t : ln];
+        },
+        ((uint64_t)width << 8) | (uint64_t)(lane_mask & 0xff), at);
     T r;
     std::memcpy(&r, &got, sizeof(T));
     return r;
 }
 
-inline unsigned __reduce_add_sync(unsigned, unsigned v, int at = __builtin_LINE()) {
+inline unsigned __reduce_add_sync(unsigned mask, unsigned v, int at = __builtin_LINE()) {
     return tfsm_emu::collective<unsigned>(
-        v,
-        [](const uint64_t *vals, unsigned, uint64_t) -> unsigned {
+        mask, v,
+        [](const uint64_t *vals, unsigned, unsigned m, uint64_t) -> unsigned {
             unsigned s = 0;
-            for (unsigned l = 0; l < 32; ++l) s += (unsigned)vals[l];
+            for (unsigned l = 0; l < 32; ++l)
+                if ((m >> l) & 1u) s += (unsigned)vals[l];
             return s;
         },
         0, at);

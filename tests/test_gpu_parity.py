@@ -237,3 +237,26 @@ def test_subpattern_pruning_keeps_results(tfsm, graphs, case, tmp_path):
     assert sb["pruned"] == 0
     if case in ("cfg1", "cfg2_t9000"):
         assert sa["pruned"] > 0
+
+
+@pytest.mark.parametrize("case", ["cfg1", "el3", "clique", "quirk_elabels", "cfg2_t9000"])
+@pytest.mark.parametrize("lanes", [8, 32])
+def test_team_sizes_keep_results(tfsm, graphs, case, lanes, tmp_path):
+    """Searches run by teams of 8 lanes (four per warp) or by whole warps: the same pattern sets and
+    exact supports."""
+    g = graphs(case)
+    saved = g.options()
+    try:
+        g.set_options(search_lanes=lanes)
+        pats, _ = mine_set(tfsm, g, case, tmp_path)
+        assert pats == golden_pattern_set(case)
+        g.set_options(search_lanes=lanes, step_budget=1, split_slice=32, round_budget=1)
+        pats, _ = mine_set(tfsm, g, case, tmp_path)
+        assert pats == golden_pattern_set(case)
+        want = golden_mni(case)
+        if want:
+            keys = list(want)[:300]
+            res = g.evaluate([tfsm.parse_key(k) for k in keys], flags=tfsm.FLAG_EXACT)
+            assert [r.mni for r in res] == [want[k] for k in keys]
+    finally:
+        g.set_options(**saved)

@@ -30,7 +30,10 @@ def emu():
 OPTS = {"default": [], "split": ["-step-budget", "1", "-split-slice", "32", "-chunk-words", "1", "-round-budget", "1"],
         "split1": ["-step-budget", "2", "-split-slice", "32", "-split-rounds", "1", "-round-budget", "1000000"],
         "plain": ["-plain", "-refine-rounds", "1"], "exact": ["-exact"], "batch3": ["-max-batch", "3"],
-        "random_orders": ["-random-orders", "7", "-step-budget", "2"]}
+        "random_orders": ["-random-orders", "7", "-step-budget", "2"],
+        "lanes8": ["-search-lanes", "8"],
+        "lanes8_split": ["-search-lanes", "8", "-step-budget", "1", "-split-slice", "32", "-round-budget", "1"],
+        "lanes8_exact": ["-search-lanes", "8", "-exact"]}
 # (the quirk case's many-call variants are the slowest to emulate; its other variants cover it)
 RUNS = [(c, o) for c in SMALL for o in OPTS if not (o in ("plain", "batch3") and c == "quirk_elabels")]
 RUNS += [(c, "tiny_buffers") for c in ("clique", "star_hub")]
