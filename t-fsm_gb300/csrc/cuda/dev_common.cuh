@@ -35,6 +35,8 @@ struct Graph {
 };
 
 // One pattern of a batch.  Plain old data, copied to the device once per batch.
+constexpr int kMaxPush = 4;  // sub-patterns besides the parent whose domains bound a child's
+
 struct PatDesc {
     int32_t n;
     int32_t n_reps;                     // orbit representatives that get search tasks
@@ -50,6 +52,8 @@ struct PatDesc {
     uint32_t words[kMaxN];              // bitmap words of u = ceil(lsize / 32)
     uint64_t off[kMaxN];                // word offset of u's bitmaps in the level pools
     int64_t parent_off[kMaxN];          // word offset of the parent's bitmaps for u, or -1
+    int64_t push_off[kMaxPush][kMaxN];  // further sub-patterns (one edge less) of the same previous
+                                        //   level: word offset of their bitmaps for u's image, or -1
     int32_t nlf_n[kMaxN];               // neighbour-label-frequency requirements of u
     uint8_t nlf_lab[kMaxN][kMaxN];
     uint8_t nlf_cnt[kMaxN][kMaxN];

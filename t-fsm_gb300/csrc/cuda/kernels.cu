@@ -130,6 +130,14 @@ __global__ void __launch_bounds__(256) k_domain_init(Graph g, const PatDesc *__r
             const uint32_t pw = __ldg(pdom + poff + word) & ~__ldg(pfailed + poff + word);
             pass = pass && ((pw >> lane) & 1u);
         }
+        // push-down: every other one-edge-smaller sub-pattern's final domain bounds u's as well
+        // (an embedding of the child restricts to one of the sub-pattern)
+        for (int k = 0; k < kMaxPush && pdom != nullptr; ++k) {
+            const int64_t so = D.push_off[k][u];
+            if (so < 0 || !TFSM_IN(39, (uint64_t)so + word, chk_pwords)) continue;
+            const uint32_t sw = __ldg(pdom + so + word) & ~__ldg(pfailed + so + word);
+            pass = pass && ((sw >> lane) & 1u);
+        }
         if (__any_sync(0xffffffffu, pass)) {
             const uint32_t x = D.lstart[u] + xl;
             uint32_t b = 0, e = 0;

@@ -426,7 +426,8 @@ void gql_plan(const Pattern &pat, const uint32_t *dsize, int start, uint8_t *ord
 }  // namespace
 
 void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::vector<int> &parent, const Level *prev,
-                         uint32_t tau, const EngineOptions &opt, Level &out, std::vector<EvalResult> &res) {
+                         uint32_t tau, const EngineOptions &opt, Level &out, std::vector<EvalResult> &res,
+                         const std::vector<std::vector<PushSource>> *push) {
     Impl &I = *impl_;
     struct WallClock {  // host wall time of the whole call, every return path
         double &acc;
@@ -488,6 +489,25 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
             if (prev && parent[p] >= 0) {
                 const PatDesc &PD = prev->impl->hdescs[(size_t)parent[p]];
                 if (u < PD.n) D.parent_off[u] = (int64_t)PD.off[u];
+            }
+        }
+        static_assert(kMaxPushSources == dev::kMaxPush, "push-down sources");
+        for (int k = 0; k < dev::kMaxPush; ++k)
+            for (int u = 0; u < dev::kMaxN; ++u) D.push_off[k][u] = -1;
+        if (prev && push && p < push->size()) {
+            int k = 0;
+            for (const PushSource &src : (*push)[p]) {
+                if (k == dev::kMaxPush) break;
+                if (src.idx < 0 || (size_t)src.idx >= prev->impl->hdescs.size()) continue;
+                const PatDesc &SD = prev->impl->hdescs[(size_t)src.idx];
+                bool any = false;
+                for (int u = 0; u < n; ++u) {
+                    const int s = src.vertex[u];
+                    if (s < 0 || s >= SD.n || SD.lab[s] != D.lab[u]) continue;  // same label: same word range
+                    D.push_off[k][u] = (int64_t)SD.off[s];
+                    any = true;
+                }
+                k += any ? 1 : 0;
             }
         }
         const std::vector<int> orb = automorphism_orbits(pat);

@@ -83,6 +83,14 @@ struct Level {
     size_t size() const;  // patterns in the batch
 };
 
+// A sub-pattern of a candidate with one edge less, evaluated in the previous level (push-down
+// pruning: its final domains bound the candidate's).  At most kMaxPushSources per candidate.
+constexpr int kMaxPushSources = 4;
+struct PushSource {
+    int idx;            // its index in the previous level
+    int8_t vertex[16];  // per candidate vertex: the sub-pattern vertex it maps to, or -1
+};
+
 class GpuEngine {
 public:
     GpuEngine(const LgGraph &g, int device = 0);
@@ -93,7 +101,8 @@ public:
     // Evaluate `pats` against the graph.  parent[i] indexes the pattern's parent in `prev`
     // (or -1).  `out` receives this batch's device memory for the next level.
     void evaluate(const std::vector<const Pattern *> &pats, const std::vector<int> &parent, const Level *prev,
-                  uint32_t tau, const EngineOptions &opt, Level &out, std::vector<EvalResult> &res);
+                  uint32_t tau, const EngineOptions &opt, Level &out, std::vector<EvalResult> &res,
+                  const std::vector<std::vector<PushSource>> *push = nullptr);
 
     const KernelTimes &times() const { return times_; }
     void reset_times() { times_ = KernelTimes(); }

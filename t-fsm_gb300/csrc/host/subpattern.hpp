@@ -30,8 +30,10 @@ struct SmallGraph {
     std::vector<std::array<int, 3>> edges;  // (a, b, edge label)
 };
 
-// Isomorphism-invariant key (bytes of int32 values).
-inline std::string canonical_key(const SmallGraph &g) {
+// Isomorphism-invariant key (bytes of int32 values).  With `order`, also the vertex at each
+// position of the canonical form: for two isomorphic graphs, order_a[i] <-> order_b[i] is an
+// isomorphism.
+inline std::string canonical_key(const SmallGraph &g, std::vector<int> *order_out = nullptr) {
     const int n = (int)g.label.size();
     std::vector<std::vector<int>> inv((size_t)n);
     for (int v = 0; v < n; ++v) inv[(size_t)v] = {g.label[(size_t)v], 0};
@@ -76,6 +78,7 @@ inline std::string canonical_key(const SmallGraph &g) {
         if (!have || cur < best) {
             best = cur;
             have = true;
+            if (order_out) *order_out = order;
         }
         // next ordering: odometer over the classes' permutations
         size_t k = 0;
@@ -101,10 +104,17 @@ inline SmallGraph small_graph(const Pattern &p) {
     return g;
 }
 
-// Keys of P's connected sub-patterns with one edge less (an edge to a degree-1 vertex goes with
-// that vertex; an edge whose removal disconnects the rest gives no connected sub-pattern).
-inline void one_edge_smaller_keys(const Pattern &p, std::vector<std::string> &keys) {
-    keys.clear();
+// A connected sub-pattern of P with one edge less: its key and, for every vertex of P, the
+// position of its image in the sub-pattern's canonical order (-1 for the dropped vertex).
+struct SubPattern {
+    std::string key;
+    std::vector<int> pos_of;  // by P vertex
+};
+
+// P's connected sub-patterns with one edge less (an edge to a degree-1 vertex goes with that
+// vertex; an edge whose removal disconnects the rest gives no connected sub-pattern).
+inline void one_edge_smaller(const Pattern &p, std::vector<SubPattern> &subs) {
+    subs.clear();
     const SmallGraph g = small_graph(p);
     const int n = (int)g.label.size(), m = (int)g.edges.size();
     if (m < 2) return;
@@ -140,8 +150,24 @@ inline void one_edge_smaller_keys(const Pattern &p, std::vector<std::string> &ke
         for (auto &e : s.edges) comp[(size_t)find(e[0])] = find(e[1]);
         bool connected = true;
         for (int v = 1; v < ns && connected; ++v) connected = find(v) == find(0);
-        if (connected) keys.push_back(canonical_key(s));
+        if (!connected) continue;
+        SubPattern sp;
+        std::vector<int> order;
+        sp.key = canonical_key(s, &order);
+        std::vector<int> pos_in_s((size_t)ns);
+        for (int i = 0; i < ns; ++i) pos_in_s[(size_t)order[(size_t)i]] = i;
+        sp.pos_of.assign((size_t)n, -1);
+        for (int v = 0; v < n; ++v)
+            if (remap[(size_t)v] >= 0) sp.pos_of[(size_t)v] = pos_in_s[(size_t)remap[(size_t)v]];
+        subs.push_back(std::move(sp));
     }
+}
+
+inline void one_edge_smaller_keys(const Pattern &p, std::vector<std::string> &keys) {
+    std::vector<SubPattern> subs;
+    one_edge_smaller(p, subs);
+    keys.clear();
+    for (auto &s : subs) keys.push_back(std::move(s.key));
 }
 
 }  // namespace tfsm

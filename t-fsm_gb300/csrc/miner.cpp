@@ -11,6 +11,7 @@
 #include <memory>
 #include <mutex>
 #include <thread>
+#include <unordered_map>
 #include <unordered_set>
 
 #include "host/lg_fast.hpp"
@@ -24,6 +25,7 @@ struct Node {
     Pattern pat;
     EvalResult res;
     bool pruned = false;   // a sub-pattern with one edge less is infrequent: decided without search
+    std::vector<PushSource> push;  // frequent sub-patterns with one edge less, in the parent's level
     Level *lvl = nullptr;  // device memory holding this pattern's final domains
     int idx = 0;           // index inside lvl
 };
@@ -146,7 +148,9 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                 std::vector<EvalResult> res;
                 const KernelTimes before = eng.times();
                 const double search_before = before.search_ms;
-                eng.evaluate(pats, par, prev, tau, eo, *cur_levels.back(), res);
+                std::vector<std::vector<PushSource>> pushes;
+                for (size_t kk = b0; kk < b1; ++kk) pushes.push_back(nodes[todo[kk]].push);
+                eng.evaluate(pats, par, prev, tau, eo, *cur_levels.back(), res, &pushes);
                 st.engine_calls++;
                 st.evaluations += b1 - b0;
                 if (verbose) {
@@ -206,7 +210,8 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                 }
                 cur_levels.emplace_back(new Level);
                 std::vector<EvalResult> res;
-                eng.evaluate(pats, par, prev, tau, eo, *cur_levels.back(), res);
+                const std::vector<std::vector<PushSource>> pushes{nodes[i].push};
+                eng.evaluate(pats, par, prev, tau, eo, *cur_levels.back(), res, &pushes);
                 st.engine_calls++;
                 nodes[i].res = std::move(res[0]);
                 nodes[i].lvl = cur_levels.back().get();
@@ -251,31 +256,55 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                 next.push_back(std::move(nd));
                 parent_of.push_back((int)i);
             }
-        if (prune_subpatterns && !next.empty()) {
-            // keys of this level's frequent patterns, then the one-edge-smaller sub-patterns of
-            // every child (both on the host pool)
-            std::vector<std::string> fkeys(level.size());
+        if (opt.subpattern_pruning && !next.empty()) {
+            // Keys (and canonical vertex orders) of this level's evaluated patterns; then, for every
+            // child, its one-edge-smaller sub-patterns:
+            //   * one evaluated and infrequent: the child is infrequent (MNI is anti-monotone);
+            //   * one missing from a complete level (single edge label): infrequent as well;
+            //   * the frequent ones held by the parent's device level bound the child's domains.
+            std::vector<std::string> keys(level.size());
+            std::vector<std::vector<int>> orders(level.size());
             {
                 std::atomic<size_t> k(0);
                 const std::function<void()> work = [&]() {
                     for (size_t i; (i = k.fetch_add(1)) < level.size();)
-                        if (level[i].res.frequent) fkeys[i] = canonical_key(small_graph(level[i].pat));
+                        if (!level[i].pruned) keys[i] = canonical_key(small_graph(level[i].pat), &orders[i]);
                 };
                 pool.run(work);
             }
-            std::unordered_set<std::string> freq;
+            std::unordered_map<std::string, size_t> evaluated;
             for (size_t i = 0; i < level.size(); ++i)
-                if (level[i].res.frequent) freq.insert(std::move(fkeys[i]));
+                if (!level[i].pruned) evaluated.emplace(keys[i], i);
             std::atomic<size_t> k(0);
             const std::function<void()> work = [&]() {
-                std::vector<std::string> keys;
+                std::vector<SubPattern> subs;
                 for (size_t i; (i = k.fetch_add(1)) < next.size();) {
-                    one_edge_smaller_keys(next[i].pat, keys);
-                    for (auto &key : keys)
-                        if (!freq.count(key)) {
-                            next[i].pruned = true;
+                    Node &child = next[i];
+                    const Node &par = level[(size_t)parent_of[i]];
+                    one_edge_smaller(child.pat, subs);
+                    for (auto &sp : subs) {
+                        auto it = evaluated.find(sp.key);
+                        if (it == evaluated.end()) {
+                            if (prune_subpatterns) child.pruned = true;
+                            if (child.pruned) break;
+                            continue;
+                        }
+                        const Node &sn = level[it->second];
+                        if (!sn.res.frequent) {
+                            child.pruned = true;
                             break;
                         }
+                        if (sn.lvl != par.lvl || it->second == (size_t)parent_of[i] || !sn.lvl) continue;
+                        if (child.push.size() >= (size_t)kMaxPushSources) continue;
+                        PushSource src;
+                        src.idx = sn.idx;
+                        for (int u = 0; u < 16; ++u) src.vertex[u] = -1;
+                        const std::vector<int> &ord = orders[it->second];
+                        for (int u = 0; u < child.pat.size() && u < 16; ++u)
+                            if (sp.pos_of[(size_t)u] >= 0) src.vertex[u] = (int8_t)ord[(size_t)sp.pos_of[(size_t)u]];
+                        child.push.push_back(src);
+                    }
+                    if (child.pruned) child.push.clear();
                 }
             };
             pool.run(work);

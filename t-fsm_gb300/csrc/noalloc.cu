@@ -149,6 +149,8 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     // ---- descriptor ----
     PatDesc D;
     std::memset(&D, 0, sizeof(D));
+    for (int k = 0; k < dev::kMaxPush; ++k)  // no previous level on this path: no push-down sources
+        for (int u = 0; u < dev::kMaxN; ++u) D.push_off[k][u] = -1;
     std::memset(D.el, dev::kNoEdge, sizeof(D.el));
     D.n = n;
     D.n_reps = n;
