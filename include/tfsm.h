@@ -146,6 +146,13 @@ typedef struct {
                                again (>= 1) */
     uint32_t search_lanes;  /* lanes per search: 8 (default: four searches per warp, for calls with
                                several patterns of at most 8 vertices) or 32; 0 means 32 */
+    uint32_t rank_window;   /* patterns per window of the search order: within a window every
+                               pattern's vertex with the smallest domain is searched first, then
+                               the next one; windows follow one another (0: one window per call) */
+    double call_ms;         /* tfsm_mine: an engine call that takes longer than this many milliseconds
+                               makes the following calls take proportionally fewer patterns (at
+                               least 4); full calls that finish sooner double it again, up to
+                               max_batch (default 2; 0: always max_batch) */
 } tfsm_options;
 
 int tfsm_get_options(const tfsm_graph *g, tfsm_options *opt);

@@ -115,11 +115,11 @@ void fill_result(const tfsm::EvalResult &r, int n, tfsm_result *out) {
 
 const char *const kKnobRules =
     "split_slice must be >= 32; chunk_words, refine_rounds, max_batch and round_budget >= 1; split_rounds in 1..64; "
-    "time_limit_s >= 0; search_lanes 8 or 32";
+    "time_limit_s and call_ms >= 0; search_lanes 8 or 32";
 
 bool knobs_valid(const tfsm_options &o) {
     return o.split_slice >= 32 && o.chunk_words >= 1 && o.refine_rounds >= 1 && o.max_batch >= 1 &&
-           o.split_rounds >= 1 && o.split_rounds <= 64 && o.round_budget >= 1 && o.time_limit_s >= 0 &&
+           o.split_rounds >= 1 && o.split_rounds <= 64 && o.round_budget >= 1 && o.time_limit_s >= 0 && o.call_ms >= 0 &&
            (o.search_lanes == 0 || o.search_lanes == 8 || o.search_lanes == 32);
 }
 
@@ -133,6 +133,8 @@ void apply_knobs(const tfsm_options &o, tfsm::EngineOptions &e) {
     e.split_rounds = o.split_rounds;
     e.round_budget = o.round_budget;
     e.search_lanes = o.search_lanes == 0 ? 32 : o.search_lanes;
+    e.rank_window = o.rank_window;
+    e.call_ms = o.call_ms;
 }
 
 tfsm::EngineOptions engine_options(const tfsm_graph *g, uint32_t flags) {
@@ -322,6 +324,8 @@ int tfsm_get_options(const tfsm_graph *g, tfsm_options *o) {
         o->time_limit_s = g->opt.time_limit_s;
         o->round_budget = g->opt.round_budget;
         o->search_lanes = g->opt.search_lanes;
+        o->rank_window = g->opt.rank_window;
+        o->call_ms = g->opt.call_ms;
         return TFSM_OK;
     });
 }

@@ -764,49 +764,65 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         if (max_n <= 8 && searched > 1) team_lanes = 8;
     }
     {
+        // The search kernel claims items in order, so the order is the order in time.  With one
+        // vertex-major order over a call of hundreds of patterns, a pattern's second vertex waits
+        // until the first vertex of every pattern has been searched, although it is often the one
+        // that shows the pattern infrequent and would have cut the first vertex's failing
+        // searches: windows of `rank_window` patterns bound that wait (vertex-major inside each).
         struct Q {
             uint32_t p, u, w, words;
         };
-        std::vector<std::vector<Q>> ranks;  // ranks[k]: the k-th smallest representative of each pattern
-        for (size_t p = 0; p < P; ++p) {
-            if (!need_search[p]) continue;
-            const PatDesc &D = L.hdescs[p];
-            std::vector<int> reps;
-            for (int u = 0; u < D.n; ++u)
-                if (D.rep[u] == u) reps.push_back(u);
-            const PatStatus &s = I.hstatus[p];
-            std::stable_sort(reps.begin(), reps.end(), [&](int a, int b) { return s.dom_size[a] < s.dom_size[b]; });
-            for (size_t k = 0; k < reps.size(); ++k) {
-                if (ranks.size() <= k) ranks.emplace_back();
-                ranks[k].push_back({(uint32_t)p, (uint32_t)reps[k], 0, D.words[reps[k]]});
-            }
-        }
+        std::vector<uint32_t> searched;
+        for (size_t p = 0; p < P; ++p)
+            if (need_search[p]) searched.push_back((uint32_t)p);
         const uint32_t cw = std::max<uint32_t>(1, opt.chunk_words);
         // Calls with few words (a level of a few patterns) split every item into interleaved parts
         // of its 32 candidates, so that enough warps search in parallel: about four items per
         // resident warp of the search kernel (152 SMs x 40 warps on GB300).
         uint64_t n_plain = 0;
-        for (auto &qs : ranks)
-            for (Q &q : qs) n_plain += (q.words + cw - 1) / cw;
+        for (uint32_t p : searched) {
+            const PatDesc &D = L.hdescs[p];
+            for (int u = 0; u < D.n; ++u)
+                if (D.rep[u] == u) n_plain += (D.words[u] + cw - 1) / cw;
+        }
         const uint64_t want = 4ull * (uint64_t)dev::resident_search_warps() * (32u / team_lanes);
         while (parts_log2 < 5 && (n_plain << parts_log2) < want) ++parts_log2;
         I.hitems.ensure((size_t)n_plain);
         dev::SearchItem *out = I.hitems.p;
-        for (auto &qs : ranks) {
-            bool more = true;
-            while (more) {
-                more = false;
-                for (Q &q : qs) {
-                    if (q.w >= q.words) continue;
-                    dev::SearchItem it;
-                    it.pat = q.p;
-                    it.u = (uint16_t)q.u;
-                    it.pad = 0;
-                    it.word_lo = q.w;
-                    it.word_hi = std::min(q.words, q.w + cw);
-                    q.w = it.word_hi;
-                    out[n_items++] = it;
-                    more = true;
+        const size_t win = opt.rank_window ? opt.rank_window : std::max<size_t>(1, searched.size());
+        std::vector<std::vector<Q>> ranks;  // ranks[k]: the k-th smallest representative of each pattern
+        for (size_t a = 0; a < searched.size(); a += win) {
+            for (auto &r : ranks) r.clear();
+            for (size_t i = a; i < std::min(searched.size(), a + win); ++i) {
+                const uint32_t p = searched[i];
+                const PatDesc &D = L.hdescs[p];
+                std::vector<int> reps;
+                for (int u = 0; u < D.n; ++u)
+                    if (D.rep[u] == u) reps.push_back(u);
+                const PatStatus &s = I.hstatus[p];
+                std::stable_sort(reps.begin(), reps.end(),
+                                 [&](int x, int y) { return s.dom_size[x] < s.dom_size[y]; });
+                for (size_t k = 0; k < reps.size(); ++k) {
+                    if (ranks.size() <= k) ranks.emplace_back();
+                    ranks[k].push_back({p, (uint32_t)reps[k], 0, D.words[reps[k]]});
+                }
+            }
+            for (auto &qs : ranks) {
+                bool more = true;
+                while (more) {
+                    more = false;
+                    for (Q &q : qs) {
+                        if (q.w >= q.words) continue;
+                        dev::SearchItem it;
+                        it.pat = q.p;
+                        it.u = (uint16_t)q.u;
+                        it.pad = 0;
+                        it.word_lo = q.w;
+                        it.word_hi = std::min(q.words, q.w + cw);
+                        q.w = it.word_hi;
+                        out[n_items++] = it;
+                        more = true;
+                    }
                 }
             }
         }
@@ -840,7 +856,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     uint64_t launches = 0;
     static_assert(KernelTimes::kRoundSlots == dev::kMaxRounds + 1, "split round slots");
     uint32_t hcnt[dev::kNumCounters];
-    constexpr int kMaxPasses = 16;
+    constexpr int kMaxPasses = 64;
     for (int pass = 0; pass < kMaxPasses; ++pass) {
         prm.defer = pass + 1 < kMaxPasses ? 1u : 0u;
         const bool split = prm.step_budget && n_items != 0;
@@ -870,10 +886,9 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
                 TFSM_CK(cudaStreamSynchronize(I.stream));
                 times_.d2h_bytes += sizeof(pending);
                 if (pending == 0) break;
-                // later rounds double the budget: the long searches that remain finish in a few
-                // rounds instead of paying a round trip per `round_budget` steps
-                const uint32_t budget = (uint32_t)std::min<uint64_t>(
-                    (uint64_t)prm.round_budget << std::min(r - fixed + 1, 20), 1u << 30);
+                // later rounds double the budget, up to 8x: the long searches that remain finish in
+                // fewer rounds, while a task never runs long enough to serialise a round behind it
+                const uint32_t budget = prm.round_budget << std::min(r - fixed + 1, 3);
                 TFSM_CK(dev::launch_split_round(I.g, L.descs.p, I.status.p, prm, I.counters.p, r, budget, L.dom.p,
                                                 L.found.p, L.failed.p, I.splits.p, I.groups.p, I.stream));
                 ++launches;

@@ -103,6 +103,15 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
     // at most max_batch of them, and never mixing parents held by different device levels (an
     // engine call reads its parents' domains from one level).  Candidates left when the time
     // limit stops the run are dropped.
+    //
+    // With call_ms set, the number of candidates per call also follows the calls' cost: a call of
+    // k candidates that took t > call_ms makes the following calls take k * call_ms / t of them (at
+    // least 4), and a full call that took less doubles that limit again, up to max_batch.  The
+    // limit carries over to the next level, whose candidates cost more.  Expensive levels gain
+    // from small calls: a call's searches share the GPU, so every pattern waits longer for the
+    // searches that decide it, and its long failing searches (hub vertices) run on meanwhile; cheap
+    // levels keep one call each.
+    size_t batch_limit = 0;
     auto evaluate_level = [&](std::vector<Node> &nodes, const std::vector<int> &parent_of,
                               const std::vector<Node> *parents) {
         if (nodes.empty()) return;
@@ -123,7 +132,9 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
             st.pruned++;
         }
         if (opt.batched) {
-            const size_t step = std::max<size_t>(1, eo.max_batch);
+            const size_t cap = std::max<size_t>(1, eo.max_batch);
+            if (batch_limit == 0 || eo.call_ms <= 0) batch_limit = cap;
+            batch_limit = std::min(batch_limit, cap);
             auto parent_level = [&](size_t k) -> const Level * {
                 const size_t i = todo[k];
                 return (parents && parent_of[i] >= 0) ? (*parents)[(size_t)parent_of[i]].lvl : nullptr;
@@ -136,7 +147,7 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                 }
                 const Level *prev = parent_level(b0);
                 size_t b1 = b0 + 1;
-                while (b1 < todo.size() && b1 - b0 < step && parent_level(b1) == prev) ++b1;
+                while (b1 < todo.size() && b1 - b0 < batch_limit && parent_level(b1) == prev) ++b1;
                 std::vector<const Pattern *> pats;
                 std::vector<int> par;
                 for (size_t k = b0; k < b1; ++k) {
@@ -153,6 +164,15 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                 eng.evaluate(pats, par, prev, tau, eo, *cur_levels.back(), res, &pushes);
                 st.engine_calls++;
                 st.evaluations += b1 - b0;
+                if (eo.call_ms > 0) {
+                    const double call = eng.times().engine_ms - before.engine_ms;
+                    const size_t k = b1 - b0;
+                    if (call > eo.call_ms)
+                        batch_limit = std::min(batch_limit, std::max<size_t>(std::min<size_t>(4, cap),
+                                                                             (size_t)((double)k * eo.call_ms / call)));
+                    else if (k >= batch_limit)
+                        batch_limit = std::min(cap, 2 * batch_limit);
+                }
                 if (verbose) {
                     uint64_t mx = 0, srch = 0, nf = 0;
                     for (auto &r : res) {

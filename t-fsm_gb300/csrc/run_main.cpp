@@ -58,6 +58,8 @@ int main(int argc, char **argv) {
     if (opt(argc, argv, "-split-rounds")) o.split_rounds = (uint32_t)std::atoi(opt(argc, argv, "-split-rounds"));
     if (opt(argc, argv, "-round-budget")) o.round_budget = (uint32_t)std::atoi(opt(argc, argv, "-round-budget"));
     if (opt(argc, argv, "-search-lanes")) o.search_lanes = (uint32_t)std::atoi(opt(argc, argv, "-search-lanes"));
+    if (opt(argc, argv, "-rank-window")) o.rank_window = (uint32_t)std::atoi(opt(argc, argv, "-rank-window"));
+    if (opt(argc, argv, "-call-ms")) o.call_ms = std::atof(opt(argc, argv, "-call-ms"));
     if (opt(argc, argv, "-time-limit")) o.time_limit_s = std::atof(opt(argc, argv, "-time-limit"));
     rc = tfsm_set_options(g, &o);
     if (rc == TFSM_OK && opt(argc, argv, "-random-orders"))  // random matching orders: same results

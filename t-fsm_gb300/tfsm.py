@@ -91,7 +91,8 @@ class GraphInfoC(C.Structure):
 class OptionsC(C.Structure):
     _fields_ = [("step_budget", C.c_uint32), ("split_slice", C.c_uint32), ("chunk_words", C.c_uint32),
                 ("refine_rounds", C.c_uint32), ("max_batch", C.c_uint32), ("split_rounds", C.c_uint32),
-                ("time_limit_s", C.c_double), ("round_budget", C.c_uint32), ("search_lanes", C.c_uint32)]
+                ("time_limit_s", C.c_double), ("round_budget", C.c_uint32), ("search_lanes", C.c_uint32),
+                ("rank_window", C.c_uint32), ("call_ms", C.c_double)]
 
 
 class MineStatsC(C.Structure):

@@ -91,6 +91,25 @@ def test_mining_in_small_batches_matches_reference(tfsm, graphs, case, tmp_path)
     assert st["complete"] == 1
 
 
+@pytest.mark.parametrize("case", ["cfg1", "el3"])
+def test_call_time_target_shrinks_calls_and_keeps_results(tfsm, graphs, case, tmp_path):
+    """Every call is slower than a 1 ns target: after the first one, calls take 4 candidates."""
+    g = graphs(case)
+    saved = g.options()
+    try:
+        g.set_options(call_ms=0.0)
+        _, whole = mine_set(tfsm, g, case, tmp_path)
+        g.set_options(call_ms=1e-6)
+        pats, st = mine_set(tfsm, g, case, tmp_path)
+    finally:
+        g.set_options(**saved)
+    assert pats == golden_pattern_set(case)
+    assert st["complete"] == 1
+    assert st["engine_calls"] >= whole["engine_calls"]
+    if case == "cfg1":  # 474 candidates over 4 levels: far more than 4 per call after the first
+        assert st["engine_calls"] > 2 * whole["engine_calls"]
+
+
 def test_time_limit_stops_between_engine_calls(tfsm, graphs, tmp_path):
     g = graphs("cfg1")
     saved = g.options()

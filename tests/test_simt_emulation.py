@@ -33,7 +33,10 @@ OPTS = {"default": [], "split": ["-step-budget", "1", "-split-slice", "32", "-ch
         "random_orders": ["-random-orders", "7", "-step-budget", "2"],
         "lanes8": ["-search-lanes", "8"],
         "lanes8_split": ["-search-lanes", "8", "-step-budget", "1", "-split-slice", "32", "-round-budget", "1"],
-        "lanes8_exact": ["-search-lanes", "8", "-exact"]}
+        "lanes8_exact": ["-search-lanes", "8", "-exact"],
+        "rank_window2": ["-rank-window", "2", "-step-budget", "2"],
+        # every emulated call is slower than 1 us: calls shrink to 4 patterns after the first
+        "adaptive_calls": ["-call-ms", "0.001"]}
 # (the quirk case's many-call variants are the slowest to emulate; its other variants cover it)
 RUNS = [(c, o) for c in SMALL for o in OPTS if not (o in ("plain", "batch3") and c == "quirk_elabels")]
 RUNS += [(c, "tiny_buffers") for c in ("clique", "star_hub")]
@@ -49,7 +52,8 @@ def test_emulated_kernels_match_reference(emu, case, opt, tmp_path):
     if opt == "tiny_buffers":
         env["TFSM_SPLIT_CAPACITY"] = "5"
     r = subprocess.run([str(emu), "-file", str(GOLDEN / c["file"]), "-freq", str(c["tau"]), "-maxNodes",
-                        str(c["max_nodes"]), "-out", str(out), *opts], capture_output=True, text=True, timeout=600,
+                        str(c["max_nodes"]), "-out", str(out), *opts, "-call-ms", "0"], capture_output=True,
+                       text=True, timeout=600,
                        env=env)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
     assert set(read_results(out)) == golden_pattern_set(case)
