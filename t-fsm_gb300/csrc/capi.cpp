@@ -240,8 +240,8 @@ int tfsm_evaluate_batch(tfsm_graph *g, const tfsm_pattern *patterns, int32_t n, 
         if (!ptrs.empty()) {
             tfsm::Level lvl;
             std::vector<tfsm::EvalResult> res;
-            std::vector<int> par(ptrs.size(), -1);
-            g->eng->evaluate(ptrs, par, nullptr, (uint32_t)std::max(tau, 0), engine_options(g, flags), lvl, res);
+            const std::vector<tfsm::LevelRef> par(ptrs.size());  // no parents
+            g->eng->evaluate(ptrs, par, (uint32_t)std::max(tau, 0), engine_options(g, flags), lvl, res);
             for (size_t k = 0; k < ptrs.size(); ++k) fill_result(res[k], ptrs[k]->size(), &results[idx[k]]);
         }
         (void)first_err;  // per-pattern errors are reported in results[i].status

@@ -37,6 +37,17 @@ struct Graph {
 // One pattern of a batch.  Plain old data, copied to the device once per batch.
 constexpr int kMaxPush = 4;  // sub-patterns besides the parent whose domains bound a child's
 
+// The bitmap pools of an earlier engine call whose final domains bound this call's initial ones
+// (parents, push-down sources).  A source reference is (slot << kSrcShift) | word offset, slot
+// indexing the call's table of SourceLevel.
+struct SourceLevel {
+    const uint32_t *dom;
+    const uint32_t *failed;
+    uint64_t words;
+};
+constexpr int kSrcShift = 40;
+constexpr uint64_t kSrcMask = (1ull << kSrcShift) - 1;
+
 struct PatDesc {
     int32_t n;
     int32_t n_reps;                     // orbit representatives that get search tasks
@@ -51,9 +62,11 @@ struct PatDesc {
     uint32_t lsize[kMaxN];              // size of u's label range
     uint32_t words[kMaxN];              // bitmap words of u = ceil(lsize / 32)
     uint64_t off[kMaxN];                // word offset of u's bitmaps in the level pools
-    int64_t parent_off[kMaxN];          // word offset of the parent's bitmaps for u, or -1
-    int64_t push_off[kMaxPush][kMaxN];  // further sub-patterns (one edge less) of the same previous
-                                        //   level: word offset of their bitmaps for u's image, or -1
+    int64_t parent_off[kMaxN];          // source reference (SourceLevel) of the parent's bitmaps
+                                        //   for u, or -1
+    int64_t push_off[kMaxPush][kMaxN];  // further sub-patterns (one edge less) of the previous
+                                        //   growth level: source reference of their bitmaps for
+                                        //   u's image, or -1
     int32_t nlf_n[kMaxN];               // neighbour-label-frequency requirements of u
     uint8_t nlf_lab[kMaxN][kMaxN];
     uint8_t nlf_cnt[kMaxN][kMaxN];

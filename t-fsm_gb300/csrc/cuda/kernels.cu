@@ -103,13 +103,25 @@ __device__ __forceinline__ uint32_t find_item(const uint64_t *__restrict__ prefi
 // ------------------------------------------------------------------------------------------------
 // K1: LDF + NLF filter.  One warp per bitmap word, one lane per vertex of the word.
 // ------------------------------------------------------------------------------------------------
+// Bit `lane` of word `word` of a source's final domain (dom & ~failed) at reference `ref`.
+__device__ __forceinline__ bool source_bit(const SourceLevel *__restrict__ srcs, uint32_t n_srcs, int64_t ref,
+                                           uint32_t word, uint32_t lane) {
+    const uint64_t slot = (uint64_t)ref >> kSrcShift;
+    const uint64_t o = ((uint64_t)ref & kSrcMask) + word;
+    if (!TFSM_IN(32, slot, n_srcs)) return true;
+    const SourceLevel S = srcs[slot];
+    if (!TFSM_IN(39, o, S.words)) return true;
+    const uint32_t w = __ldg(S.dom + o) & ~__ldg(S.failed + o);
+    return (w >> lane) & 1u;
+}
+
 __global__ void __launch_bounds__(256) k_domain_init(Graph g, const PatDesc *__restrict__ descs,
                                                      PatStatus *__restrict__ st, const uint32_t *__restrict__ item_pu,
                                                      const uint64_t *__restrict__ prefix, uint32_t n_items,
                                                      uint32_t *__restrict__ dom, uint32_t *__restrict__ found,
-                                                     uint32_t *__restrict__ failed, const uint32_t *__restrict__ pdom,
-                                                     const uint32_t *__restrict__ pfailed, uint64_t chk_words,
-                                                     uint64_t chk_pwords) {
+                                                     uint32_t *__restrict__ failed,
+                                                     const SourceLevel *__restrict__ srcs, uint32_t n_srcs,
+                                                     uint64_t chk_words) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -123,21 +135,12 @@ __global__ void __launch_bounds__(256) k_domain_init(Graph g, const PatDesc *__r
         const uint32_t word = (uint32_t)(gw - prefix[item]);
         const uint32_t xl = word * 32 + lane;
         bool pass = xl < D.lsize[u];
-        const int64_t poff = D.parent_off[u];
         if (!TFSM_IN(30, word, D.words[u]) || !TFSM_IN(31, D.off[u] + word, chk_words)) continue;
-        if (poff >= 0 && !TFSM_IN(32, (uint64_t)poff + word, chk_pwords)) continue;
-        if (poff >= 0) {
-            const uint32_t pw = __ldg(pdom + poff + word) & ~__ldg(pfailed + poff + word);
-            pass = pass && ((pw >> lane) & 1u);
-        }
-        // push-down: every other one-edge-smaller sub-pattern's final domain bounds u's as well
-        // (an embedding of the child restricts to one of the sub-pattern)
-        for (int k = 0; k < kMaxPush && pdom != nullptr; ++k) {
-            const int64_t so = D.push_off[k][u];
-            if (so < 0 || !TFSM_IN(39, (uint64_t)so + word, chk_pwords)) continue;
-            const uint32_t sw = __ldg(pdom + so + word) & ~__ldg(pfailed + so + word);
-            pass = pass && ((sw >> lane) & 1u);
-        }
+        // the parent's final domain, and push-down: every other one-edge-smaller sub-pattern's
+        // final domain bounds u's as well (an embedding of the child restricts to one of each)
+        if (D.parent_off[u] >= 0) pass = pass && source_bit(srcs, n_srcs, D.parent_off[u], word, lane);
+        for (int k = 0; k < kMaxPush; ++k)
+            if (D.push_off[k][u] >= 0) pass = pass && source_bit(srcs, n_srcs, D.push_off[k][u], word, lane);
         if (__any_sync(0xffffffffu, pass)) {
             const uint32_t x = D.lstart[u] + xl;
             uint32_t b = 0, e = 0;
@@ -993,15 +996,15 @@ static int num_sms() {
 
 cudaError_t launch_domain_init(const Graph &g, const PatDesc *descs, PatStatus *st, const uint32_t *item_pu,
                                const uint64_t *prefix, uint32_t n_items, uint64_t total_words, uint32_t *dom,
-                               uint32_t *found, uint32_t *failed, const uint32_t *pdom, const uint32_t *pfailed,
-                               uint64_t chk_words, uint64_t chk_pwords, cudaStream_t s) {
+                               uint32_t *found, uint32_t *failed, const SourceLevel *srcs, uint32_t n_srcs,
+                               uint64_t chk_words, cudaStream_t s) {
     if (n_items == 0 || total_words == 0) return cudaSuccess;
     const uint64_t warps = total_words;
     uint64_t blocks = (warps * 32 + 255) / 256;
     const uint64_t cap = (uint64_t)num_sms() * 8 * 4;
     if (blocks > cap) blocks = cap;
     TFSM_LAUNCH(k_domain_init, (unsigned)blocks, 256, s, g, descs, st, item_pu, prefix, n_items, dom, found, failed,
-                pdom, pfailed, chk_words, chk_pwords);
+                srcs, n_srcs, chk_words);
 #ifdef TFSM_BOUNDS_CHECK
     if (cudaStreamSynchronize(s) != cudaSuccess) return cudaGetLastError();
 #endif

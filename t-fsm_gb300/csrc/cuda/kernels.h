@@ -12,8 +12,8 @@ constexpr int kSearchWarps = 8;  // warps per block of the search kernels
 
 cudaError_t launch_domain_init(const Graph &g, const PatDesc *descs, PatStatus *st, const uint32_t *item_pu,
                                const uint64_t *prefix, uint32_t n_items, uint64_t total_words, uint32_t *dom,
-                               uint32_t *found, uint32_t *failed, const uint32_t *pdom, const uint32_t *pfailed,
-                               uint64_t chk_words, uint64_t chk_pwords, cudaStream_t s);
+                               uint32_t *found, uint32_t *failed, const SourceLevel *srcs, uint32_t n_srcs,
+                               uint64_t chk_words, cudaStream_t s);
 
 // Arc-consistency round `round` (0..31) over the items' words; see k_refine for which patterns
 // take part.

@@ -208,6 +208,7 @@ struct GpuEngine::Impl {
     DevBuf<uint64_t> prefix;
     DevBuf<dev::SearchItem> items;
     PinnedBuf<dev::SearchItem> hitems;  // staging of the search items (rewritten each call)
+    DevBuf<dev::SourceLevel> srcs;      // the earlier calls' pools read by this call's domain init
     DevBuf<uint32_t> counters;
     DevBuf<dev::SplitTask> splits;
     DevBuf<dev::SplitGroup> groups;
@@ -425,7 +426,7 @@ void gql_plan(const Pattern &pat, const uint32_t *dsize, int start, uint8_t *ord
 
 }  // namespace
 
-void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::vector<int> &parent, const Level *prev,
+void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::vector<LevelRef> &parent,
                          uint32_t tau, const EngineOptions &opt, Level &out, std::vector<EvalResult> &res,
                          const std::vector<std::vector<PushSource>> *push) {
     Impl &I = *impl_;
@@ -452,6 +453,22 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     L.hdescs.assign(P, PatDesc());
     std::vector<char> trivial(P, 0), express(P, 0);
     uint64_t total = 0;
+    // the earlier calls' pools this call reads (parents, push-down sources): one table slot each
+    std::vector<dev::SourceLevel> srcs;
+    std::map<const Level::Impl *, uint32_t> slot_of;
+    auto source = [&](const LevelRef &r) -> const PatDesc * {
+        if (!r.lvl || !r.lvl->impl || r.idx < 0 || (size_t)r.idx >= r.lvl->impl->hdescs.size()) return nullptr;
+        return &r.lvl->impl->hdescs[(size_t)r.idx];
+    };
+    auto ref = [&](const LevelRef &r, uint64_t off) -> int64_t {
+        const Level::Impl *li = r.lvl->impl.get();
+        auto it = slot_of.find(li);
+        if (it == slot_of.end()) {
+            it = slot_of.emplace(li, (uint32_t)srcs.size()).first;
+            srcs.push_back({li->dom.p, li->failed.p, li->words});
+        }
+        return (int64_t)(((uint64_t)it->second << dev::kSrcShift) | off);
+    };
     for (size_t p = 0; p < P; ++p) {
         const Pattern &pat = *pats[p];
         PatDesc &D = L.hdescs[p];
@@ -486,25 +503,23 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
             D.off[u] = total;
             total += D.words[u];
             D.parent_off[u] = -1;
-            if (prev && parent[p] >= 0) {
-                const PatDesc &PD = prev->impl->hdescs[(size_t)parent[p]];
-                if (u < PD.n) D.parent_off[u] = (int64_t)PD.off[u];
-            }
+            const PatDesc *PD = p < parent.size() ? source(parent[p]) : nullptr;
+            if (PD && u < PD->n) D.parent_off[u] = ref(parent[p], PD->off[u]);
         }
         static_assert(kMaxPushSources == dev::kMaxPush, "push-down sources");
         for (int k = 0; k < dev::kMaxPush; ++k)
             for (int u = 0; u < dev::kMaxN; ++u) D.push_off[k][u] = -1;
-        if (prev && push && p < push->size()) {
+        if (push && p < push->size()) {
             int k = 0;
             for (const PushSource &src : (*push)[p]) {
                 if (k == dev::kMaxPush) break;
-                if (src.idx < 0 || (size_t)src.idx >= prev->impl->hdescs.size()) continue;
-                const PatDesc &SD = prev->impl->hdescs[(size_t)src.idx];
+                const PatDesc *SD = source(src.at);
+                if (!SD) continue;
                 bool any = false;
                 for (int u = 0; u < n; ++u) {
                     const int s = src.vertex[u];
-                    if (s < 0 || s >= SD.n || SD.lab[s] != D.lab[u]) continue;  // same label: same word range
-                    D.push_off[k][u] = (int64_t)SD.off[s];
+                    if (s < 0 || s >= SD->n || SD->lab[s] != D.lab[u]) continue;  // same label: same word range
+                    D.push_off[k][u] = ref(src.at, SD->off[s]);
                     any = true;
                 }
                 k += any ? 1 : 0;
@@ -532,8 +547,12 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     times_.h2d_bytes += P * sizeof(PatDesc);
     TFSM_CK(cudaMemsetAsync(I.status.p, 0, P * sizeof(PatStatus), I.stream));
 
-    const uint32_t *pdom = prev ? prev->impl->dom.p : nullptr;
-    const uint32_t *pfailed = prev ? prev->impl->failed.p : nullptr;
+    I.srcs.ensure(std::max<size_t>(1, srcs.size()));
+    if (!srcs.empty()) {
+        TFSM_CK(cudaMemcpyAsync(I.srcs.p, srcs.data(), srcs.size() * sizeof(dev::SourceLevel), cudaMemcpyHostToDevice,
+                                I.stream));
+        times_.h2d_bytes += srcs.size() * sizeof(dev::SourceLevel);
+    }
 
     // ---- domain init over every (pattern, vertex) ----
     std::vector<uint32_t> item_pu;
@@ -589,8 +608,8 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         run_captured(I.stream, I.exec_init, [&]() {
             TFSM_CK(record_in_sequence(I.ev0, I.stream));
             TFSM_CK(dev::launch_domain_init(I.g, L.descs.p, I.status.p, I.item_pu.p, I.prefix.p, n_it, words, L.dom.p,
-                                            L.found.p, L.failed.p, pdom, pfailed, total,
-                                            prev ? prev->impl->words : 0, I.stream));
+                                            L.found.p, L.failed.p, I.srcs.p, (uint32_t)srcs.size(), total,
+                                            I.stream));
             TFSM_CK(record_in_sequence(I.ev_mid, I.stream));
             for (int r = 0; r < fixed_refine; ++r)
                 TFSM_CK(dev::launch_refine(I.g, L.descs.p, I.status.p, I.item_pu.p, I.prefix.p, n_it, words, L.dom.p,

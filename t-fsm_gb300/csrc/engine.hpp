@@ -86,11 +86,18 @@ struct Level {
     size_t size() const;  // patterns in the batch
 };
 
-// A sub-pattern of a candidate with one edge less, evaluated in the previous level (push-down
-// pruning: its final domains bound the candidate's).  At most kMaxPushSources per candidate.
+// A pattern evaluated by an earlier engine call: `idx` in the batch that call wrote to `lvl`.
+struct LevelRef {
+    const Level *lvl = nullptr;
+    int idx = -1;
+};
+
+// A sub-pattern of a candidate with one edge less, evaluated in the previous growth level
+// (push-down pruning: its final domains bound the candidate's).  At most kMaxPushSources per
+// candidate.
 constexpr int kMaxPushSources = 4;
 struct PushSource {
-    int idx;            // its index in the previous level
+    LevelRef at;        // where its bitmaps are
     int8_t vertex[16];  // per candidate vertex: the sub-pattern vertex it maps to, or -1
 };
 
@@ -101,10 +108,12 @@ public:
     GpuEngine(const GpuEngine &) = delete;
     GpuEngine &operator=(const GpuEngine &) = delete;
 
-    // Evaluate `pats` against the graph.  parent[i] indexes the pattern's parent in `prev`
-    // (or -1).  `out` receives this batch's device memory for the next level.
-    void evaluate(const std::vector<const Pattern *> &pats, const std::vector<int> &parent, const Level *prev,
-                  uint32_t tau, const EngineOptions &opt, Level &out, std::vector<EvalResult> &res,
+    // Evaluate `pats` against the graph.  parent[i] is the pattern's parent (lvl == nullptr:
+    // none); parents and push-down sources may come from any number of earlier calls, whose
+    // Levels must stay alive during the call.  `out` receives this batch's device memory for the
+    // next level.
+    void evaluate(const std::vector<const Pattern *> &pats, const std::vector<LevelRef> &parent, uint32_t tau,
+                  const EngineOptions &opt, Level &out, std::vector<EvalResult> &res,
                   const std::vector<std::vector<PushSource>> *push = nullptr);
 
     const KernelTimes &times() const { return times_; }

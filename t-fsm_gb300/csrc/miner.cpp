@@ -25,7 +25,7 @@ struct Node {
     Pattern pat;
     EvalResult res;
     bool pruned = false;   // a sub-pattern with one edge less is infrequent: decided without search
-    std::vector<PushSource> push;  // frequent sub-patterns with one edge less, in the parent's level
+    std::vector<PushSource> push;  // frequent sub-patterns with one edge less (previous level)
     Level *lvl = nullptr;  // device memory holding this pattern's final domains
     int idx = 0;           // index inside lvl
 };
@@ -100,9 +100,8 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
         return !st.complete;
     };
     // Evaluates a level's candidates.  Batched: consecutive candidates go into one engine call,
-    // at most max_batch of them, and never mixing parents held by different device levels (an
-    // engine call reads its parents' domains from one level).  Candidates left when the time
-    // limit stops the run are dropped.
+    // at most max_batch of them (their parents and push-down sources may come from any of the
+    // previous level's calls).  Candidates left when the time limit stops the run are dropped.
     //
     // With call_ms set, the number of candidates per call also follows the calls' cost: a call of
     // k candidates that took t > call_ms makes the following calls take k * call_ms / t of them (at
@@ -118,6 +117,11 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
         const int lvl_no = st.levels + 1;
         const EngineOptions &eo = opt.engine_for(lvl_no);
         const double wall_before = eng.times().engine_ms;
+        auto parent_ref = [&](size_t i) -> LevelRef {
+            if (!parents || parent_of[i] < 0) return LevelRef{};
+            const Node &pn = (*parents)[(size_t)parent_of[i]];
+            return LevelRef{pn.lvl, pn.idx};
+        };
         // sub-pattern pruning decided some candidates already; the engine evaluates the rest
         std::vector<size_t> todo;
         for (size_t i = 0; i < nodes.size(); ++i) {
@@ -135,25 +139,19 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
             const size_t cap = std::max<size_t>(1, eo.max_batch);
             if (batch_limit == 0 || eo.call_ms <= 0) batch_limit = cap;
             batch_limit = std::min(batch_limit, cap);
-            auto parent_level = [&](size_t k) -> const Level * {
-                const size_t i = todo[k];
-                return (parents && parent_of[i] >= 0) ? (*parents)[(size_t)parent_of[i]].lvl : nullptr;
-            };
             size_t b0 = 0;
             while (b0 < todo.size()) {
                 if (out_of_time()) {
                     nodes.resize(todo[b0]);
                     break;
                 }
-                const Level *prev = parent_level(b0);
-                size_t b1 = b0 + 1;
-                while (b1 < todo.size() && b1 - b0 < batch_limit && parent_level(b1) == prev) ++b1;
+                const size_t b1 = std::min(todo.size(), b0 + batch_limit);
                 std::vector<const Pattern *> pats;
-                std::vector<int> par;
+                std::vector<LevelRef> par;
                 for (size_t k = b0; k < b1; ++k) {
                     const size_t i = todo[k];
                     pats.push_back(&nodes[i].pat);
-                    par.push_back(prev ? (*parents)[(size_t)parent_of[i]].idx : -1);
+                    par.push_back(parent_ref(i));
                 }
                 cur_levels.emplace_back(new Level);
                 std::vector<EvalResult> res;
@@ -161,7 +159,7 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                 const double search_before = before.search_ms;
                 std::vector<std::vector<PushSource>> pushes;
                 for (size_t kk = b0; kk < b1; ++kk) pushes.push_back(nodes[todo[kk]].push);
-                eng.evaluate(pats, par, prev, tau, eo, *cur_levels.back(), res, &pushes);
+                eng.evaluate(pats, par, tau, eo, *cur_levels.back(), res, &pushes);
                 st.engine_calls++;
                 st.evaluations += b1 - b0;
                 if (eo.call_ms > 0) {
@@ -221,17 +219,11 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                 }
                 st.evaluations++;
                 std::vector<const Pattern *> pats{&nodes[i].pat};
-                std::vector<int> par{-1};
-                const Level *prev = nullptr;
-                if (parents && parent_of[i] >= 0) {
-                    const Node &pn = (*parents)[(size_t)parent_of[i]];
-                    par[0] = pn.idx;
-                    prev = pn.lvl;
-                }
+                const std::vector<LevelRef> par{parent_ref(i)};
                 cur_levels.emplace_back(new Level);
                 std::vector<EvalResult> res;
                 const std::vector<std::vector<PushSource>> pushes{nodes[i].push};
-                eng.evaluate(pats, par, prev, tau, eo, *cur_levels.back(), res, &pushes);
+                eng.evaluate(pats, par, tau, eo, *cur_levels.back(), res, &pushes);
                 st.engine_calls++;
                 nodes[i].res = std::move(res[0]);
                 nodes[i].lvl = cur_levels.back().get();
@@ -281,7 +273,7 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
             // child, its one-edge-smaller sub-patterns:
             //   * one evaluated and infrequent: the child is infrequent (MNI is anti-monotone);
             //   * one missing from a complete level (single edge label): infrequent as well;
-            //   * the frequent ones held by the parent's device level bound the child's domains.
+            //   * the frequent ones bound the child's domains (up to kMaxPushSources of them).
             std::vector<std::string> keys(level.size());
             std::vector<std::vector<int>> orders(level.size());
             {
@@ -300,7 +292,6 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                 std::vector<SubPattern> subs;
                 for (size_t i; (i = k.fetch_add(1)) < next.size();) {
                     Node &child = next[i];
-                    const Node &par = level[(size_t)parent_of[i]];
                     one_edge_smaller(child.pat, subs);
                     for (auto &sp : subs) {
                         auto it = evaluated.find(sp.key);
@@ -314,10 +305,10 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                             child.pruned = true;
                             break;
                         }
-                        if (sn.lvl != par.lvl || it->second == (size_t)parent_of[i] || !sn.lvl) continue;
+                        if (it->second == (size_t)parent_of[i] || !sn.lvl) continue;
                         if (child.push.size() >= (size_t)kMaxPushSources) continue;
                         PushSource src;
-                        src.idx = sn.idx;
+                        src.at = LevelRef{sn.lvl, sn.idx};
                         for (int u = 0; u < 16; ++u) src.vertex[u] = -1;
                         const std::vector<int> &ord = orders[it->second];
                         for (int u = 0; u < child.pat.size() && u < 16; ++u)

@@ -251,7 +251,7 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     NA_CK(cudaMemcpyAsync(d_prefix, prefix, (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
     // every bitmap word of every vertex is written here, so no clearing of the pools is needed
     NA_CK(dev::launch_domain_init(g, d_desc, d_status, d_item_pu, d_prefix, (uint32_t)n, words, d_dom, d_found,
-                                  d_failed, nullptr, nullptr, words, 0, s));
+                                  d_failed, nullptr, 0, words, s));
     PatStatus st;
     NA_CK(cudaMemcpyAsync(&st, d_status, sizeof(st), cudaMemcpyDeviceToHost, s));
     NA_CK(cudaStreamSynchronize(s));
