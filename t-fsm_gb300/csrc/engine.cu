@@ -1,8 +1,9 @@
 // Host orchestration of the GPU support evaluation.
 //
-// evaluate() runs, for one batch of patterns (one pattern in the plain path, a whole growth
-// level in the batched path):
+// evaluate() runs, for one batch of patterns (one pattern in the plain path, a growth level or
+// a slice of one in the batched path):
 //   1. k_domain_init     LDF + NLF bitmaps, children starting from their parent's final domains
+//                        (and those of further sub-patterns), read from earlier calls' pools
 //   2. k_refine x R      arc consistency (to a fixpoint for distinct-label trees)
 //   3. host              decide what the domain sizes already decide; matching orders (GQL
 //                        order by domain size, serial/gmatch.h:584-685) for the rest
