@@ -465,6 +465,8 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         const Level::Impl *li = r.lvl->impl.get();
         auto it = slot_of.find(li);
         if (it == slot_of.end()) {
+            // slot << kSrcShift must stay a non-negative int64 (a negative reference means none)
+            if (srcs.size() >= (1ull << (63 - dev::kSrcShift))) throw EngineError(6, "too many source levels");
             it = slot_of.emplace(li, (uint32_t)srcs.size()).first;
             srcs.push_back({li->dom.p, li->failed.p, li->words});
         }
