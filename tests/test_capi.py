@@ -68,3 +68,34 @@ def test_cli_usage_error(built):
 
     r = subprocess.run([str(built / "bin" / "run")], capture_output=True, text=True)
     assert r.returncode == 2 and "usage" in r.stderr
+
+
+def test_ctypes_structs_match_the_header_layout(tfsm, tmp_path):
+    """Every struct of the binding has the size and field offsets the C compiler gives the header's
+    (the option and statistics structs grow at their ends; a mismatch would shift fields)."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"tfsm_dfs_code": tfsm.DfsCode, "tfsm_pattern": tfsm.PatternC, "tfsm_result": tfsm.ResultC,
+               "tfsm_graph_info_t": tfsm.GraphInfoC, "tfsm_mine_stats": tfsm.MineStatsC,
+               "tfsm_options": tfsm.OptionsC}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "tfsm.h"', "int main(void) {"]
+    for cname, cls in structs.items():
+        lines.append(f'    printf("{cname} %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            cfield = fname.rstrip("_")  # ctypes name from_ is the C field from
+            lines.append(f'    printf("{cname}.{fname} %zu\\n", offsetof({cname}, {cfield}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(line.rsplit(" ", 1) for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                              check=True).stdout.splitlines())
+    for cname, cls in structs.items():
+        assert int(got[cname]) == C.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert int(got[f"{cname}.{fname}"]) == getattr(cls, fname).offset, f"{cname}.{fname}"
