@@ -10,6 +10,9 @@ namespace dev {
 
 constexpr int kSearchWarps = 8;  // warps per block of the search kernels
 
+// LDF + NLF bitmaps of the items' (pattern, vertex) pairs, intersected with the final domains of
+// the sources that PatDesc::parent_off / push_off reference in the table `srcs` (n_srcs pools of
+// earlier calls; may be empty).
 cudaError_t launch_domain_init(const Graph &g, const PatDesc *descs, PatStatus *st, const uint32_t *item_pu,
                                const uint64_t *prefix, uint32_t n_items, uint64_t total_words, uint32_t *dom,
                                uint32_t *found, uint32_t *failed, const SourceLevel *srcs, uint32_t n_srcs,
