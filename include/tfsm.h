@@ -122,6 +122,34 @@ int tfsm_evaluate_support(tfsm_graph *g, const tfsm_pattern *pattern, int32_t ta
 int tfsm_evaluate_batch(tfsm_graph *g, const tfsm_pattern *patterns, int32_t n, int32_t tau, uint32_t flags,
                         tfsm_result *results);
 
+/* Final domains of the patterns of one tfsm_evaluate_level call, kept on the device so that the
+ * next growth level starts from them.  Replaces the reference's parent PatternProgress and its
+ * cache of non-candidates handed to children (parallel/graph.h:402-414,
+ * parallel/comper.h:1582-1612). */
+typedef struct tfsm_domains tfsm_domains;
+
+/* A pattern's parent: pattern `index` (the position in its call's `patterns`) of an earlier
+ * tfsm_evaluate_level call on the same graph, whose domains `domains` holds.  The parent must be a
+ * sub-pattern of the child under the same vertex numbering: every parent vertex keeps its id and
+ * label, and every parent edge is a child edge, as when the child's DFS code extends the parent's. */
+typedef struct {
+    const tfsm_domains *domains; /* NULL: no parent */
+    int32_t index;
+} tfsm_parent;
+
+/* tfsm_evaluate_batch with parents (`parents` may be NULL).  A pattern starts from its parent's
+ * final domains (candidates minus proven non-candidates), which only removes vertices that cannot
+ * be in its MNI domains: `frequent` equals the result without a parent, and so do `mni` and
+ * `support` with TFSM_FLAG_EXACT.  A parent that is not a sub-pattern as above, that belongs to
+ * another graph or whose own evaluation failed makes that pattern's status TFSM_ERR_ARG.  With
+ * out != NULL the call's final domains stay on the device and *out receives them (NULL when no
+ * pattern was evaluated); release them with tfsm_domains_free, which may come before or after
+ * tfsm_graph_free but not during a call that reads them. */
+int tfsm_evaluate_level(tfsm_graph *g, const tfsm_pattern *patterns, int32_t n, int32_t tau, uint32_t flags,
+                        const tfsm_parent *parents, tfsm_result *results, tfsm_domains **out);
+
+void tfsm_domains_free(tfsm_domains *d);
+
 /* Whole mining run: frequent patterns with at most max_nodes vertices (-1: unbounded), written
  * to `results_path` (may be NULL) in the serial reference's grami_results.txt format.
  * Replaces GraMi::project (serial/grami.h:224-234) and Worker::run (parallel/worker.h:226-284). */

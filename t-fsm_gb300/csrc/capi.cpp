@@ -34,6 +34,13 @@ struct tfsm_cost_model {
     std::unique_ptr<tfsm::CostModel> m;
 };
 
+struct tfsm_domains {
+    const tfsm_graph *g = nullptr;
+    tfsm::Level lvl;                  // the call's bitmap pools
+    std::vector<tfsm::Pattern> pats;  // by position in the call (for the sub-pattern check)
+    std::vector<int> slot;            // by position in the call: index in lvl, or -1 (not evaluated)
+};
+
 namespace {
 
 thread_local std::string g_err;
@@ -214,39 +221,83 @@ int tfsm_graph_info(const tfsm_graph *g, tfsm_graph_info_t *info) {
     });
 }
 
-int tfsm_evaluate_batch(tfsm_graph *g, const tfsm_pattern *patterns, int32_t n, int32_t tau, uint32_t flags,
-                        tfsm_result *results) {
+namespace {
+
+// `par` is a sub-pattern of `child` under the same vertex numbering (same labels, every edge kept).
+bool is_parent_of(const tfsm::Pattern &par, const tfsm::Pattern &child) {
+    if (par.size() > child.size()) return false;
+    for (int u = 0; u < par.size(); ++u) {
+        if (par.vertices[(size_t)u].label != child.vertices[(size_t)u].label) return false;
+        for (const tfsm::PEdge &e : par.vertices[(size_t)u].edges) {
+            bool kept = false;
+            for (const tfsm::PEdge &f : child.vertices[(size_t)u].edges) kept = kept || (f.to == e.to && f.label == e.label);
+            if (!kept) return false;
+        }
+    }
+    return true;
+}
+
+}  // namespace
+
+int tfsm_evaluate_level(tfsm_graph *g, const tfsm_pattern *patterns, int32_t n, int32_t tau, uint32_t flags,
+                        const tfsm_parent *parents, tfsm_result *results, tfsm_domains **out) {
     return guarded([&]() -> int {
+        if (out) *out = nullptr;
         if (!g || (n > 0 && (!patterns || !results)) || n < 0) return fail(TFSM_ERR_ARG, "null argument");
         std::lock_guard<std::mutex> lk(g->mu);
-        std::vector<tfsm::Pattern> pats((size_t)n);
+        std::unique_ptr<tfsm_domains> keep(new tfsm_domains);
+        keep->g = g;
+        keep->pats.resize((size_t)n);
+        keep->slot.assign((size_t)n, -1);
         std::vector<const tfsm::Pattern *> ptrs;
+        std::vector<tfsm::LevelRef> par;
         std::vector<int> idx;
-        int first_err = TFSM_OK;
         for (int i = 0; i < n; ++i) {
             std::string why;
             std::memset(&results[i], 0, sizeof(tfsm_result));
-            if (!build_pattern(&patterns[i], pats[(size_t)i], why)) {
-                results[i].status = why.find("16 vertices") != std::string::npos ? TFSM_ERR_PATTERN : TFSM_ERR_ARG;
-                if (first_err == TFSM_OK) {
-                    first_err = results[i].status;
-                    g_err = why;
+            tfsm::Pattern &p = keep->pats[(size_t)i];
+            tfsm::LevelRef ref;
+            bool ok = build_pattern(&patterns[i], p, why);
+            if (ok && parents && parents[i].domains) {
+                const tfsm_domains *d = parents[i].domains;
+                const int j = parents[i].index;
+                if (d->g != g) {
+                    ok = false;
+                    why = "parent domains belong to another graph";
+                } else if (j < 0 || (size_t)j >= d->slot.size() || d->slot[(size_t)j] < 0) {
+                    ok = false;
+                    why = "parent index names no evaluated pattern of that call";
+                } else if (!is_parent_of(d->pats[(size_t)j], p)) {
+                    ok = false;
+                    why = "parent is not a sub-pattern of the pattern under the same vertex numbering";
+                } else {
+                    ref = tfsm::LevelRef{&d->lvl, d->slot[(size_t)j]};
                 }
+            }
+            if (!ok) {
+                results[i].status = why.find("16 vertices") != std::string::npos ? TFSM_ERR_PATTERN : TFSM_ERR_ARG;
+                if (g_err.empty()) g_err = why;  // per-pattern errors are reported in results[i].status
                 continue;
             }
-            ptrs.push_back(&pats[(size_t)i]);
+            keep->slot[(size_t)i] = (int)ptrs.size();
+            ptrs.push_back(&p);
+            par.push_back(ref);
             idx.push_back(i);
         }
-        if (!ptrs.empty()) {
-            tfsm::Level lvl;
-            std::vector<tfsm::EvalResult> res;
-            const std::vector<tfsm::LevelRef> par(ptrs.size());  // no parents
-            g->eng->evaluate(ptrs, par, (uint32_t)std::max(tau, 0), engine_options(g, flags), lvl, res);
-            for (size_t k = 0; k < ptrs.size(); ++k) fill_result(res[k], ptrs[k]->size(), &results[idx[k]]);
-        }
-        (void)first_err;  // per-pattern errors are reported in results[i].status
+        if (ptrs.empty()) return TFSM_OK;
+        std::vector<tfsm::EvalResult> res;
+        g->eng->evaluate(ptrs, par, (uint32_t)std::max(tau, 0), engine_options(g, flags), keep->lvl, res);
+        for (size_t k = 0; k < ptrs.size(); ++k) fill_result(res[k], ptrs[k]->size(), &results[idx[k]]);
+        if (out) *out = keep.release();
         return TFSM_OK;
     });
+}
+
+void tfsm_domains_free(tfsm_domains *d) { delete d; }
+
+int tfsm_evaluate_batch(tfsm_graph *g, const tfsm_pattern *patterns, int32_t n, int32_t tau, uint32_t flags,
+                        tfsm_result *results) {
+    return tfsm_evaluate_level(g, patterns, n, tau, flags, nullptr, results, nullptr);
 }
 
 int tfsm_evaluate_support(tfsm_graph *g, const tfsm_pattern *pattern, int32_t tau, uint32_t flags,

@@ -38,6 +38,8 @@ EXPORTED = (
     "tfsm_graph_info",
     "tfsm_evaluate_support",
     "tfsm_evaluate_batch",
+    "tfsm_evaluate_level",
+    "tfsm_domains_free",
     "tfsm_mine",
     "tfsm_get_options",
     "tfsm_set_options",
@@ -74,6 +76,10 @@ class DfsCode(C.Structure):
 
 class PatternC(C.Structure):
     _fields_ = [("n_codes", C.c_int32), ("codes", C.POINTER(DfsCode))]
+
+
+class ParentC(C.Structure):
+    _fields_ = [("domains", C.c_void_p), ("index", C.c_int32)]
 
 
 class ResultC(C.Structure):
@@ -128,6 +134,10 @@ def lib() -> C.CDLL:
                                             C.POINTER(ResultC)]
         L.tfsm_evaluate_batch.argtypes = [C.c_void_p, C.POINTER(PatternC), C.c_int32, C.c_int32, C.c_uint32,
                                           C.POINTER(ResultC)]
+        L.tfsm_evaluate_level.argtypes = [C.c_void_p, C.POINTER(PatternC), C.c_int32, C.c_int32, C.c_uint32,
+                                          C.POINTER(ParentC), C.POINTER(ResultC), C.POINTER(C.c_void_p)]
+        L.tfsm_domains_free.argtypes = [C.c_void_p]
+        L.tfsm_domains_free.restype = None
         L.tfsm_mine.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_uint32, C.c_char_p, C.POINTER(MineStatsC)]
         L.tfsm_get_options.argtypes = [C.c_void_p, C.POINTER(OptionsC)]
         L.tfsm_set_options.argtypes = [C.c_void_p, C.POINTER(OptionsC)]
@@ -150,7 +160,7 @@ def lib() -> C.CDLL:
         L.tfsm_last_error.argtypes = []
         L.tfsm_last_error.restype = C.c_char_p
         for f in EXPORTED:
-            if f not in ("tfsm_graph_free", "tfsm_last_error", "tfsm_cost_model_free"):
+            if f not in ("tfsm_graph_free", "tfsm_last_error", "tfsm_cost_model_free", "tfsm_domains_free"):
                 getattr(L, f).restype = C.c_int
         _lib = L
     return _lib
@@ -182,6 +192,45 @@ class Result:
     decided_by_filter: bool
     searches: int
     steps: int
+
+
+def _pattern_array(patterns: Iterable[Sequence[Code]]):
+    pats = [list(p) for p in patterns]
+    n = len(pats)
+    keep = []
+    arr = (PatternC * max(n, 1))()
+    for i, p in enumerate(pats):
+        codes = (DfsCode * max(len(p), 1))(*[DfsCode(*c) for c in p])
+        keep.append(codes)
+        arr[i].n_codes = len(p)
+        arr[i].codes = C.cast(codes, C.POINTER(DfsCode))
+    return arr, n, keep
+
+
+def _results(res, n: int) -> list[Result]:
+    return [Result(r.status, bool(r.frequent), r.support, list(r.mni[: r.n_vertices]), bool(r.decided_by_filter),
+                   r.searches, r.steps) for r in res[:n]]
+
+
+class Domains:
+    """Final domains of one Graph.evaluate_level call, kept on the device (tfsm_domains)."""
+
+    def __init__(self, h: int):
+        self._h = h
+
+    def close(self) -> None:
+        if self._h:
+            lib().tfsm_domains_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 class Graph:
@@ -235,20 +284,34 @@ class Graph:
         return {f: getattr(gi, f) for f, _ in GraphInfoC._fields_}
 
     def evaluate(self, patterns: Iterable[Sequence[Code]], tau: int | None = None, flags: int = 0) -> list[Result]:
-        pats = [list(p) for p in patterns]
-        n = len(pats)
-        keep = []
-        arr = (PatternC * max(n, 1))()
-        for i, p in enumerate(pats):
-            codes = (DfsCode * max(len(p), 1))(*[DfsCode(*c) for c in p])
-            keep.append(codes)
-            arr[i].n_codes = len(p)
-            arr[i].codes = C.cast(codes, C.POINTER(DfsCode))
+        arr, n, _keep = _pattern_array(patterns)
         res = (ResultC * max(n, 1))()
         rc = lib().tfsm_evaluate_batch(self._h, arr, n, int(self.tau if tau is None else tau), int(flags), res)
         _check(rc)
-        return [Result(r.status, bool(r.frequent), r.support, list(r.mni[: r.n_vertices]), bool(r.decided_by_filter),
-                       r.searches, r.steps) for r in res[:n]]
+        return _results(res, n)
+
+    def evaluate_level(self, patterns: Iterable[Sequence[Code]], parents: Sequence | None = None,
+                       tau: int | None = None, flags: int = 0, keep: bool = False):
+        """tfsm_evaluate_level: like evaluate, with parents[i] = (Domains, index) or None per pattern.
+        Returns (results, Domains or None); with keep=True the call's final domains stay on the
+        device for the next level's parents."""
+        arr, n, _keep = _pattern_array(patterns)
+        par = None
+        if parents is not None:
+            if len(parents) != n:
+                raise ValueError("one parent entry per pattern")
+            par = (ParentC * max(n, 1))()
+            for i, pr in enumerate(parents):
+                if pr is not None:
+                    d, idx = pr
+                    par[i].domains = d._h
+                    par[i].index = int(idx)
+        res = (ResultC * max(n, 1))()
+        h = C.c_void_p()
+        rc = lib().tfsm_evaluate_level(self._h, arr, n, int(self.tau if tau is None else tau), int(flags), par, res,
+                                       C.byref(h) if keep else None)
+        _check(rc)
+        return _results(res, n), (Domains(h.value) if keep and h.value else None)
 
     def options(self) -> dict:
         o = OptionsC()

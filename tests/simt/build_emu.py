@@ -1,8 +1,9 @@
 """Build the host-side SIMT emulation of the engine (test infrastructure only).
 
 Compiles the product's kernel and engine sources unchanged, as C++ for the CPU, against
-tests/simt/cuda_runtime.h, with sanitizers, into tests/simt/_build/run_emu (the `run` CLI).
-usage: python tests/simt/build_emu.py [asan|tsan]
+tests/simt/cuda_runtime.h, with sanitizers, into tests/simt/_build/run_emu_<kind> (the `run` CLI)
+or, with main="abi", tests/simt/_build/abi_emu_<kind> (the C-ABI driver tests/simt/abi_main.cpp).
+usage: python tests/simt/build_emu.py [asan|tsan|none] [run|abi]
 """
 from __future__ import annotations
 
@@ -18,13 +19,15 @@ SANITIZE = {"asan": ["-fsanitize=address,undefined", "-fno-sanitize-recover=unde
             "tsan": ["-fsanitize=thread"], "none": []}
 
 
-def build(kind: str = "asan") -> Path:
+def build(kind: str = "asan", main: str = "run") -> Path:
     out_dir = HERE / "_build"
     out_dir.mkdir(exist_ok=True)
-    exe = out_dir / f"run_emu_{kind}"
+    exe = out_dir / f"{main}_emu_{kind}"
+    entry = CSRC / "run_main.cpp" if main == "run" else HERE / "abi_main.cpp"
     srcs = [CSRC / "cuda" / "kernels.cu", CSRC / "engine.cu", CSRC / "noalloc.cu", CSRC / "miner.cpp",
-            CSRC / "capi.cpp", CSRC / "run_main.cpp", HERE / "costmodel_stub.cpp"]
-    deps = srcs + list(CSRC.rglob("*.h*")) + list(CSRC.rglob("*.cuh")) + [HERE / "cuda_runtime.h"]
+            CSRC / "capi.cpp", entry, HERE / "costmodel_stub.cpp"]
+    deps = srcs + list(CSRC.rglob("*.h*")) + list(CSRC.rglob("*.cuh")) + [HERE / "cuda_runtime.h",
+                                                                          ROOT / "include" / "tfsm.h"]
     if exe.exists() and all(d.stat().st_mtime <= exe.stat().st_mtime for d in deps):
         return exe
     cmd = ["g++", "-std=c++20", "-O1", "-g", "-pthread", "-DTFSM_SIMT_EMULATION", "-I", str(HERE), "-I", str(CSRC),
@@ -36,4 +39,4 @@ def build(kind: str = "asan") -> Path:
 
 
 if __name__ == "__main__":
-    print(build(sys.argv[1] if len(sys.argv) > 1 else "asan"))
+    print(build(sys.argv[1] if len(sys.argv) > 1 else "asan", sys.argv[2] if len(sys.argv) > 2 else "run"))

@@ -150,6 +150,39 @@ def test_lazy_decision_matches_exact_support(tfsm, graphs, case):
     assert [r.frequent for r in single] == [r.frequent for r in res[:40]]
 
 
+@pytest.mark.parametrize("case", ["cfg1", "el3", "clique", "cfg2_t9000"])
+def test_level_calls_with_parent_domains_keep_results(tfsm, graphs, case):
+    """tfsm_evaluate_level, level by level: a pattern whose DFS-code prefix was evaluated by the
+    previous call starts from the prefix's kept domains; exact MNI counts equal the reference's and
+    lazy decisions equal exact support >= tau."""
+    want = golden_mni(case)
+    tau = CASES[case]["tau"]
+    by_len: dict[int, list[str]] = {}
+    for k in want:
+        by_len.setdefault(len(k.split()), []).append(k)
+    g = graphs(case)
+    prev, prev_idx, used = None, {}, 0
+    for n_codes in sorted(by_len):
+        keys = by_len[n_codes]
+        parents = []
+        for k in keys:
+            i = prev_idx.get(" ".join(k.split()[:-1]))
+            parents.append((prev, i) if prev is not None and i is not None else None)
+        used += sum(p is not None for p in parents)
+        pats = [tfsm.parse_key(k) for k in keys]
+        res, dom = g.evaluate_level(pats, parents=parents, flags=tfsm.FLAG_EXACT, keep=True)
+        assert [r.mni for r in res] == [want[k] for k in keys]
+        lazy, none = g.evaluate_level(pats, parents=parents)
+        assert none is None
+        assert [r.frequent for r in lazy] == [min(want[k]) >= tau for k in keys]
+        if prev is not None:
+            prev.close()
+        prev, prev_idx = dom, {k: i for i, k in enumerate(keys)}
+    if prev is not None:
+        prev.close()
+    assert used > 0
+
+
 def test_forced_splits_keep_exact_supports(tfsm, graphs):
     case = "el3"
     want = golden_mni(case)

@@ -57,3 +57,25 @@ def test_emulated_kernels_match_reference(emu, case, opt, tmp_path):
                        env=env)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
     assert set(read_results(out)) == golden_pattern_set(case)
+
+
+@pytest.fixture(scope="module")
+def abi_emu():
+    import build_emu
+
+    return build_emu.build("asan", "abi")
+
+
+@pytest.mark.parametrize("case", SMALL)
+def test_emulated_level_calls_with_parent_domains_match_golden_mni(abi_emu, case):
+    """tfsm_evaluate_level, level by level with exact MNI: every pattern whose DFS-code prefix was
+    evaluated by the previous call starts from the prefix's kept domains, and every count equals the
+    reference's; bad parents (not a sub-pattern, index out of range, another graph) are rejected."""
+    c = CASES[case]
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=1:abort_on_error=1", UBSAN_OPTIONS="halt_on_error=1")
+    r = subprocess.run([str(abi_emu), str(GOLDEN / c["file"]), str(c["tau"]), str(GOLDEN / f"{case}.mni.txt")],
+                       capture_output=True, text=True, timeout=600, env=env)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
+    last = r.stdout.strip().splitlines()[-1]
+    assert last.startswith("ok"), last
+    assert int(last.split("with_parent=")[1].split()[0]) > 0
