@@ -19,6 +19,11 @@
 #include "noalloc.hpp"
 
 struct tfsm_graph {
+    uint64_t serial = next_serial();  // unique per handle (an address may be reused after a free)
+    static uint64_t next_serial() {
+        static std::atomic<uint64_t> n(0);
+        return ++n;
+    }
     tfsm::LgGraph lg;
     std::unique_ptr<tfsm::GpuEngine> eng;
     tfsm::EngineOptions opt;  // tuning knobs (tfsm_set_options), order policy and cost model
@@ -35,7 +40,7 @@ struct tfsm_cost_model {
 };
 
 struct tfsm_domains {
-    const tfsm_graph *g = nullptr;
+    uint64_t graph = 0;               // serial of the graph whose pools these are
     tfsm::Level lvl;                  // the call's bitmap pools
     std::vector<tfsm::Pattern> pats;  // by position in the call (for the sub-pattern check)
     std::vector<int> slot;            // by position in the call: index in lvl, or -1 (not evaluated)
@@ -246,7 +251,7 @@ int tfsm_evaluate_level(tfsm_graph *g, const tfsm_pattern *patterns, int32_t n, 
         if (!g || (n > 0 && (!patterns || !results)) || n < 0) return fail(TFSM_ERR_ARG, "null argument");
         std::lock_guard<std::mutex> lk(g->mu);
         std::unique_ptr<tfsm_domains> keep(new tfsm_domains);
-        keep->g = g;
+        keep->graph = g->serial;
         keep->pats.resize((size_t)n);
         keep->slot.assign((size_t)n, -1);
         std::vector<const tfsm::Pattern *> ptrs;
@@ -261,7 +266,7 @@ int tfsm_evaluate_level(tfsm_graph *g, const tfsm_pattern *patterns, int32_t n, 
             if (ok && parents && parents[i].domains) {
                 const tfsm_domains *d = parents[i].domains;
                 const int j = parents[i].index;
-                if (d->g != g) {
+                if (d->graph != g->serial) {
                     ok = false;
                     why = "parent domains belong to another graph";
                 } else if (j < 0 || (size_t)j >= d->slot.size() || d->slot[(size_t)j] < 0) {
