@@ -81,7 +81,7 @@ def test_ctypes_structs_match_the_header_layout(tfsm, tmp_path):
         pytest.skip("no C compiler")
     structs = {"tfsm_dfs_code": tfsm.DfsCode, "tfsm_pattern": tfsm.PatternC, "tfsm_result": tfsm.ResultC,
                "tfsm_graph_info_t": tfsm.GraphInfoC, "tfsm_mine_stats": tfsm.MineStatsC,
-               "tfsm_options": tfsm.OptionsC}
+               "tfsm_options": tfsm.OptionsC, "tfsm_parent": tfsm.ParentC}
     lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "tfsm.h"', "int main(void) {"]
     for cname, cls in structs.items():
         lines.append(f'    printf("{cname} %zu\\n", sizeof({cname}));')
