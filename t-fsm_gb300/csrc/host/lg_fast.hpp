@@ -11,6 +11,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cstdlib>
 #include <atomic>
 #include <condition_variable>
 #include <cstdint>
@@ -28,7 +29,16 @@ namespace tfsm {
 
 namespace fast {
 
-inline int default_threads() { return (int)std::max(1u, std::min(64u, std::thread::hardware_concurrency())); }
+// Host threads for parallel host work: TFSM_HOST_THREADS when set (1..64), else the cores (<= 64).
+inline int default_threads() {
+    static const int n = []() {
+        const char *env = std::getenv("TFSM_HOST_THREADS");
+        const int want = env ? std::atoi(env) : 0;
+        if (want >= 1) return std::min(64, want);
+        return (int)std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    }();
+    return n;
+}
 
 // Process-wide workers for the loader's parallel passes (creating a thread per core for each
 // pass costs about as much as a pass on a 1 M-edge graph).  One job at a time: callers are

@@ -6,6 +6,7 @@
 #include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
+#include <exception>
 #include <fstream>
 #include <functional>
 #include <memory>
@@ -48,24 +49,113 @@ class Pool {
     int threads_;
 };
 
-// Extends every frequent node (rightmost extension + canonical check), in parallel over parents.
-void extend_all(const std::vector<Node> &level, const ExtendContext &ctx, Pool &pool,
-                std::vector<std::vector<Pattern>> &kids) {
-    kids.assign(level.size(), {});
-    std::atomic<size_t> next(0);
-    const std::function<void()> work = [&]() {
-        for (;;) {
-            const size_t i = next.fetch_add(1);
-            if (i >= level.size()) break;
-            if (!level[i].res.frequent) continue;
-            extend_pattern(level[i].pat, ctx, kids[i]);
+// A level's host growth, computed while the GPU evaluates the level.  A pattern's children
+// (rightmost extension + canonical check), its canonical key and vertex order, and its children's
+// one-edge-smaller sub-patterns depend only on the pattern, not on its support: a helper thread
+// computes them on the host workers for every candidate while the level's engine calls run.  Once
+// the results are in (`publish`), candidates that turned out infrequent are skipped; the rest are
+// finished by `join`.  Candidates already decided infrequent (pruned) are never extended.
+class Growth {
+  public:
+    Growth(const std::vector<Node> &level, const ExtendContext &ctx, Pool &pool, bool want_subs)
+        : ctx_(ctx), pool_(pool), want_subs_(want_subs) {
+        const size_t n = level.size();
+        pats_.reserve(n);
+        for (auto &nd : level) {
+            pats_.push_back(nd.pat);
+            pruned_.push_back(nd.pruned ? 1 : 0);
         }
-    };
-    size_t n_freq = 0;
-    for (auto &nd : level) n_freq += nd.res.frequent ? 1 : 0;
-    if (n_freq <= 2) work();  // not worth waking the workers
-    else pool.run(work);
-}
+        frequent_.assign(n, 0);
+        kids_.assign(n, {});
+        extended_.assign(n, 0);
+        keys_.assign(n, {});
+        orders_.assign(n, {});
+        subs_.assign(n, {});
+        subs_done_.assign(n, 0);
+        th_ = std::thread([this]() {
+            try {
+                work();
+            } catch (...) {
+                err_ = std::current_exception();
+            }
+        });
+    }
+    ~Growth() {
+        if (th_.joinable()) {
+            known_.store(true, std::memory_order_release);  // every frequent_ flag still 0: stop early
+            th_.join();
+        }
+    }
+    Growth(const Growth &) = delete;
+    Growth &operator=(const Growth &) = delete;
+
+    // The level's results are in (candidates beyond `level`'s size were dropped): wait for the
+    // helper, then finish what it skipped for frequent candidates.
+    void join(const std::vector<Node> &level) {
+        for (size_t i = 0; i < pats_.size(); ++i) frequent_[i] = i < level.size() && level[i].res.frequent ? 1 : 0;
+        known_.store(true, std::memory_order_release);
+        th_.join();
+        if (err_) std::rethrow_exception(err_);
+        for (size_t i = 0; i < pats_.size(); ++i)
+            if (frequent_[i]) {
+                if (!extended_[i]) extend(i);
+                if (want_subs_ && !subs_done_[i]) subs(i);
+            }
+    }
+
+    // after join: the children of candidate i (frequent ones only), moved out
+    std::vector<Pattern> take_kids(size_t i) { return frequent_[i] ? std::move(kids_[i]) : std::vector<Pattern>(); }
+    const std::string &key(size_t i) const { return keys_[i]; }
+    const std::vector<int> &order(size_t i) const { return orders_[i]; }
+    const std::vector<SubPattern> &child_subs(size_t i, size_t j) const { return subs_[i][j]; }
+
+  private:
+    bool dropped(size_t i) const {  // known to be infrequent
+        return pruned_[i] || (known_.load(std::memory_order_acquire) && !frequent_[i]);
+    }
+    void extend(size_t i) {
+        kids_[i].clear();
+        extend_pattern(pats_[i], ctx_, kids_[i]);
+        extended_[i] = 1;
+    }
+    void subs(size_t i) {
+        subs_[i].resize(kids_[i].size());
+        for (size_t j = 0; j < kids_[i].size(); ++j) one_edge_smaller(kids_[i][j], subs_[i][j]);
+        subs_done_[i] = 1;
+    }
+    void work() {
+        const size_t n = pats_.size();
+        std::atomic<size_t> k(0);
+        const std::function<void()> first = [&]() {
+            for (size_t i; (i = k.fetch_add(1)) < n;) {
+                if (pruned_[i]) continue;
+                if (want_subs_) keys_[i] = canonical_key(small_graph(pats_[i]), &orders_[i]);
+                if (!dropped(i)) extend(i);
+            }
+        };
+        pool_.run(first);
+        if (!want_subs_) return;
+        k.store(0);
+        const std::function<void()> second = [&]() {
+            for (size_t i; (i = k.fetch_add(1)) < n;)
+                if (extended_[i] && !dropped(i)) subs(i);
+        };
+        pool_.run(second);
+    }
+
+    const ExtendContext &ctx_;
+    Pool &pool_;
+    const bool want_subs_;
+    std::vector<Pattern> pats_;
+    std::vector<char> pruned_, frequent_, extended_, subs_done_;
+    std::atomic<bool> known_{false};
+    std::vector<std::vector<Pattern>> kids_;
+    std::vector<std::string> keys_;
+    std::vector<std::vector<int>> orders_;
+    std::vector<std::vector<std::vector<SubPattern>>> subs_;
+    std::exception_ptr err_;
+    std::thread th_;  // joined in the destructor, before the members above go
+};
 
 }  // namespace
 
@@ -73,8 +163,10 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
     auto t0 = std::chrono::steady_clock::now();
     out.clear();
     st = MineStats();
-    const int threads = opt.host_threads > 0 ? opt.host_threads : (int)std::max(1u, std::thread::hardware_concurrency());
-    Pool pool(threads);
+    const int threads = opt.host_threads > 0 ? opt.host_threads : fast::default_threads();
+    // growth runs beside the engine calls: two threads fewer, so the host thread that prepares
+    // and launches the device work keeps a core
+    Pool pool(std::max(1, threads - 2));
     ExtendContext ctx;
     ctx.freq_elabels = g.freq_elabels;
     ctx.max_nodes = opt.max_nodes;
@@ -247,85 +339,78 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
         nd.pat.push(DfsCode{0, 1, ep.la, ep.el, ep.lb});
         level.push_back(std::move(nd));
     }
+    const bool want_subs = opt.subpattern_pruning;
+    std::unique_ptr<Growth> growth(new Growth(level, ctx, pool, want_subs));
     evaluate_level(level, std::vector<int>(level.size(), -1), nullptr);
     for (auto &nd : level) {
         if (!opt.engine.exact) nd.res.frequent = true;
         else nd.res.frequent = nd.res.support >= tau;
     }
+    growth->join(level);
     st.levels = level.empty() ? 0 : 1;
     while (!level.empty()) {
         for (auto &nd : level)
             if (nd.res.frequent) out.push_back({nd.pat, nd.res});
         auto te = std::chrono::steady_clock::now();
-        std::vector<std::vector<Pattern>> kids;
-        extend_all(level, ctx, pool, kids);
         std::vector<Node> next;
         std::vector<int> parent_of;
-        for (size_t i = 0; i < kids.size(); ++i)
-            for (auto &k : kids[i]) {
+        std::vector<size_t> child_no;  // by child: its position among its parent's children
+        for (size_t i = 0; i < level.size(); ++i) {
+            std::vector<Pattern> kids = growth->take_kids(i);
+            for (size_t j = 0; j < kids.size(); ++j) {
                 Node nd;
-                nd.pat = std::move(k);
+                nd.pat = std::move(kids[j]);
                 next.push_back(std::move(nd));
                 parent_of.push_back((int)i);
+                child_no.push_back(j);
             }
-        if (opt.subpattern_pruning && !next.empty()) {
-            // Keys (and canonical vertex orders) of this level's evaluated patterns; then, for every
-            // child, its one-edge-smaller sub-patterns:
+        }
+        if (want_subs && !next.empty()) {
+            // For every child, its one-edge-smaller sub-patterns (keys and canonical vertex orders
+            // from the growth), matched against this level's evaluated patterns:
             //   * one evaluated and infrequent: the child is infrequent (MNI is anti-monotone);
             //   * one missing from a complete level (single edge label): infrequent as well;
             //   * the frequent ones bound the child's domains (up to kMaxPushSources of them).
-            std::vector<std::string> keys(level.size());
-            std::vector<std::vector<int>> orders(level.size());
-            {
-                std::atomic<size_t> k(0);
-                const std::function<void()> work = [&]() {
-                    for (size_t i; (i = k.fetch_add(1)) < level.size();)
-                        if (!level[i].pruned) keys[i] = canonical_key(small_graph(level[i].pat), &orders[i]);
-                };
-                pool.run(work);
-            }
             std::unordered_map<std::string, size_t> evaluated;
             for (size_t i = 0; i < level.size(); ++i)
-                if (!level[i].pruned) evaluated.emplace(keys[i], i);
-            std::atomic<size_t> k(0);
-            const std::function<void()> work = [&]() {
-                std::vector<SubPattern> subs;
-                for (size_t i; (i = k.fetch_add(1)) < next.size();) {
-                    Node &child = next[i];
-                    one_edge_smaller(child.pat, subs);
-                    for (auto &sp : subs) {
-                        auto it = evaluated.find(sp.key);
-                        if (it == evaluated.end()) {
-                            if (prune_subpatterns) child.pruned = true;
-                            if (child.pruned) break;
-                            continue;
-                        }
-                        const Node &sn = level[it->second];
-                        if (!sn.res.frequent) {
-                            child.pruned = true;
-                            break;
-                        }
-                        if (it->second == (size_t)parent_of[i] || !sn.lvl) continue;
-                        if (child.push.size() >= (size_t)kMaxPushSources) continue;
-                        PushSource src;
-                        src.at = LevelRef{sn.lvl, sn.idx};
-                        for (int u = 0; u < 16; ++u) src.vertex[u] = -1;
-                        const std::vector<int> &ord = orders[it->second];
-                        for (int u = 0; u < child.pat.size() && u < 16; ++u)
-                            if (sp.pos_of[(size_t)u] >= 0) src.vertex[u] = (int8_t)ord[(size_t)sp.pos_of[(size_t)u]];
-                        child.push.push_back(src);
+                if (!level[i].pruned) evaluated.emplace(growth->key(i), i);
+            for (size_t i = 0; i < next.size(); ++i) {
+                Node &child = next[i];
+                for (const SubPattern &sp : growth->child_subs((size_t)parent_of[i], child_no[i])) {
+                    auto it = evaluated.find(sp.key);
+                    if (it == evaluated.end()) {
+                        if (prune_subpatterns) child.pruned = true;
+                        if (child.pruned) break;
+                        continue;
                     }
-                    if (child.pruned) child.push.clear();
+                    const Node &sn = level[it->second];
+                    if (!sn.res.frequent) {
+                        child.pruned = true;
+                        break;
+                    }
+                    if (it->second == (size_t)parent_of[i] || !sn.lvl) continue;
+                    if (child.push.size() >= (size_t)kMaxPushSources) continue;
+                    PushSource src;
+                    src.at = LevelRef{sn.lvl, sn.idx};
+                    for (int u = 0; u < 16; ++u) src.vertex[u] = -1;
+                    const std::vector<int> &ord = growth->order(it->second);
+                    for (int u = 0; u < child.pat.size() && u < 16; ++u)
+                        if (sp.pos_of[(size_t)u] >= 0) src.vertex[u] = (int8_t)ord[(size_t)sp.pos_of[(size_t)u]];
+                    child.push.push_back(src);
                 }
-            };
-            pool.run(work);
+                if (child.pruned) child.push.clear();
+            }
         }
         st.extend_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - te).count();
         if (next.empty()) break;
+        growth.reset(new Growth(next, ctx, pool, want_subs));  // runs during the next level's engine calls
         prev_levels = std::move(cur_levels);
         cur_levels.clear();
         evaluate_level(next, parent_of, &level);
         prev_levels.clear();  // parents' device memory
+        const auto tj = std::chrono::steady_clock::now();
+        growth->join(next);
+        st.extend_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tj).count();
         level = std::move(next);
         st.levels++;
     }

@@ -21,7 +21,7 @@ struct MineOptions {
     int tau = 1;
     int max_nodes = -1;
     bool batched = true;
-    int host_threads = 0;  // threads for extension + canonical checks (0: hardware concurrency)
+    int host_threads = 0;  // threads for extension + canonical checks (0: TFSM_HOST_THREADS or the cores)
     bool subpattern_pruning = true;  // Apriori: a child with an infrequent one-edge-smaller sub-pattern is infrequent
     EngineOptions engine;
     // per growth level (index = pattern edges): options for that level's engine calls, when set
