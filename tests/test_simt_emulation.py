@@ -99,3 +99,19 @@ def test_emulated_mining_is_race_free_under_thread_sanitizer(tmp_path):
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
     assert "ThreadSanitizer" not in r.stderr
     assert set(read_results(out)) == golden_pattern_set("clique")
+
+
+@pytest.mark.parametrize("case", ["clique", "quirk_elabels"])
+@pytest.mark.parametrize("limit", ["0.000001", "0.2"])  # before the first call; after some calls
+def test_emulated_time_limit_stops_cleanly(emu, case, limit, tmp_path):
+    """The time limit drops a level's remaining candidates while their growth runs on the helper
+    thread: the run ends cleanly (sanitizers on) and reports a subset of the reference's patterns."""
+    c = CASES[case]
+    out = tmp_path / "res.txt"
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=1:abort_on_error=1", UBSAN_OPTIONS="halt_on_error=1",
+               TFSM_HOST_THREADS="3")
+    r = subprocess.run([str(emu), "-file", str(GOLDEN / c["file"]), "-freq", str(c["tau"]), "-maxNodes",
+                        str(c["max_nodes"]), "-out", str(out), "-max-batch", "2", "-time-limit", limit],
+                       capture_output=True, text=True, timeout=600, env=env)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    assert set(read_results(out)) <= golden_pattern_set(case)
