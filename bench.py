@@ -34,7 +34,7 @@ PKG = ROOT / "t-fsm_gb300"
 METRIC = "FSM wall-clock & pattern-support evals/s: batched vs plain GPU, identical output"
 
 WORKLOADS = {
-    # BASELINE config 2: plain GPU drop-in at medium scale
+    # plain GPU drop-in at medium scale (the headline workload)
     "cfg2_t9000": dict(gen=dict(n=100000, mean=22, gamma=2.2, max_degree=1400, labels=29, zipf=1.2, elabels=1,
                                 seed=1), tau=9000, max_nodes=5,
                        desc="Chung-Lu 100k vertices / 1.1M edges (gamma 2.2), 29 Zipf(1.2) labels, tau=9000, "
