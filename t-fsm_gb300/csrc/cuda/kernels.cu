@@ -106,11 +106,13 @@ __device__ __forceinline__ uint32_t find_item(const uint64_t *__restrict__ prefi
 // Bit `lane` of word `word` of a source's final domain (dom & ~failed) at reference `ref`.
 __device__ __forceinline__ bool source_bit(const SourceLevel *__restrict__ srcs, uint32_t n_srcs, int64_t ref,
                                            uint32_t word, uint32_t lane) {
+    // A restriction only removes candidates, so one that cannot be read is skipped (checked
+    // builds also record it): results never depend on it.
     const uint64_t slot = (uint64_t)ref >> kSrcShift;
     const uint64_t o = ((uint64_t)ref & kSrcMask) + word;
-    if (!TFSM_IN(32, slot, n_srcs)) return true;
+    if (!TFSM_IN(32, slot, n_srcs) || slot >= n_srcs) return true;
     const SourceLevel S = srcs[slot];
-    if (!TFSM_IN(39, o, S.words)) return true;
+    if (!TFSM_IN(39, o, S.words) || o >= S.words) return true;
     const uint32_t w = __ldg(S.dom + o) & ~__ldg(S.failed + o);
     return (w >> lane) & 1u;
 }
