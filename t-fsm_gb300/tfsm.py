@@ -224,7 +224,10 @@ class Domains:
             self._h = None
 
     def __del__(self):
-        self.close()
+        try:
+            self.close()
+        except Exception:  # interpreter shutdown: the library may already be gone
+            pass
 
     def __enter__(self):
         return self
