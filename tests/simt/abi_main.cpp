@@ -5,10 +5,12 @@
 // pattern whose DFS-code prefix (its code minus the last edge: the same vertex numbering, one edge
 // less) was evaluated by the previous level's call starts from that prefix's kept domains. Every
 // pattern's exact MNI counts must equal the golden ones. Then the parent checks: a parent that is
-// not a sub-pattern, an index out of range and domains of another graph give TFSM_ERR_ARG.
+// not a sub-pattern (other labels, more vertices), an index out of range and domains of another
+// graph give TFSM_ERR_ARG; a pattern may be its own parent.
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
+#include <iterator>
 #include <map>
 #include <sstream>
 #include <string>
@@ -123,6 +125,18 @@ int main(int argc, char **argv) {
                    r.status == TFSM_ERR_ARG,
                "a parent with other labels is TFSM_ERR_ARG");
         break;
+    }
+    if (levels.size() > 1) {  // a larger pattern is no sub-pattern of a single edge
+        const std::vector<Golden> &two = std::next(levels.begin())->second;
+        std::vector<tfsm_pattern> p2(two.size());
+        for (size_t i = 0; i < two.size(); ++i) p2[i] = tfsm_pattern{(int32_t)two[i].codes.size(), two[i].codes.data()};
+        tfsm_domains *d2 = nullptr;
+        tfsm_result r2;
+        expect(tfsm_evaluate_level(g, p2.data(), 1, tau, 0, nullptr, &r2, &d2) == TFSM_OK && d2, "second-level call");
+        tfsm_parent big{d2, 0};
+        expect(tfsm_evaluate_level(g, p1.data(), 1, tau, 0, &big, &r, nullptr) == TFSM_OK && r.status == TFSM_ERR_ARG,
+               "a larger parent is TFSM_ERR_ARG");
+        tfsm_domains_free(d2);
     }
     expect(tfsm_evaluate_level(g, p1.data(), 1, tau, TFSM_FLAG_EXACT, &self, &r, nullptr) == TFSM_OK &&
                r.status == TFSM_OK && (size_t)r.n_vertices == one[0].mni.size() && r.mni[0] == one[0].mni[0],
