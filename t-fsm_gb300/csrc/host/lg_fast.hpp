@@ -40,10 +40,12 @@ inline int default_threads() {
     return n;
 }
 
-// Process-wide workers for the loader's parallel passes (creating a thread per core for each
-// pass costs about as much as a pass on a 1 M-edge graph).  One job at a time: callers are
-// serialised on `job_mu`; a job runs `tasks` calls of `fn(task)` spread over the workers and the
-// caller.
+// Process-wide workers for the host's parallel passes (creating a thread per core for each pass
+// costs about as much as a pass on a 1 M-edge graph).  One job at a time: callers are serialised
+// on `job_mu`; a job runs `tasks` calls of `fn(task)` spread over the workers and the caller.
+// Each job's state (function, task count, claim and completion counters) lives in its own record,
+// and a job ends only when every task is done and no worker is still inside it, so a worker
+// leaving one job can never claim a task of the next.
 class Workers {
   public:
     static Workers &get() {
@@ -52,19 +54,17 @@ class Workers {
     }
     void run(size_t tasks, const std::function<void(size_t)> &fn) {
         std::lock_guard<std::mutex> job(job_mu_);
+        Job j(&fn, tasks);
         {
             std::lock_guard<std::mutex> lk(mu_);
-            fn_ = &fn;
-            tasks_ = tasks;
-            next_.store(0);
-            done_ = 0;
+            job_ = &j;
             ++gen_;
         }
         cv_.notify_all();
-        drain();
+        drain(j);
         std::unique_lock<std::mutex> lk(mu_);
-        done_cv_.wait(lk, [&]() { return done_ == tasks_; });
-        fn_ = nullptr;
+        done_cv_.wait(lk, [&]() { return j.done.load() == j.tasks && active_ == 0; });
+        job_ = nullptr;
     }
     ~Workers() {
         {
@@ -76,34 +76,46 @@ class Workers {
     }
 
   private:
+    struct Job {
+        Job(const std::function<void(size_t)> *f, size_t n) : fn(f), tasks(n) {}
+        const std::function<void(size_t)> *fn;
+        const size_t tasks;
+        std::atomic<size_t> next{0}, done{0};
+    };
     explicit Workers(int n) {
         for (int i = 0; i < n; ++i) th_.emplace_back([this]() { loop(); });
     }
-    void drain() {
-        for (size_t k; (k = next_.fetch_add(1)) < tasks_;) {
-            (*fn_)(k);
-            std::lock_guard<std::mutex> lk(mu_);
-            if (++done_ == tasks_) done_cv_.notify_all();
+    void drain(Job &j) {
+        for (size_t k; (k = j.next.fetch_add(1)) < j.tasks;) {
+            (*j.fn)(k);
+            if (j.done.fetch_add(1) + 1 == j.tasks) {
+                std::lock_guard<std::mutex> lk(mu_);
+                done_cv_.notify_all();
+            }
         }
     }
     void loop() {
         uint64_t seen = 0;
         for (;;) {
+            Job *j = nullptr;
             {
                 std::unique_lock<std::mutex> lk(mu_);
-                cv_.wait(lk, [&]() { return quit_ || gen_ != seen; });
+                cv_.wait(lk, [&]() { return quit_ || (job_ != nullptr && gen_ != seen); });
                 if (quit_) return;
                 seen = gen_;
+                j = job_;
+                ++active_;
             }
-            drain();
+            drain(*j);
+            std::lock_guard<std::mutex> lk(mu_);
+            if (--active_ == 0) done_cv_.notify_all();
         }
     }
     std::vector<std::thread> th_;
     std::mutex job_mu_, mu_;
     std::condition_variable cv_, done_cv_;
-    const std::function<void(size_t)> *fn_ = nullptr;
-    std::atomic<size_t> next_{0};
-    size_t tasks_ = 0, done_ = 0;
+    Job *job_ = nullptr;  // the running job (guarded by mu_)
+    size_t active_ = 0;   // workers inside job_ (guarded by mu_)
     uint64_t gen_ = 0;
     bool quit_ = false;
 };
