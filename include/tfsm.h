@@ -36,7 +36,7 @@ extern "C" {
 /* flags */
 #define TFSM_FLAG_EXACT 1u    /* exact MNI per vertex: no early exit at tau */
 #define TFSM_FLAG_PLAIN 2u    /* tfsm_mine: one engine call per candidate pattern (unbatched) */
-#define TFSM_FLAG_NO_SPLIT 4u /* disable splitting of long searches (hub tasks) */
+#define TFSM_FLAG_NO_SPLIT 4u /* no work sharing: every search runs to its end on one team */
 #define TFSM_FLAG_NO_SUBPATTERN_PRUNING 8u /* tfsm_mine: search every candidate, even one with an
                                               infrequent one-edge-smaller sub-pattern */
 
@@ -91,6 +91,10 @@ typedef struct {
                                          pattern edges; 0 unused) */
     uint64_t pruned;       /* candidates decided infrequent by an infrequent sub-pattern (counted in
                               evaluations and by_filter; no engine call) */
+    uint64_t split_searches; /* searches that shared work through the device ring */
+    uint64_t split_tasks;  /* tasks they shared */
+    uint64_t intersections; /* set intersections of the searches: one per chunk of up to 32 anchor
+                               candidates and backward neighbour (the anchor's own range included) */
 } tfsm_mine_stats;
 
 /* Load a .lg graph and prune it for threshold `tau` (label frequency, edge-label frequency and
@@ -158,20 +162,29 @@ int tfsm_mine(tfsm_graph *g, int32_t tau, int32_t max_nodes, uint32_t flags, con
 
 /* Tuning knobs of the GPU search (no counterpart in the reference, whose only knobs are the
  * compile-time TIMEOUT_THRESHOLD / DECOMPOSE_TIME_THRESHOLD of parallel/global.h:30-33).
- * They change speed only, never results. */
+ * They change speed only, never results.
+ *
+ * Versioned by size: set struct_size = sizeof(tfsm_options) before calling tfsm_get_options or
+ * tfsm_set_options.  The library reads and writes only the first struct_size bytes, so a caller
+ * built against an older header (a shorter struct, fields only ever added at the end) keeps
+ * working; a struct_size below TFSM_OPTIONS_MIN_SIZE or above the library's own size is rejected
+ * with TFSM_ERR_ARG. */
 typedef struct {
-    uint32_t step_budget;   /* 32-candidate chunks a search may evaluate before its unexplored
-                               branches (at every depth) become split tasks (0: never split) */
-    uint32_t split_slice;   /* adjacency positions per split task (>= 32) */
+    uint32_t struct_size;   /* sizeof(tfsm_options) as the caller compiled it */
+    uint32_t step_budget;   /* 32-candidate chunks a search may take in the first search pass of
+                               an engine call before it is set aside; each later pass allows 8x
+                               more and the last (the fourth) has no limit, so the quick searches
+                               of every candidate run first (0: one pass without limit) */
+    uint32_t split_slice;   /* least adjacency positions per part when a search of the last pass
+                               shares out its current depth on the device work ring (>= 1) */
     uint32_t chunk_words;   /* 32-bit domain-bitmap words per search work item (>= 1) */
     uint32_t refine_rounds; /* arc-consistency passes for patterns that need a search (>= 1) */
     uint32_t max_batch;     /* tfsm_mine: most patterns per engine call (>= 1) */
-    uint32_t split_rounds;  /* split rounds launched right after the search pass (1..64); later rounds
-                               run while tasks remain (64 rounds at most, the last without a budget) */
+    uint32_t hub_span;      /* a search whose first depth has more adjacency positions than this
+                               (a hub vertex's label range) shares it out at once ... */
+    uint32_t hub_parts;     /* ... in this many parts, one of them kept (1..32; 1: off) */
     double time_limit_s;    /* tfsm_mine: stop between engine calls after this many seconds (0: none);
                                the run is then reported incomplete */
-    uint32_t round_budget;  /* chunk evaluations of a split task before its own remainder is split
-                               again (>= 1) */
     uint32_t search_lanes;  /* lanes per search: 8 (default: four searches per warp, for calls with
                                several patterns of at most 8 vertices) or 32; 0 means 32 */
     uint32_t rank_window;   /* patterns per window of the search order: within a window every
@@ -181,7 +194,14 @@ typedef struct {
                                makes the following calls take proportionally fewer patterns (at
                                least 4); full calls that finish sooner double it again, up to
                                max_batch (default 2; 0: always max_batch) */
+    uint32_t isect_ratio;   /* intersection form of a search step against a further backward
+                               neighbour: its candidate run is merged (read once, coalesced) when it
+                               is at most isect_ratio times the step's survivors, and probed by
+                               galloping search otherwise (>= 1; the autotuner tries 4, 16, 64) */
+    uint32_t reserved;      /* 0 */
 } tfsm_options;
+
+#define TFSM_OPTIONS_MIN_SIZE 64u /* the first versioned layout: struct_size .. reserved */
 
 int tfsm_get_options(const tfsm_graph *g, tfsm_options *opt);
 int tfsm_set_options(tfsm_graph *g, const tfsm_options *opt);

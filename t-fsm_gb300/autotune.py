@@ -1,7 +1,8 @@
 """Autotuner of the engine's speed-only knobs, per growth level, keyed on the graph's label and
 degree statistics.
 
-The knobs (split budgets, split slice, work-item size, refinement rounds, split rounds) never
+The knobs (lanes per search, work-item size, merge/galloping switch ratio, teams per hub
+search, sharing budget and slice, refinement rounds) never
 change a result, only the work's shape; the best values depend on the pattern size (the growth
 level) and on the graph's degree and label distribution.  `tune()` runs complete mining runs of
 the caller's workload, one knob at a time (coordinate descent), and keeps for every level the
@@ -21,11 +22,11 @@ from typing import Callable
 SPACE = [
     ("search_lanes", [8, 32]),
     ("chunk_words", [1, 2]),
-    ("step_budget", [16, 8, 32, 64]),
-    ("round_budget", [32, 16, 64]),
-    ("split_slice", [64, 32, 128]),
+    ("isect_ratio", [16, 4, 64]),
+    ("hub_parts", [4, 1, 2, 8]),
+    ("step_budget", [64, 16, 256, 0]),
+    ("split_slice", [32, 64, 128]),
     ("refine_rounds", [1, 2]),
-    ("split_rounds", [2, 4]),
 ]
 
 

@@ -126,12 +126,12 @@ void fill_result(const tfsm::EvalResult &r, int n, tfsm_result *out) {
 }
 
 const char *const kKnobRules =
-    "split_slice must be >= 32; chunk_words, refine_rounds, max_batch and round_budget >= 1; split_rounds in 1..64; "
-    "time_limit_s and call_ms >= 0; search_lanes 8 or 32";
+    "split_slice, chunk_words, refine_rounds, max_batch and isect_ratio must be >= 1; hub_parts in 1..32; "
+    "time_limit_s and call_ms >= 0; search_lanes 0, 8 or 32";
 
 bool knobs_valid(const tfsm_options &o) {
-    return o.split_slice >= 32 && o.chunk_words >= 1 && o.refine_rounds >= 1 && o.max_batch >= 1 &&
-           o.split_rounds >= 1 && o.split_rounds <= 64 && o.round_budget >= 1 && o.time_limit_s >= 0 && o.call_ms >= 0 &&
+    return o.split_slice >= 1 && o.chunk_words >= 1 && o.refine_rounds >= 1 && o.max_batch >= 1 &&
+           o.hub_parts >= 1 && o.hub_parts <= 32 && o.isect_ratio >= 1 && o.time_limit_s >= 0 && o.call_ms >= 0 &&
            (o.search_lanes == 0 || o.search_lanes == 8 || o.search_lanes == 32);
 }
 
@@ -142,17 +142,51 @@ void apply_knobs(const tfsm_options &o, tfsm::EngineOptions &e) {
     e.chunk_words = o.chunk_words;
     e.refine_rounds = o.refine_rounds;
     e.max_batch = o.max_batch;
-    e.split_rounds = o.split_rounds;
-    e.round_budget = o.round_budget;
+    e.hub_span = o.hub_span;
+    e.hub_parts = o.hub_parts;
     e.search_lanes = o.search_lanes == 0 ? 32 : o.search_lanes;
     e.rank_window = o.rank_window;
     e.call_ms = o.call_ms;
+    e.isect_ratio = o.isect_ratio;
 }
+
+// The engine's knobs as a full tfsm_options.
+tfsm_options knobs_of(const tfsm::EngineOptions &e) {
+    tfsm_options o;
+    std::memset(&o, 0, sizeof(o));
+    o.struct_size = sizeof(tfsm_options);
+    o.step_budget = e.step_budget;
+    o.split_slice = e.split_slice;
+    o.chunk_words = e.chunk_words;
+    o.refine_rounds = e.refine_rounds;
+    o.max_batch = e.max_batch;
+    o.hub_span = e.hub_span;
+    o.hub_parts = e.hub_parts;
+    o.time_limit_s = e.time_limit_s;
+    o.search_lanes = e.search_lanes;
+    o.rank_window = e.rank_window;
+    o.call_ms = e.call_ms;
+    o.isect_ratio = e.isect_ratio;
+    return o;
+}
+
+// A caller's options of struct_size bytes over the current ones (fields past struct_size keep
+// their values); false when struct_size is outside [TFSM_OPTIONS_MIN_SIZE, sizeof(tfsm_options)].
+bool read_options(const tfsm_options *in, const tfsm::EngineOptions &cur, tfsm_options &out) {
+    if (in->struct_size < TFSM_OPTIONS_MIN_SIZE || in->struct_size > sizeof(tfsm_options)) return false;
+    out = knobs_of(cur);
+    std::memcpy(&out, in, in->struct_size);
+    out.struct_size = sizeof(tfsm_options);
+    return true;
+}
+
+const char *const kSizeRule = "tfsm_options.struct_size must be set to sizeof(tfsm_options) (at least "
+                              "TFSM_OPTIONS_MIN_SIZE, at most the library's own size)";
 
 tfsm::EngineOptions engine_options(const tfsm_graph *g, uint32_t flags) {
     tfsm::EngineOptions o = g->opt;
     o.exact = (flags & TFSM_FLAG_EXACT) != 0;
-    if (flags & TFSM_FLAG_NO_SPLIT) o.step_budget = 0;
+    if (flags & TFSM_FLAG_NO_SPLIT) o.split = false;
     o.records = g->recording ? &g->records : nullptr;
     return o;
 }
@@ -363,6 +397,9 @@ int tfsm_mine(tfsm_graph *g, int32_t tau, int32_t max_nodes, uint32_t flags, con
             stats->complete = st.complete ? 1 : 0;
             for (size_t l = 0; l < st.level_ms.size() && l < TFSM_MAX_LEVELS; ++l) stats->level_ms[l] = st.level_ms[l];
             stats->pruned = st.pruned;
+            stats->split_searches = kt.split_groups;
+            stats->split_tasks = kt.split_tasks;
+            stats->intersections = kt.isects;
         }
         return TFSM_OK;
     });
@@ -371,17 +408,11 @@ int tfsm_mine(tfsm_graph *g, int32_t tau, int32_t max_nodes, uint32_t flags, con
 int tfsm_get_options(const tfsm_graph *g, tfsm_options *o) {
     return guarded([&]() -> int {
         if (!g || !o) return fail(TFSM_ERR_ARG, "null argument");
-        o->step_budget = g->opt.step_budget;
-        o->split_slice = g->opt.split_slice;
-        o->chunk_words = g->opt.chunk_words;
-        o->refine_rounds = g->opt.refine_rounds;
-        o->max_batch = g->opt.max_batch;
-        o->split_rounds = g->opt.split_rounds;
-        o->time_limit_s = g->opt.time_limit_s;
-        o->round_budget = g->opt.round_budget;
-        o->search_lanes = g->opt.search_lanes;
-        o->rank_window = g->opt.rank_window;
-        o->call_ms = g->opt.call_ms;
+        const uint32_t size = o->struct_size;
+        if (size < TFSM_OPTIONS_MIN_SIZE || size > sizeof(tfsm_options)) return fail(TFSM_ERR_ARG, kSizeRule);
+        const tfsm_options cur = knobs_of(g->opt);
+        std::memcpy(o, &cur, size);
+        o->struct_size = size;
         return TFSM_OK;
     });
 }
@@ -389,10 +420,12 @@ int tfsm_get_options(const tfsm_graph *g, tfsm_options *o) {
 int tfsm_set_options(tfsm_graph *g, const tfsm_options *o) {
     return guarded([&]() -> int {
         if (!g || !o) return fail(TFSM_ERR_ARG, "null argument");
-        if (!knobs_valid(*o)) return fail(TFSM_ERR_ARG, kKnobRules);
         std::lock_guard<std::mutex> lk(g->mu);
-        apply_knobs(*o, g->opt);
-        g->opt.time_limit_s = o->time_limit_s;
+        tfsm_options full;
+        if (!read_options(o, g->opt, full)) return fail(TFSM_ERR_ARG, kSizeRule);
+        if (!knobs_valid(full)) return fail(TFSM_ERR_ARG, kKnobRules);
+        apply_knobs(full, g->opt);
+        g->opt.time_limit_s = full.time_limit_s;
         return TFSM_OK;
     });
 }
@@ -401,30 +434,34 @@ int tfsm_set_level_options(tfsm_graph *g, int32_t level, const tfsm_options *o) 
     return guarded([&]() -> int {
         if (!g) return fail(TFSM_ERR_ARG, "null argument");
         if (level < 0 || level >= TFSM_MAX_LEVELS) return fail(TFSM_ERR_ARG, "level must be in 0..TFSM_MAX_LEVELS-1");
-        if (o && !knobs_valid(*o)) return fail(TFSM_ERR_ARG, kKnobRules);
         std::lock_guard<std::mutex> lk(g->mu);
+        tfsm_options full;
+        if (o && !read_options(o, g->opt, full)) return fail(TFSM_ERR_ARG, kSizeRule);
+        if (o && !knobs_valid(full)) return fail(TFSM_ERR_ARG, kKnobRules);
         if (level == 0) {
             g->level_opt.clear();
             return TFSM_OK;
         }
         if (g->level_opt.size() <= (size_t)level) g->level_opt.resize((size_t)level + 1);
-        g->level_opt[(size_t)level] = o ? std::make_pair(true, *o) : std::make_pair(false, tfsm_options{});
+        g->level_opt[(size_t)level] = o ? std::make_pair(true, full) : std::make_pair(false, tfsm_options{});
         return TFSM_OK;
     });
 }
 
 int tfsm_evaluate_support_noalloc(tfsm_graph *g, const tfsm_pattern *pattern, int32_t tau, uint32_t flags,
                                   tfsm_result *out) {
-    if (!g || !pattern || !out) return fail(TFSM_ERR_ARG, "null argument");
-    std::lock_guard<std::mutex> lk(g->mu);
-    const char *msg = "";
-    const int rc = tfsm::noalloc_evaluate(*g->eng, pattern, (uint32_t)std::max(tau, 0),
-                                          (flags & TFSM_FLAG_EXACT) != 0, out, msg);
-    if (rc != TFSM_OK) {
-        out->status = rc;
-        return fail(rc, msg);
-    }
-    return TFSM_OK;
+    return guarded([&]() -> int {
+        if (!g || !pattern || !out) return fail(TFSM_ERR_ARG, "null argument");
+        std::lock_guard<std::mutex> lk(g->mu);
+        const char *msg = "";
+        const int rc = tfsm::noalloc_evaluate(*g->eng, pattern, (uint32_t)std::max(tau, 0),
+                                              (flags & TFSM_FLAG_EXACT) != 0, out, msg);
+        if (rc != TFSM_OK) {
+            out->status = rc;
+            return fail(rc, msg);
+        }
+        return TFSM_OK;
+    });
 }
 
 const char *tfsm_last_error(void) { return g_err.c_str(); }

@@ -11,6 +11,8 @@
 #include "host/lg_graph.hpp"
 #include "host/pattern.hpp"
 
+struct CUstream_st;  // cudaStream_t without the CUDA runtime header
+
 namespace tfsm {
 
 namespace dev {
@@ -34,10 +36,17 @@ struct EvalResult {
 
 struct EngineOptions {
     bool exact = false;                // evaluate every candidate (exact MNI), no early exit
-    uint32_t step_budget = 16;         // chunk evaluations before a search is split (0: never)
-    uint32_t split_slice = 64;         // anchor positions per split task
-    uint32_t round_budget = 32;        // step budget of a split task (the 64th round has none)
-    uint32_t split_rounds = 2;         // split rounds launched without checking for remaining tasks
+    bool split = true;                 // long searches of the last pass share out work through the
+                                       //   device ring
+    uint32_t step_budget = 16;         // chunk evaluations a search may take in the first search pass
+                                       //   before it is set aside; 8x more in each later pass, no limit
+                                       //   in the last (0: one pass without limit)
+    uint32_t split_slice = 32;         // least anchor positions per shared part of the current depth
+    uint32_t hub_span = 4096;          // a search whose first depth has more anchor positions ...
+    uint32_t hub_parts = 4;            //   ... shares it out at once in this many parts (1: off)
+    uint32_t isect_ratio = 16;         // merge a further backward neighbour's candidate run when it
+                                       //   is at most this many times the step's survivors, else
+                                       //   galloping search
     uint32_t chunk_words = 1;          // bitmap words per search work item (x32 candidates)
     uint32_t search_lanes = 8;         // lanes per search: 32, or 8 (four searches per warp, used for
                                        //   calls with several patterns of at most 8 vertices)
@@ -66,13 +75,16 @@ struct KernelTimes {                   // accumulated device time (CUDA events),
     uint64_t search_calls = 0;         // search phases (k_search, plus k_split when splitting)
     uint64_t init_words = 0, refine_words = 0;  // bitmap words processed
     uint64_t search_bytes = 0;         // algorithmic bytes read by the search kernels
+    uint64_t isects = 0;               // set intersections (chunk x backward neighbour) of the searches
     uint64_t h2d_bytes = 0, d2h_bytes = 0;      // host<->device copies of the evaluations
-    static constexpr int kRoundSlots = 65;      // split rounds + one
-    uint64_t split_groups = 0;                  // searches handed to the split rounds
-    uint64_t deferred = 0;                      // searches left for another pass (buffers full)
+    uint64_t split_groups = 0;                  // searches that shared work
+    uint64_t split_tasks = 0;                   // tasks shared through the ring
+    uint64_t split_refused = 0;                 // donations refused (ring or group table full)
+    uint64_t wait_expired = 0;                  // teams that stopped waiting for work at the limit
+    uint64_t queue_max = 0;                     // deepest ring seen
+    uint64_t abandoned = 0;                     // searches set aside at a pass's step budget
+    uint64_t search_passes = 0;                 // search passes that ran (launches that had work)
     double order_ms = 0;                        // host + cost-model time spent choosing orders
-    uint64_t search_passes = 0;
-    uint64_t split_tasks[kRoundSlots] = {};     // tasks written for each split round
 };
 
 // Device memory of one evaluated batch; kept while the batch's patterns are parents.
@@ -123,8 +135,10 @@ public:
     const std::string &load_breakdown() const { return load_breakdown_; }  // engine construction phases
     int dense_label(int label) const;  // -1 when the label is not frequent
     uint32_t n_vertices() const;
+    void device_memory(size_t &free_bytes, size_t &total_bytes) const;  // of the engine's device
     // Read-only views used by the allocation-free entry point (noalloc.cu).
     int device() const;
+    CUstream_st *stream() const;                     // the engine's own (non-blocking) stream
     const dev::Graph &device_graph() const;
     int dense_edge_label(int label) const;           // -1 when the edge label is not frequent
     uint32_t label_first(int dense) const;           // first vertex id of a dense label
@@ -136,6 +150,7 @@ private:
     KernelTimes times_;
     double upload_ms_ = 0;
     std::string load_breakdown_;
+    uint32_t share_steps_ = 0;  // TFSM_SHARE_STEPS (tests): last-pass searches share work after this many steps
 };
 
 }  // namespace tfsm

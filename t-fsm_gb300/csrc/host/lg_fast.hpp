@@ -15,6 +15,7 @@
 #include <atomic>
 #include <condition_variable>
 #include <cstdint>
+#include <exception>
 #include <functional>
 #include <mutex>
 #include <cstring>
@@ -45,7 +46,8 @@ inline int default_threads() {
 // on `job_mu`; a job runs `tasks` calls of `fn(task)` spread over the workers and the caller.
 // Each job's state (function, task count, claim and completion counters) lives in its own record,
 // and a job ends only when every task is done and no worker is still inside it, so a worker
-// leaving one job can never claim a task of the next.
+// leaving one job can never claim a task of the next.  A task that throws still counts as done;
+// the job keeps the first exception and run() rethrows it once the job has ended.
 class Workers {
   public:
     static Workers &get() {
@@ -62,9 +64,12 @@ class Workers {
         }
         cv_.notify_all();
         drain(j);
-        std::unique_lock<std::mutex> lk(mu_);
-        done_cv_.wait(lk, [&]() { return j.done.load() == j.tasks && active_ == 0; });
-        job_ = nullptr;
+        {
+            std::unique_lock<std::mutex> lk(mu_);
+            done_cv_.wait(lk, [&]() { return j.done.load() == j.tasks && active_ == 0; });
+            job_ = nullptr;
+        }
+        if (j.error) std::rethrow_exception(j.error);
     }
     ~Workers() {
         {
@@ -81,13 +86,20 @@ class Workers {
         const std::function<void(size_t)> *fn;
         const size_t tasks;
         std::atomic<size_t> next{0}, done{0};
+        std::mutex err_mu;
+        std::exception_ptr error;  // the first exception a task threw
     };
     explicit Workers(int n) {
         for (int i = 0; i < n; ++i) th_.emplace_back([this]() { loop(); });
     }
     void drain(Job &j) {
         for (size_t k; (k = j.next.fetch_add(1)) < j.tasks;) {
-            (*j.fn)(k);
+            try {
+                (*j.fn)(k);
+            } catch (...) {
+                std::lock_guard<std::mutex> lk(j.err_mu);
+                if (!j.error) j.error = std::current_exception();
+            }
             if (j.done.fetch_add(1) + 1 == j.tasks) {
                 std::lock_guard<std::mutex> lk(mu_);
                 done_cv_.notify_all();

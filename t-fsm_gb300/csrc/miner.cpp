@@ -15,6 +15,8 @@
 #include <unordered_map>
 #include <unordered_set>
 
+#include <unistd.h>
+
 #include "host/lg_fast.hpp"
 #include "host/subpattern.hpp"
 
@@ -157,6 +159,16 @@ class Growth {
     std::thread th_;  // joined in the destructor, before the members above go
 };
 
+// Resident host memory of this process in MB (Linux; 0 elsewhere), for the verbose level lines.
+double host_rss_mb() {
+    FILE *f = std::fopen("/proc/self/statm", "r");
+    if (!f) return 0;
+    long pages = 0, resident = 0;
+    const int got = std::fscanf(f, "%ld %ld", &pages, &resident);
+    std::fclose(f);
+    return got == 2 ? (double)resident * (double)sysconf(_SC_PAGESIZE) / 1048576.0 : 0.0;
+}
+
 }  // namespace
 
 void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<MinedPattern> &out, MineStats &st) {
@@ -282,18 +294,16 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                                  now.phase_ms[0] - before.phase_ms[0], now.phase_ms[1] - before.phase_ms[1],
                                  now.phase_ms[2] - before.phase_ms[2], now.phase_ms[3] - before.phase_ms[3],
                                  now.phase_ms[4] - before.phase_ms[4], now.phase_ms[5] - before.phase_ms[5]);
-                    if (now.split_groups > before.split_groups) {
-                        std::fprintf(stderr, "          split: %llu searches, %llu passes, %llu deferred, tasks per round",
-                                     (unsigned long long)(now.split_groups - before.split_groups),
-                                     (unsigned long long)(now.search_passes - before.search_passes),
-                                     (unsigned long long)(now.deferred - before.deferred));
-                        int last = 0;
-                        for (int r = 0; r < KernelTimes::kRoundSlots; ++r)
-                            if (now.split_tasks[r] != before.split_tasks[r]) last = r;
-                        for (int r = 0; r <= last; ++r)
-                            std::fprintf(stderr, " %llu", (unsigned long long)(now.split_tasks[r] - before.split_tasks[r]));
-                        std::fprintf(stderr, "\n");
-                    }
+                    std::fprintf(stderr,
+                                 "          passes %llu (%llu searches set aside); shared: %llu searches, %llu tasks, "
+                                 "%llu refused, ring depth <= %llu, %llu waits expired\n",
+                                 (unsigned long long)(now.search_passes - before.search_passes),
+                                 (unsigned long long)(now.abandoned - before.abandoned),
+                                 (unsigned long long)(now.split_groups - before.split_groups),
+                                 (unsigned long long)(now.split_tasks - before.split_tasks),
+                                 (unsigned long long)(now.split_refused - before.split_refused),
+                                 (unsigned long long)now.queue_max,
+                                 (unsigned long long)(now.wait_expired - before.wait_expired));
                 }
                 for (size_t k = b0; k < b1; ++k) {
                     const size_t i = todo[k];
@@ -403,6 +413,14 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
         }
         st.extend_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - te).count();
         if (next.empty()) break;
+        if (verbose) {
+            size_t pruned = 0, dfree = 0, dtotal = 0;
+            for (auto &nd : next) pruned += nd.pruned ? 1 : 0;
+            eng.device_memory(dfree, dtotal);
+            std::fprintf(stderr, "[level %d starts] %zu candidates (%zu decided by sub-patterns), host RSS %.0f MB, "
+                                 "device free %.0f of %.0f MB\n",
+                         st.levels + 1, next.size(), pruned, host_rss_mb(), dfree / 1048576.0, dtotal / 1048576.0);
+        }
         growth.reset(new Growth(next, ctx, pool, want_subs));  // runs during the next level's engine calls
         prev_levels = std::move(cur_levels);
         cur_levels.clear();

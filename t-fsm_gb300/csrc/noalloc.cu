@@ -12,14 +12,18 @@
 // Limits and sharing:
 //   * the array holds kScratchBytes (16 MiB) on every GPU that loads the library, until exit;
 //   * a pattern whose domain bitmaps need more than that is rejected with TFSM_ERR_LIMIT;
-//   * hub splitting is off on this path (its queues would need more scratch); automorphic vertices
+//   * work sharing is off on this path (its ring would need more scratch); automorphic vertices
 //     are searched separately — both change speed only, never results;
 //   * every call on a device reuses the same array and leaves its contents behind: the status block
 //     and counters are cleared at the start of each call and the kernels rewrite every bitmap word
 //     they read, but two calls whose work overlaps on the GPU race on the array, so calls must not
 //     overlap (calls on one graph handle are serialised by the handle's lock);
 //   * the first call on a device looks up the array's device address (cudaGetSymbolAddress) with
-//     that device current; make that first call before any stream capture.
+//     that device current; make that first call before any stream capture;
+//   * the address is kept for the life of the process: after cudaDeviceReset (or anything else
+//     that destroys the device's primary context) this entry point must not be called again;
+//   * the work runs on the graph handle's own non-blocking stream, and the caller's current
+//     device is restored before the call returns.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -62,6 +66,19 @@ int scratch_address(int device, unsigned char **out) {
 }
 
 size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+// Makes `device` current for the guard's lifetime and restores the caller's device afterwards.
+struct DeviceGuard {
+    int saved = -1;
+    bool ok = false;
+    explicit DeviceGuard(int device) {
+        if (cudaGetDevice(&saved) != cudaSuccess) return;
+        ok = saved == device || cudaSetDevice(device) == cudaSuccess;
+    }
+    ~DeviceGuard() {
+        if (saved >= 0) cudaSetDevice(saved);
+    }
+};
 
 #define NA_CK(x)                                   \
     do {                                           \
@@ -207,7 +224,7 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     const size_t o_desc = 0;
     const size_t o_status = align_up(o_desc + sizeof(PatDesc));
     const size_t o_counters = align_up(o_status + sizeof(PatStatus));
-    const size_t o_item_pu = align_up(o_counters + dev::kNumCounters * sizeof(uint32_t));
+    const size_t o_item_pu = align_up(o_counters + dev::kPassCounters * sizeof(uint32_t));
     const size_t o_prefix = align_up(o_item_pu + dev::kMaxN * sizeof(uint32_t));
     const size_t o_items = align_up(o_prefix + (dev::kMaxN + 1) * sizeof(uint64_t));
     const size_t o_pools = align_up(o_items + max_items * sizeof(dev::SearchItem));
@@ -218,7 +235,11 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
         return TFSM_ERR_LIMIT;
     }
     // ---- set-up on the graph's device ----
-    NA_CK(cudaSetDevice(eng.device()));
+    const DeviceGuard on_device(eng.device());
+    if (!on_device.ok) {
+        msg = "cannot make the graph's device current";
+        return TFSM_ERR_CUDA;
+    }
     unsigned char *base = nullptr;
     const int rc = scratch_address(eng.device(), &base);
     if (rc != TFSM_OK) {
@@ -234,7 +255,7 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     uint32_t *d_dom = reinterpret_cast<uint32_t *>(base + o_pools);
     uint32_t *d_found = d_dom + words;
     uint32_t *d_failed = d_found + words;
-    cudaStream_t s = 0;
+    cudaStream_t s = eng.stream();
     const dev::Graph &g = eng.device_graph();
 
     uint32_t item_pu[dev::kMaxN];
@@ -246,7 +267,7 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     }
     NA_CK(cudaMemcpyAsync(d_desc, &D, sizeof(D), cudaMemcpyHostToDevice, s));
     NA_CK(cudaMemsetAsync(d_status, 0, sizeof(PatStatus), s));  // the previous call's status stays behind
-    NA_CK(cudaMemsetAsync(d_counters, 0, dev::kNumCounters * sizeof(uint32_t), s));
+    NA_CK(cudaMemsetAsync(d_counters, 0, dev::kPassCounters * sizeof(uint32_t), s));
     NA_CK(cudaMemcpyAsync(d_item_pu, item_pu, n * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     NA_CK(cudaMemcpyAsync(d_prefix, prefix, (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
     // every bitmap word of every vertex is written here, so no clearing of the pools is needed
@@ -284,7 +305,10 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     // ---- search ----
     for (int u = 0; u < n; ++u) plan_from(n, adj, deg, st.dom_size, u, D.order[u], D.bn[u]);
     NA_CK(cudaMemcpyAsync(d_desc, &D, sizeof(D), cudaMemcpyHostToDevice, s));
-    dev::SearchItem buf[256];
+    // Staged through a small pageable buffer: cudaMemcpyAsync from pageable memory returns once the
+    // source has been copied out, so the buffer can be refilled without waiting for the device.
+    constexpr size_t kBuf = 1024;
+    dev::SearchItem buf[kBuf];
     size_t n_items = 0, fill = 0;
     uint32_t next_word[dev::kMaxN] = {0};
     for (bool more = true; more;) {  // round-robin over vertices, as the engine interleaves its items
@@ -300,9 +324,8 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
             next_word[u] = it.word_hi;
             buf[fill++] = it;
             more = true;
-            if (fill == 256) {
+            if (fill == kBuf) {
                 NA_CK(cudaMemcpyAsync(d_items + n_items, buf, fill * sizeof(it), cudaMemcpyHostToDevice, s));
-                NA_CK(cudaStreamSynchronize(s));  // buf is reused
                 n_items += fill;
                 fill = 0;
             }
@@ -317,13 +340,11 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     prm.tau = tau;
     prm.exact = exact ? 1 : 0;
     prm.n_items = (uint32_t)n_items;
-    prm.step_budget = 0;  // no hub splitting on this path
+    prm.split = 0;  // no work sharing on this path (no ring or group table)
     prm.team_lanes = 32;
-    prm.split_slice = 32;
     prm.n_pats = 1;
     prm.words = words;
-    NA_CK(dev::launch_search(g, d_desc, d_status, d_items, prm, d_counters, d_dom, d_found, d_failed, nullptr, nullptr,
-                             s));
+    NA_CK(dev::launch_search(g, d_desc, d_status, d_items, prm, d_counters, d_dom, d_found, d_failed, s));
     NA_CK(cudaMemcpyAsync(&st, d_status, sizeof(st), cudaMemcpyDeviceToHost, s));
     NA_CK(cudaStreamSynchronize(s));
     mn = UINT32_MAX;

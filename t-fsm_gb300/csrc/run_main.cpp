@@ -2,7 +2,8 @@
 //
 //   run -file G.lg -freq TAU [-thread T] [-maxNodes N] [-plain] [-exact] [-out PATH]
 //       [-step-budget B] [-split-slice S] [-chunk-words W] [-refine-rounds R] [-max-batch M]
-//       [-split-rounds K] [-round-budget B] [-time-limit SECONDS] [-random-orders SEED] [-no-prune]
+//       [-hub-span S] [-hub-parts K] [-isect-ratio R] [-search-lanes L] [-rank-window W] [-call-ms MS]
+//       [-no-split] [-time-limit SECONDS] [-random-orders SEED] [-no-prune]
 //
 // Frequent patterns go to ./grami_results.txt (or -out PATH) in the serial build's format
 // (serial/grami.h:622-635); timing and counts are printed as the parallel build prints them.
@@ -41,6 +42,7 @@ int main(int argc, char **argv) {
     if (flag(argc, argv, "-plain")) flags |= TFSM_FLAG_PLAIN;
     if (flag(argc, argv, "-exact")) flags |= TFSM_FLAG_EXACT;
     if (flag(argc, argv, "-no-prune")) flags |= TFSM_FLAG_NO_SUBPATTERN_PRUNING;
+    if (flag(argc, argv, "-no-split")) flags |= TFSM_FLAG_NO_SPLIT;
 
     tfsm_graph *g = nullptr;
     int rc = tfsm_graph_load(file, tau, &g);
@@ -49,14 +51,16 @@ int main(int argc, char **argv) {
         return 1;
     }
     tfsm_options o;
+    o.struct_size = sizeof(o);
     tfsm_get_options(g, &o);
     if (opt(argc, argv, "-step-budget")) o.step_budget = (uint32_t)std::atoi(opt(argc, argv, "-step-budget"));
     if (opt(argc, argv, "-split-slice")) o.split_slice = (uint32_t)std::atoi(opt(argc, argv, "-split-slice"));
     if (opt(argc, argv, "-chunk-words")) o.chunk_words = (uint32_t)std::atoi(opt(argc, argv, "-chunk-words"));
     if (opt(argc, argv, "-refine-rounds")) o.refine_rounds = (uint32_t)std::atoi(opt(argc, argv, "-refine-rounds"));
     if (opt(argc, argv, "-max-batch")) o.max_batch = (uint32_t)std::atoi(opt(argc, argv, "-max-batch"));
-    if (opt(argc, argv, "-split-rounds")) o.split_rounds = (uint32_t)std::atoi(opt(argc, argv, "-split-rounds"));
-    if (opt(argc, argv, "-round-budget")) o.round_budget = (uint32_t)std::atoi(opt(argc, argv, "-round-budget"));
+    if (opt(argc, argv, "-hub-span")) o.hub_span = (uint32_t)std::atoi(opt(argc, argv, "-hub-span"));
+    if (opt(argc, argv, "-hub-parts")) o.hub_parts = (uint32_t)std::atoi(opt(argc, argv, "-hub-parts"));
+    if (opt(argc, argv, "-isect-ratio")) o.isect_ratio = (uint32_t)std::atoi(opt(argc, argv, "-isect-ratio"));
     if (opt(argc, argv, "-search-lanes")) o.search_lanes = (uint32_t)std::atoi(opt(argc, argv, "-search-lanes"));
     if (opt(argc, argv, "-rank-window")) o.rank_window = (uint32_t)std::atoi(opt(argc, argv, "-rank-window"));
     if (opt(argc, argv, "-call-ms")) o.call_ms = std::atof(opt(argc, argv, "-call-ms"));

@@ -95,10 +95,15 @@ class GraphInfoC(C.Structure):
 
 
 class OptionsC(C.Structure):
-    _fields_ = [("step_budget", C.c_uint32), ("split_slice", C.c_uint32), ("chunk_words", C.c_uint32),
-                ("refine_rounds", C.c_uint32), ("max_batch", C.c_uint32), ("split_rounds", C.c_uint32),
-                ("time_limit_s", C.c_double), ("round_budget", C.c_uint32), ("search_lanes", C.c_uint32),
-                ("rank_window", C.c_uint32), ("call_ms", C.c_double)]
+    _fields_ = [("struct_size", C.c_uint32), ("step_budget", C.c_uint32), ("split_slice", C.c_uint32),
+                ("chunk_words", C.c_uint32), ("refine_rounds", C.c_uint32), ("max_batch", C.c_uint32),
+                ("hub_span", C.c_uint32), ("hub_parts", C.c_uint32), ("time_limit_s", C.c_double),
+                ("search_lanes", C.c_uint32), ("rank_window", C.c_uint32), ("call_ms", C.c_double),
+                ("isect_ratio", C.c_uint32), ("reserved", C.c_uint32)]
+
+    def __init__(self, **kw):
+        super().__init__(**kw)
+        self.struct_size = C.sizeof(OptionsC)
 
 
 class MineStatsC(C.Structure):
@@ -110,7 +115,8 @@ class MineStatsC(C.Structure):
                 ("evaluations", C.c_uint64), ("frequent", C.c_uint64), ("searches", C.c_uint64),
                 ("steps", C.c_uint64), ("by_filter", C.c_uint64), ("engine_calls", C.c_uint64),
                 ("levels", C.c_int32), ("complete", C.c_int32), ("level_ms", C.c_double * MAX_LEVELS),
-                ("pruned", C.c_uint64)]
+                ("pruned", C.c_uint64), ("split_searches", C.c_uint64), ("split_tasks", C.c_uint64),
+                ("intersections", C.c_uint64)]
 
 
 _lib = None
@@ -319,7 +325,7 @@ class Graph:
     def options(self) -> dict:
         o = OptionsC()
         _check(lib().tfsm_get_options(self._h, C.byref(o)))
-        return {f: getattr(o, f) for f, _ in OptionsC._fields_}
+        return {f: getattr(o, f) for f, _ in OptionsC._fields_ if f not in ("struct_size", "reserved")}
 
     def set_options(self, **kw) -> None:
         cur = self.options()

@@ -1,7 +1,7 @@
 """Generate the golden fixtures of the parity tests from the reference T-FSM itself.
 
-Runs only where the reference sources exist (they are read from /root/reference by
-oracle/Makefile): `make -C oracle ref harness port` builds
+Runs only where the reference sources exist (oracle/Makefile reads them from the tree its REF
+variable names): `make -C oracle ref harness port REF=<tree>` builds
   oracle/_ref/serial_run    the reference serial miner   (serial/Makefile flags)
   oracle/_ref/parallel_run  the reference parallel miner (parallel/Makefile flags)
   oracle/_ref/mni_harness   exact MNI domains from the reference's GMatchEngine
@@ -22,6 +22,7 @@ from __future__ import annotations
 import json
 import os
 import random
+import re
 import subprocess
 import sys
 import tempfile
@@ -45,6 +46,17 @@ GEN_CASES = {
                                 seed=1), tau=9000, max_nodes=5, mni="all"),
     "cfg2_t7000": dict(gen=dict(n=100000, mean=22, gamma=2.2, max_degree=1400, labels=29, zipf=1.2, elabels=1,
                                 seed=1), tau=7000, max_nodes=5, mni="none", serial=False),
+    # the batched workload: the config-2 graph at tau 5000 with up to 6 pattern vertices (the
+    # 5,000-vertex graph has no label frequent at tau 5000)
+    "cfg3": dict(gen=dict(n=100000, mean=22, gamma=2.2, max_degree=1400, labels=29, zipf=1.2, elabels=1,
+                          seed=1), tau=5000, max_nodes=6, mni="none", serial=False, threads=0),
+    # the held-out graph of the learned-order evaluation: config-2 shape, seed 99, tau 20000
+    "cfg5_seed99": dict(gen=dict(n=100000, mean=22, gamma=2.2, max_degree=1400, labels=29, zipf=1.2, elabels=1,
+                                 seed=99), tau=20000, max_nodes=5, mni="all"),
+    # the hub-heavy 2M-vertex graph (3 edge labels) with up to 3 pattern vertices: the largest
+    # maxNodes the reference's parallel build completes here in about an hour on all cores
+    "cfg4_m3": dict(gen=dict(n=2000000, mean=20, gamma=2.05, max_degree=50000, labels=50, zipf=1.1, elabels=3,
+                             seed=2), tau=20000, max_nodes=3, mni="none", serial=False, threads=0),
 }
 
 # Small hand-made graphs for edge cases, written by make_small_graphs().
@@ -131,7 +143,7 @@ def run(cmd, cwd=None, timeout=None) -> subprocess.CompletedProcess:
 def main(names: list[str]) -> None:
     for tool in (REF / "serial_run", REF / "parallel_run", REF / "mni_harness", PORT, GEN):
         if not tool.exists():
-            sys.exit(f"missing {tool}: run `make -C oracle ref harness port` and t-fsm_gb300/build.py first")
+            sys.exit(f"missing {tool}: run `make -C oracle ref harness port REF=<tree>` and t-fsm_gb300/build.py first")
     make_small_graphs()
     cases_path = HERE / "cases.json"
     cases = json.loads(cases_path.read_text()) if cases_path.exists() else {}
@@ -152,10 +164,15 @@ def main(names: list[str]) -> None:
                 sdir.mkdir()
                 run([REF / "serial_run", "-file", graph, "-freq", tau, "-maxNodes", mn], cwd=sdir)
                 ser = sorted(read_results(sdir / "grami_results.txt"))
-            # one thread: the parallel build prints patterns from several threads without a lock,
-            # which can garble its stdout; the task-based code path is the same
-            pr = run([REF / "parallel_run", "-file", graph, "-freq", tau, "-thread", 1, "-maxNodes", mn], cwd=tmp)
+            # one thread by default: the parallel build prints patterns from several threads without
+            # a lock, which can garble its stdout; the task-based code path is the same.  Long cases
+            # use every core (threads=0) and must then reproduce the build's own pattern count.
+            threads = spec.get("threads", 1) or (os.cpu_count() or 4)
+            pr = run([REF / "parallel_run", "-file", graph, "-freq", tau, "-thread", threads, "-maxNodes", mn],
+                     cwd=tmp)
             par = sorted(read_parallel_stdout(pr.stdout))
+            m = re.search(r"# Frequent Patterns: (\d+)", pr.stdout)
+            n_one_edge = None
             if ser is not None:
                 multi = sorted(k for k in ser if " " in k)
                 if multi != par:
@@ -168,6 +185,9 @@ def main(names: list[str]) -> None:
                      port_out])
                 one_edge = sorted(k for k in read_results(port_out) if " " not in k)
                 pats = sorted(one_edge + par)
+                n_one_edge = len(one_edge)
+            if m and n_one_edge is not None and int(m.group(1)) != len(pats):
+                sys.exit(f"{name}: parsed {len(pats)} patterns, the parallel build counted {m.group(1)}")
             (HERE / f"{name}.patterns.txt").write_text("".join(k + "\n" for k in pats))
             mni_lines = 0
             if spec["mni"] != "none":
@@ -187,7 +207,8 @@ def main(names: list[str]) -> None:
                 (HERE / f"{name}.mni.txt").write_text("".join(ln + "\n" for ln in lines))
                 mni_lines = len(lines)
             rec = {"tau": tau, "max_nodes": mn, "n_patterns": len(pats), "n_mni": mni_lines,
-                   "checksum": graph_checksum(graph), "serial_checked": ser is not None}
+                   "checksum": graph_checksum(graph), "serial_checked": ser is not None,
+                   "parallel_threads": threads}
             rec.update({"gen": spec["gen"]} if "gen" in spec else {"file": spec["file"]})
             cases[name] = rec
             print(name, rec, flush=True)

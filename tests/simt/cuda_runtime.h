@@ -296,6 +296,15 @@ inline unsigned atomicCAS(unsigned *p, unsigned cmp, unsigned val) {
     __atomic_compare_exchange_n(p, &cmp, val, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED);
     return cmp;
 }
+inline unsigned atomicExch(unsigned *p, unsigned v) { return __atomic_exchange_n(p, v, __ATOMIC_RELAXED); }
+inline unsigned atomicMax(unsigned *p, unsigned v) {
+    unsigned cur = __atomic_load_n(p, __ATOMIC_RELAXED);
+    while (cur < v && !__atomic_compare_exchange_n(p, &cur, v, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
+    }
+    return cur;
+}
+// __nanosleep of a team waiting for work: let the other emulated lanes run
+inline void tfsm_emu_nap(unsigned) { std::this_thread::yield(); }
 
 // ---------------- runtime API subset ----------------
 typedef int cudaError_t;
@@ -303,11 +312,11 @@ enum : int { cudaSuccess = 0, cudaErrorInvalidValue = 1, cudaErrorMemoryAllocati
 enum cudaMemcpyKind { cudaMemcpyHostToHost, cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost, cudaMemcpyDeviceToDevice };
 enum cudaDeviceAttr { cudaDevAttrMultiProcessorCount = 16 };
 #define cudaStreamNonBlocking 0x01
-struct EmuStream {};
+struct CUstream_st {};  // the runtime's stream type (engine.hpp names it)
 struct EmuEvent {
     std::chrono::steady_clock::time_point t;
 };
-typedef EmuStream *cudaStream_t;
+typedef CUstream_st *cudaStream_t;
 typedef EmuEvent *cudaEvent_t;
 
 inline const char *cudaGetErrorString(cudaError_t e) { return e == cudaSuccess ? "no error" : "emulated error"; }
@@ -317,6 +326,10 @@ inline cudaError_t cudaGetDeviceCount(int *n) {
     return cudaSuccess;
 }
 inline cudaError_t cudaSetDevice(int) { return cudaSuccess; }
+inline cudaError_t cudaMemGetInfo(size_t *f, size_t *t) {
+    *f = *t = 0;
+    return cudaSuccess;
+}
 inline cudaError_t cudaGetDevice(int *d) {
     *d = 0;
     return cudaSuccess;
@@ -358,7 +371,7 @@ inline cudaError_t cudaMemcpyFromSymbol(void *dst, const T &sym, size_t n) {
     return cudaSuccess;
 }
 inline cudaError_t cudaStreamCreateWithFlags(cudaStream_t *s, unsigned) {
-    *s = new EmuStream;
+    *s = new CUstream_st;
     return cudaSuccess;
 }
 inline cudaError_t cudaStreamSynchronize(cudaStream_t) { return cudaSuccess; }

@@ -58,10 +58,10 @@ def test_mining_plain_matches_reference(tfsm, graphs, case, tmp_path):
     assert st["engine_calls"] == st["evaluations"] - st["pruned"]  # one engine call per searched candidate
 
 
-SPLIT_OPTS = [dict(step_budget=1, split_slice=32, round_budget=1),   # splits again in every round
-              dict(step_budget=1, split_slice=32, split_rounds=1, round_budget=1 << 30),  # no re-splitting
-              dict(step_budget=3, split_slice=64, round_budget=2, split_rounds=3),
-              dict(step_budget=0)]                                    # no splitting
+SPLIT_OPTS = [dict(step_budget=1, split_slice=1),          # passes with budgets 1, 8, 64, none
+              dict(step_budget=3, split_slice=32),
+              dict(step_budget=0, hub_span=0, hub_parts=8, split_slice=1),  # first depths shared at once
+              dict(step_budget=0, hub_parts=1)]                     # one pass, sharing with waiting teams
 
 
 @pytest.mark.parametrize("case", ["cfg1", "el3", "star_hub", "clique"])
@@ -190,8 +190,8 @@ def test_forced_splits_keep_exact_supports(tfsm, graphs):
     g = graphs(case)
     saved = g.options()
     try:
-        for opts in (dict(step_budget=1, split_slice=32, chunk_words=1, round_budget=1),
-                     dict(step_budget=2, split_slice=64, chunk_words=7, refine_rounds=1, split_rounds=2)):
+        for opts in (dict(step_budget=1, split_slice=1, chunk_words=1),
+                     dict(step_budget=2, split_slice=8, chunk_words=7, refine_rounds=1, hub_span=0, hub_parts=3)):
             g.set_options(**opts)
             res = g.evaluate([tfsm.parse_key(k) for k in keys], flags=tfsm.FLAG_EXACT)
             assert [r.mni for r in res] == [want[k] for k in keys]
@@ -248,15 +248,16 @@ def test_cli_writes_reference_format(built, case_graph, tmp_path):
 
 
 @pytest.mark.parametrize("case", ["star_hub", "clique", "el3"])
-def test_split_buffers_full_keep_results(built, case_graph, case, tmp_path):
-    """Split buffers of 5 tasks / 5 groups: claims straddle the end, searches finish in place."""
+@pytest.mark.parametrize("ring", ["1", "4"])
+def test_work_ring_full_keeps_results(built, case_graph, case, ring, tmp_path):
+    """A work ring of 1 or 4 slots: most donations are refused and those searches go on in place."""
     import os
     c = CASES[case]
     out = tmp_path / "grami_results.txt"
-    env = dict(os.environ, TFSM_SPLIT_CAPACITY="5")
+    env = dict(os.environ, TFSM_QUEUE_CAPACITY=ring)
     r = subprocess.run([str(built / "bin" / "run"), "-file", str(case_graph(case)), "-freq", str(c["tau"]),
-                        "-maxNodes", str(c["max_nodes"]), "-step-budget", "1", "-round-budget", "1", "-split-slice",
-                        "32", "-out", str(out)], capture_output=True, text=True, timeout=300, env=env)
+                        "-maxNodes", str(c["max_nodes"]), "-step-budget", "1", "-split-slice", "1", "-out", str(out)],
+                       capture_output=True, text=True, timeout=300, env=env)
     assert r.returncode == 0, r.stderr
     assert set(read_results(out)) == golden_pattern_set(case)
 
@@ -302,7 +303,7 @@ def test_team_sizes_keep_results(tfsm, graphs, case, lanes, tmp_path):
         g.set_options(search_lanes=lanes)
         pats, _ = mine_set(tfsm, g, case, tmp_path)
         assert pats == golden_pattern_set(case)
-        g.set_options(search_lanes=lanes, step_budget=1, split_slice=32, round_budget=1)
+        g.set_options(search_lanes=lanes, step_budget=1, split_slice=1, hub_span=0, hub_parts=8)
         pats, _ = mine_set(tfsm, g, case, tmp_path)
         assert pats == golden_pattern_set(case)
         want = golden_mni(case)
