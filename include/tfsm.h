@@ -36,7 +36,7 @@ extern "C" {
 /* flags */
 #define TFSM_FLAG_EXACT 1u    /* exact MNI per vertex: no early exit at tau */
 #define TFSM_FLAG_PLAIN 2u    /* tfsm_mine: one engine call per candidate pattern (unbatched) */
-#define TFSM_FLAG_NO_SPLIT 4u /* no work sharing: every search runs to its end on one team */
+#define TFSM_FLAG_NO_SPLIT 4u /* disable splitting of long searches (hub tasks) */
 #define TFSM_FLAG_NO_SUBPATTERN_PRUNING 8u /* tfsm_mine: search every candidate, even one with an
                                               infrequent one-edge-smaller sub-pattern */
 
@@ -91,8 +91,8 @@ typedef struct {
                                          pattern edges; 0 unused) */
     uint64_t pruned;       /* candidates decided infrequent by an infrequent sub-pattern (counted in
                               evaluations and by_filter; no engine call) */
-    uint64_t split_searches; /* searches that shared work through the device ring */
-    uint64_t split_tasks;  /* tasks they shared */
+    uint64_t split_searches; /* searches split into tasks */
+    uint64_t split_tasks;  /* split tasks written (all rounds) */
     uint64_t intersections; /* set intersections of the searches: one per chunk of up to 32 anchor
                                candidates and backward neighbour (the anchor's own range included) */
 } tfsm_mine_stats;
@@ -171,18 +171,17 @@ int tfsm_mine(tfsm_graph *g, int32_t tau, int32_t max_nodes, uint32_t flags, con
  * with TFSM_ERR_ARG. */
 typedef struct {
     uint32_t struct_size;   /* sizeof(tfsm_options) as the caller compiled it */
-    uint32_t step_budget;   /* 32-candidate chunks a search may take in the first search pass of
-                               an engine call before it is set aside; each later pass allows 8x
-                               more and the last (the fourth) has no limit, so the quick searches
-                               of every candidate run first (0: one pass without limit) */
-    uint32_t split_slice;   /* least adjacency positions per part when a search of the last pass
-                               shares out its current depth on the device work ring (>= 1) */
+    uint32_t step_budget;   /* 32-candidate chunks a search may evaluate before its unexplored
+                               branches (at every depth) become split tasks; split tasks get twice
+                               that, doubling per round up to 8x; a search whose tasks find no room
+                               is retried by a later pass with 8x the budgets (0: never split) */
+    uint32_t split_slice;   /* adjacency positions per split task (>= 1) */
     uint32_t chunk_words;   /* 32-bit domain-bitmap words per search work item (>= 1) */
     uint32_t refine_rounds; /* arc-consistency passes for patterns that need a search (>= 1) */
     uint32_t max_batch;     /* tfsm_mine: most patterns per engine call (>= 1) */
     uint32_t hub_span;      /* a search whose first depth has more adjacency positions than this
-                               (a hub vertex's label range) shares it out at once ... */
-    uint32_t hub_parts;     /* ... in this many parts, one of them kept (1..32; 1: off) */
+                               (a hub vertex's label range) is split at once ... */
+    uint32_t hub_parts;     /* ... into this many tasks, as many teams (1..32; 1: off) */
     double time_limit_s;    /* tfsm_mine: stop between engine calls after this many seconds (0: none);
                                the run is then reported incomplete */
     uint32_t search_lanes;  /* lanes per search: 8 (default: four searches per warp, for calls with
@@ -195,9 +194,10 @@ typedef struct {
                                least 4); full calls that finish sooner double it again, up to
                                max_batch (default 2; 0: always max_batch) */
     uint32_t isect_ratio;   /* intersection form of a search step against a further backward
-                               neighbour: its candidate run is merged (read once, coalesced) when it
-                               is at most isect_ratio times the step's survivors, and probed by
-                               galloping search otherwise (>= 1; the autotuner tries 4, 16, 64) */
+                               neighbour: its candidate range is merged (streamed once with 128-bit
+                               loads) when it is at most isect_ratio times the anchor's range, and
+                               probed by binary search otherwise (>= 1; the reference switches at
+                               50; the autotuner tries 4, 16, 64) */
     uint32_t reserved;      /* 0 */
 } tfsm_options;
 

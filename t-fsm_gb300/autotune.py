@@ -23,9 +23,9 @@ SPACE = [
     ("search_lanes", [8, 32]),
     ("chunk_words", [1, 2]),
     ("isect_ratio", [16, 4, 64]),
-    ("hub_parts", [4, 1, 2, 8]),
-    ("step_budget", [64, 16, 256, 0]),
-    ("split_slice", [32, 64, 128]),
+    ("hub_parts", [4, 1, 2, 8]),  # teams that search one hub candidate's first depth together
+    ("step_budget", [16, 8, 32, 64]),
+    ("split_slice", [64, 32, 128]),
     ("refine_rounds", [1, 2]),
 ]
 

@@ -27,6 +27,9 @@ ROOT = PKG.parent
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CXXFLAGS = ["-std=c++17", "-O3", "-fPIC", "-Wall", "-Wno-unused-function"]
+# TFSM_HOST_DEBUG=1: host code keeps frame pointers and debug information (crash reports with
+# symbolised stacks); device code is unchanged.
+HOST_DEBUG = ["-g", "-fno-omit-frame-pointer"] if os.environ.get("TFSM_HOST_DEBUG") == "1" else []
 
 
 def _cuda_home() -> Path:
@@ -71,13 +74,15 @@ def build(verbose: bool = False) -> Path:
         obj = BUILD / (src.stem + ".o")
         objs.append(obj)
         if _stale(obj, [src] + headers):
-            jobs.append([nvcc, *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(CSRC),
+            jobs.append([nvcc, *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
+                         *(["-Xcompiler", ",".join(HOST_DEBUG)] if HOST_DEBUG else []), "-I", str(CSRC),
                          *(["-DTFSM_BOUNDS_CHECK"] if CHECKED else []), "-c", str(src), "-o", str(obj)])
     for src in cpp:
         obj = BUILD / (src.stem + ".o")
         objs.append(obj)
         if _stale(obj, [src] + headers):
-            jobs.append(["g++", *CXXFLAGS, "-pthread", "-I", str(CSRC), "-I", str(cuda / "include"), "-c", str(src),
+            jobs.append(["g++", *CXXFLAGS, *HOST_DEBUG, "-pthread", "-I", str(CSRC), "-I", str(cuda / "include"),
+                         "-c", str(src),
                          "-o", str(obj)])
     gen = BIN / "gen_lg"
     gen_src = CSRC / "tools" / "gen_lg.cpp"
@@ -101,7 +106,7 @@ def build(verbose: bool = False) -> Path:
     run_bin = BIN / "run"
     run_src = CSRC / "run_main.cpp"
     if _stale(run_bin, [run_src, LIB]):
-        cmd = ["g++", "-std=c++17", "-O2", str(run_src), "-o", str(run_bin), "-L", str(PKG), "-ltfsm_gb300",
+        cmd = ["g++", "-std=c++17", "-O2", *HOST_DEBUG, str(run_src), "-o", str(run_bin), "-L", str(PKG), "-ltfsm_gb300",
                "-Wl,-rpath,$ORIGIN/.."]
         if verbose:
             print(" ".join(cmd), flush=True)

@@ -3,7 +3,8 @@
 // Data graph in HBM (built once per graph, read-only afterwards):
 //   vertices are renumbered so that each frequent vertex label owns one contiguous id range
 //   [label_start[L], label_start[L+1]) — ids keep the reference's pruned order inside a label.
-//   row_off[n+1] (u32) / col[2m] (u32, ascending) / elab[2m] (u8, dense edge label)
+//   row_off[n+1] (u32) / col[2m] (u32, ascending; followed by kColPad entries of 0xffffffff so
+//   that 128-bit loads near the end stay inside the allocation) / elab[2m] (u8, dense edge label)
 //   Ascending neighbour ids are therefore ordered by (neighbour label, id): the neighbours of v
 //   that carry label L are one sub-range of v's list; a per-vertex table of label offsets gives its
 //   bounds with two independent loads.
@@ -19,6 +20,7 @@ namespace dev {
 
 constexpr int kMaxN = 16;          // pattern vertices supported by the device path
 constexpr uint8_t kNoEdge = 0xff;  // edge-label matrix entry for "not adjacent"
+constexpr uint32_t kColPad = 128;  // padding entries after col (at least 4 x the widest team)
 
 struct Graph {
     uint32_t n = 0;
@@ -114,13 +116,12 @@ inline uint32_t part_mask(uint32_t part, uint32_t log2) {
     return m;
 }
 
-// Split task: a donated part of one (u, v) search — the candidates at anchor positions [lo, hi) of
-// depth `depth` of u's matching order, below the partial embedding prefix[0..depth-1] (data
-// vertices of the pattern vertices order[0..depth-1]).  A search shares out the unexplored
-// remainder of its shallowest open depth this way when other teams wait for work, when it has run
-// past its step budget, or at once when its first level is a hub's long adjacency range
-// (parallel/comper.h:640-749 spawns the remaining branches of a timed-out search with their
-// partial embeddings the same way).
+// Split task: an unexplored part of one (u, v) search — the candidates at positions [lo, hi) of the
+// anchor list at `depth`, below the partial embedding prefix[0..depth-1] (data vertices of the
+// pattern vertices order[0..depth-1] of u's matching order).  A search that exceeds its step budget
+// turns its whole unexplored remainder, at every depth, into such tasks (parallel/comper.h:640-749
+// spawns every remaining branch with its partial embedding the same way); a search whose first
+// depth is a hub's long adjacency range does so at once.
 struct SplitTask {
     uint32_t pat;
     uint16_t u;
@@ -128,82 +129,64 @@ struct SplitTask {
     uint8_t pad;
     uint32_t v;              // candidate of u: the search this task belongs to
     uint32_t lo, hi;         // anchor positions at `depth`
-    uint32_t group;          // group slot that decides v
+    uint32_t group;          // index of the group that decides v
     uint32_t prefix[kMaxN];  // prefix[k] = data vertex of order[k], k < depth
 };
-constexpr int kTaskWords = sizeof(SplitTask) / 4;
-static_assert(sizeof(SplitTask) % 4 == 0, "task words");
 
-// One slot of the work queue, a bounded multi-producer multi-consumer ring with a sequence number
-// per slot (D. Vyukov's bounded MPMC queue): the slot of position p is free for a producer when
-// seq == p, holds a task for a consumer when seq == p + 1, and is handed to position p + capacity
-// by the consumer that took it.  Producers and consumers claim positions with compare-and-swap on
-// the ring's tail / head; no one ever waits on a slot, so a full ring only refuses a donation and
-// an empty one only sends the team on to other work.
-struct QueueCell {
-    uint32_t seq;
-    uint32_t pad;
-    SplitTask task;
+// All tasks of one (u, v) search; the last task to finish decides v when none found an embedding
+// (parallel/taskprogmap.h:10-85 tracks a split search's subtasks the same way).
+constexpr uint32_t kNullTask = 0xffffffffu;  // SplitTask::pat of a slot that holds no task
+
+struct SplitGroup {
+    uint32_t pat;
+    uint16_t u;
+    uint16_t pad;
+    uint32_t v;
+    uint32_t pending;    // tasks not yet finished
+    uint32_t incomplete; // a task stopped without an answer (pattern decided, or set aside for the
+                         //   next pass): failure cannot be concluded
 };
-static_assert(sizeof(QueueCell) % 8 == 0, "queue cell alignment");
 
-// Group of a split search: one 32-bit word per slot in a recycled table, the number of units (the
-// donor and its tasks) not yet finished, plus kGroupIncomplete when one of them stopped without an
-// answer (its pattern was decided).  0 is a free slot; a donor claims one with CAS 0 -> 1 and adds
-// the tasks it donates before they become visible; the unit whose decrement reaches zero frees
-// the slot and, when no unit found an embedding and none stopped early, records v's failure.
-constexpr uint32_t kNoGroup = 0xffffffffu;
-constexpr uint32_t kGroupIncomplete = 0x80000000u;
-
-// Counters of one search pass (zeroed before the call), one per 128-byte line: the hot ones are
-// polled by every waiting team.
-enum : int {
-    kCntItem = 0,     // next work item
-    kCntWork,         // outstanding units: teams inside an item, tasks queued or running
-    kCntIdle,         // teams waiting for work
-    kCntGroupCursor,  // next group slot to try
-    kCntGroups,       // searches that donated (groups claimed)
-    kCntTasks,        // tasks donated
-    kCntRefused,      // donations refused (no free group slot, or the ring full)
-    kCntWaitExpired,  // teams that stopped waiting at the wait limit (a statistic, not an error)
-    kCntQueueMax,     // deepest ring seen by a donor
-    kCntBadTask,      // tasks taken off the ring with fields out of range (skipped; an engine fault)
-    kCntAbandoned,    // searches set aside at the pass's step budget (the next pass retries them)
-    kNumCounters
-};
-constexpr int kCntStride = 32;                       // u32 per counter line
-constexpr int kPassCounters = kNumCounters * kCntStride;
-constexpr int kMaxPasses = 4;                        // search passes per call
-constexpr int kQctlHead = 0, kQctlTail = kCntStride;  // ring positions, one line each
+// Split rounds after a search pass: every round but the last possible one (kMaxRounds - 1) has a
+// step budget, so a task keeps being cut until the rounds drain.
+constexpr int kMaxRounds = 64;
+// Counters of one search pass: [0] next item, [1] groups used, [2 + r] tasks written for round r
+// (may pass the buffer capacity; readers clamp), [kClaimBase + r] next task of round r to process,
+// [kCntAbandoned] searches and tasks set aside for the next pass (no room for their remainder) and
+// teams that stopped starting searches because the buffers were full.
+constexpr int kClaimBase = 2 + kMaxRounds + 1;
+constexpr int kCntAbandoned = kClaimBase + kMaxRounds + 1;
+constexpr int kNumCounters = kCntAbandoned + 1;
+// Search passes per engine call: a search may take step_budget chunk steps before its remainder
+// becomes split tasks; what did not fit the buffers is retried by the next pass, whose budgets are
+// 8x larger; in the last pass such a search finishes in place.
+constexpr int kMaxPasses = 4;
 
 struct SearchParams {
     uint32_t tau;
     uint32_t exact;          // 1: evaluate every candidate, no early exit
     uint32_t n_items;
-    uint32_t split;          // 0: searches never donate (no ring or group table needed)
-    uint32_t split_slice;    // least anchor positions per donated part of the current depth
-    uint32_t hub_span;       // a search whose first depth has more anchor positions than this
-                             //   shares it out at once ...
-    uint32_t hub_parts;      //   ... into this many parts (the donor keeps one; 1: off)
-    uint32_t soft_cap;       // ring depth above which budget and hub donations are skipped
+    uint32_t split;          // 0: searches never split (no buffers needed)
+    uint32_t step_budget;    // chunk evaluations before a search is split
+    uint32_t split_slice;    // anchor positions per split task
+    uint32_t hub_span;       // a search whose first depth has more anchor positions than this is
+                             //   split at once ...
+    uint32_t hub_parts;      //   ... into this many tasks (1: off)
+    uint32_t isect_ratio;    // a further backward neighbour's range at most this many times the
+                             //   anchor's is merged, a longer one probed
+    uint32_t split_cap;      // capacity of each of the two split-task buffers
+    uint32_t split_slack;    // slots above a sliced-claim limit, kept for compact remainders
+    uint32_t search_fill;    // sliced-claim limit of the search pass (the split rounds use
+                             //    split_cap - split_slack): the rounds' tasks can outnumber it
+    uint32_t group_cap;      // capacity of the split-group buffer
+    uint32_t last;           // 1: the last pass (a remainder without room finishes in place);
+                             //   0: it is set aside for the next pass
     uint32_t team_lanes;     // lanes per search: 32, or 8 (four searches per warp; patterns of at
                              //    most 8 vertices)
     uint32_t parts_log2;     // every item is claimed 2^parts_log2 times, claim k searching the bits b of
                              //    its words with b % 2^parts_log2 == k (small calls: more warps busy)
     uint32_t n_pats;         // patterns of the batch
-    uint32_t qcap;           // ring slots (a power of two)
-    uint32_t gcap;           // group slots (a power of two)
-    uint32_t budget;         // chunk evaluations a search may take in this pass before it is set
-                             //   aside for the next one (0: the last pass, no limit)
-    uint32_t max_idle;       // teams that may wait for shared work at once (the others end)
-    uint32_t share_steps;    // last pass: a search that has run this many chunk steps also shares
-                             //   work while the ring is short of soft_cap (0: only to waiting teams)
     uint64_t words;          // size of each level bitmap pool (32-bit words)
-    QueueCell *cells;        // [qcap]
-    uint32_t *qctl;          // [kQctlHead] head, [kQctlTail] tail: positions, kept across launches
-    uint32_t *groups;        // [gcap]
-    const uint32_t *prev;    // the previous pass's counters (nullptr in the first pass): a pass
-                             //   whose predecessor set nothing aside has nothing to do
 };
 
 }  // namespace dev

@@ -7,18 +7,19 @@
 //                  (pruneCandidates, parallel/gmatch.h:600-658, pull direction).  Iterated to a
 //                  fixpoint for distinct-label trees, whose domains are then the exact MNI
 //                  domains (parallel/comper.h:1619-1653).
-//   k_search       persistent backtracking: a team of lanes (a warp, or a quarter of one) per
-//                  (pattern vertex u, candidate v) search looks for one embedding with u -> v
+//   k_search       backtracking, one search pass: a team of lanes (a warp, or a quarter of one)
+//                  per (pattern vertex u, candidate v) search looks for one embedding with u -> v
 //                  (LFTJ, serial/gmatch.h:906-987).  Local candidates at each depth are the label
 //                  sub-range of the smallest backward neighbour's adjacency, checked G at a time
 //                  (one per lane) against the domain bitmap, injectivity and every other backward
-//                  neighbour; the survivors are a ballot mask.  Found embeddings add all their
-//                  vertices (and automorphic images) to the MNI domains; early exit per vertex at
-//                  tau and per pattern when tau can no longer be reached
-//                  (parallel/comper.h:288-297).  Long searches share out their unexplored
-//                  branches as tasks on a device ring that any team takes (work sharing for hub
-//                  vertices, parallel/comper.h:640-749, 865-973); the last unit of a split search
-//                  to finish decides its failure (parallel/taskprogmap.h:10-85).
+//                  neighbour (merged or probed, by their size ratio); the survivors are a ballot
+//                  mask.  Found embeddings add all their vertices (and automorphic images) to the
+//                  MNI domains; early exit per vertex at tau and per pattern when tau can no
+//                  longer be reached (parallel/comper.h:288-297).  A search that exceeds its step
+//                  budget (or starts at a hub) turns its unexplored remainder into split tasks
+//                  (parallel/comper.h:640-749, 865-973).
+//   k_split        one split round over those tasks; the last task of a search to finish decides
+//                  its failure (parallel/taskprogmap.h:10-85).
 #include <cstdint>
 #include <cstdio>
 
@@ -289,7 +290,7 @@ __global__ void __launch_bounds__(256) k_refine(Graph g, const PatDesc *__restri
 
 
 // ------------------------------------------------------------------------------------------------
-// K5 / K6: persistent search with device-side work sharing.
+// K5 / K6: search passes and split rounds.
 // ------------------------------------------------------------------------------------------------
 namespace {
 
@@ -333,25 +334,6 @@ struct TeamMaxN {
     static constexpr int value = G == 32 ? kMaxN : 8;
 };
 
-// Acquire load / release store at device scope: the hand-over of a ring slot between the team
-// that writes a task and the team that reads it.
-__device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
-#ifdef TFSM_SIMT_EMULATION
-    return __atomic_load_n(p, __ATOMIC_ACQUIRE);
-#else
-    uint32_t v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-#endif
-}
-__device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
-#ifdef TFSM_SIMT_EMULATION
-    __atomic_store_n(p, v, __ATOMIC_RELEASE);
-#else
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-#endif
-}
-
 template <int N>
 struct Plan {
     uint32_t off[N];
@@ -377,11 +359,19 @@ struct State {
     uint32_t mask[N];     // by depth: surviving candidates already known to be in w's MNI domain
     uint32_t rest[N];     // by depth: the other surviving candidates (tried after `mask`)
     uint8_t anchor[N];    // by depth: pattern vertex whose adjacency is scanned
-    uint32_t blo[N][N];   // [depth][backward neighbour b]: label range of order[depth]'s
-    uint32_t bhi[N][N];   //   label inside emb[b]'s adjacency
+    uint32_t merge[N];    // by depth: backward neighbours intersected by merging (bit b), the
+                          //   others by probing
+    uint32_t blo[N][N];   // [depth][backward neighbour b]: the unconsumed part of order[depth]'s
+    uint32_t bhi[N][N];   //   label range inside emb[b]'s adjacency (blo advances chunk by chunk)
 };
 
-enum : int { kFail = 0, kFound = 1, kCancel = 3, kAbandon = 4 };
+// Staging tile of the merge form: 4 elements per lane, filled with one 128-bit load each.
+template <int G>
+struct Tile {
+    uint32_t v[4 * G];
+};
+
+enum : int { kFail = 0, kFound = 1, kAbort = 2, kCancel = 3 };
 
 // What makes a running search pointless: the searched (u, v) has been found by another team's
 // embedding, or the pattern (or, lazily, vertex u) has been decided.  Checked every kCheckEvery
@@ -394,24 +384,10 @@ struct Cancel {
     bool exact;
 };
 constexpr uint32_t kCheckEvery = 16;
-// A waiting team sleeps between looks at the ring (doubling from 256 ns up to 16 us) and stops
-// waiting after this many looks (about two seconds): the teams still at work finish every unit
-// they hold and every task they shared, so leaving early only costs balance, never a result.
-constexpr uint32_t kMaxWaits = 1u << 17;
-constexpr uint32_t kNapMin = 256, kNapMax = 16384;
 
 // Try candidates already known to be in w's MNI domain first.  Measured slower on the benchmark
 // graphs (the extra ballot and found-word loads cost more than the reordering saves): off.
 constexpr bool kFoundFirst = false;
-
-// The search's share of the launch: which (pattern, vertex, candidate) it decides and the group
-// it belongs to once it has shared work (kNoGroup before).
-struct Donor {
-    uint32_t p;
-    int u;
-    uint32_t v;
-    uint32_t group;
-};
 
 template <int G, int N>
 __device__ __forceinline__ void load_plan(const Team<G> &T, Plan<N> &P, const PatDesc &D, uint32_t p, int u,
@@ -442,10 +418,13 @@ __device__ __forceinline__ void load_plan(const Team<G> &T, Plan<N> &P, const Pa
 }
 
 // Anchor of depth d: the backward neighbour whose label sub-range is the shortest.  Lane k
-// handles the k-th backward neighbour; a team minimum picks the winner.
+// handles the k-th backward neighbour; a team minimum picks the winner.  Every other backward
+// neighbour's range is marked for merging when it is at most `ratio` times the anchor's, else for
+// probing: the reference's rule (intersection/computesetintersection.cpp:9-44 gallops when one
+// list is more than 50 times the other).
 template <int G, int N>
 __device__ __forceinline__ void setup_depth(const Team<G> &T, const Graph &g, const Plan<N> &P, State<N> &S, int d,
-                                            uint32_t &bytes) {
+                                            uint32_t ratio, uint32_t &bytes) {
     const int w = P.order[d];
     const uint32_t bnm = P.bn[d];
     const int nb = __popc(bnm);
@@ -473,6 +452,12 @@ __device__ __forceinline__ void setup_depth(const Team<G> &T, const Graph &g, co
         key = o < key ? o : key;
     }
     const int win = (int)(key & (unsigned long long)(G - 1));
+    const uint32_t alen = (uint32_t)(key >> 32);
+    uint32_t mbit = (int)T.lane < nb && (int)T.lane != win && (uint64_t)(hi - lo) <= (uint64_t)ratio * alen
+                        ? 1u << b
+                        : 0u;
+#pragma unroll
+    for (int s = G / 2; s > 0; s >>= 1) mbit |= T.xor_shfl(mbit, s);
     lo = T.bcast(lo, win);
     hi = T.bcast(hi, win);
     b = T.bcast(b, win);
@@ -482,11 +467,13 @@ __device__ __forceinline__ void setup_depth(const Team<G> &T, const Graph &g, co
         S.mask[d] = 0;
         S.rest[d] = 0;
         S.anchor[d] = (uint8_t)b;
+        S.merge[d] = mbit;
     }
     T.sync();
 }
 
-// Is adjacency position `idx` of the depth-d anchor a valid extension?  (one lane, one position)
+// Is adjacency position `idx` of the depth-d anchor a valid extension apart from the other
+// backward neighbours (one lane, one position): edge label, domain bit, not failed, injective.
 // `known` is set when x is already proven to be in w's MNI domain (a found embedding maps w to x).
 // A candidate proven to be in no embedding as w (its `failed` bit) is rejected: sound pruning.
 template <int N>
@@ -514,196 +501,140 @@ __device__ __forceinline__ bool check_candidate(const Graph &g, const Plan<N> &P
     }
     for (int k = 0; k < d; ++k)
         if (S.emb[P.order[k]] == x) return false;
-    uint32_t others = P.bn[d] & ~(1u << a);
+    return true;
+}
+
+// Does adjacency position `pos` of a sorted run [.., hi), or one of the parallel edges after it,
+// hold x with edge label `want`?
+__device__ __forceinline__ bool edge_at(const Graph &g, uint32_t pos, uint32_t hi, uint32_t x, uint8_t want,
+                                        uint32_t &bytes) {
+    while (pos < hi && TFSM_IN(6, pos, g.m2) && __ldg(g.col + pos) == x) {  // parallel edges: any with the label
+        bytes += 5;
+        if (__ldg(g.elab + pos) == want) return true;
+        ++pos;
+    }
+    return false;
+}
+
+// Team-uniform: the lanes' candidates x (where `ok`) intersected with the label ranges of the
+// depth's other backward neighbours.  The lanes' x ascend with the lane (consecutive anchor
+// positions), and so do the chunks of one depth visit, so each range is consumed front to back:
+//   merge   (range at most isect_ratio times the anchor's): the range is streamed from its cursor
+//           blo in tiles of 4G elements, one 128-bit load per lane, each lane looks its x up in the
+//           tile in shared memory, and the cursor moves to the chunk's largest x;
+//   probe   (a much longer range): each lane binary-searches its x in [blo, bhi), and blo moves to
+//           the largest x's position (the galloping start of the next chunk).
+template <int G, int N>
+__device__ __forceinline__ bool intersect_others(const Team<G> &T, const Graph &g, const Plan<N> &P, State<N> &S,
+                                                 Tile<G> &tile, int d, uint32_t x, bool ok, uint32_t &bytes) {
+    const int w = P.order[d];
+    uint32_t others = P.bn[d] & ~(1u << S.anchor[d]);
     while (others) {
         const int b = __ffs(others) - 1;
         others &= others - 1;
-        const uint32_t re = S.bhi[d][b];
-        uint32_t pos = lower_bound_cnt(g.col, S.blo[d][b], re, x, bytes, g.m2);
-        bool hit = false;
+        const uint32_t lo = S.blo[d][b], hi = S.bhi[d][b];
+        const bool merge = (S.merge[d] >> b) & 1u;
+        const uint32_t surv = T.ballot(ok);  // also orders every lane's reads before lane 0's writes
+        if (!surv) return false;
         const uint8_t want = P.el[w][b];
-        while (pos < re && TFSM_IN(6, pos, g.m2) && __ldg(g.col + pos) == x) {  // parallel edges: any with the label
-            bytes += 5;
-            if (__ldg(g.elab + pos) == want) {
-                hit = true;
-                break;
+        const int top = 31 - __clz(surv);
+        const uint32_t xtop = T.bcast(x, top);  // the chunk's largest surviving candidate
+        uint32_t next = hi;                      // blo for the next chunk
+        if (merge) {
+            bool hit = false;
+            uint32_t cur = lo;
+            while (cur < hi) {
+                const uint32_t base = cur & ~3u;  // 16-byte aligned (col is 256-byte aligned)
+                const uint32_t first = base + 4 * T.lane;
+                if (first < hi) {  // col is padded: the 4 elements never pass its allocation
+                    const uint4 q = __ldg(reinterpret_cast<const uint4 *>(g.col + first));
+                    tile.v[4 * T.lane] = q.x;
+                    tile.v[4 * T.lane + 1] = q.y;
+                    tile.v[4 * T.lane + 2] = q.z;
+                    tile.v[4 * T.lane + 3] = q.w;
+                    const uint32_t valid = hi - first;
+                    bytes += 4 * (valid < 4 ? valid : 4);
+                }
+                T.sync();
+                const uint32_t n_t = hi - base < 4u * G ? hi - base : 4u * G;
+                const uint32_t lo_t = cur - base;
+                if (ok && !hit) {
+                    uint32_t l = lo_t, h = n_t;
+                    while (l < h) {
+                        const uint32_t m = (l + h) >> 1;
+                        if (tile.v[m] < x) l = m + 1;
+                        else h = m;
+                    }
+                    if (l < n_t && tile.v[l] == x) hit = edge_at(g, base + l, hi, x, want, bytes);
+                }
+                const uint32_t last = tile.v[n_t - 1];
+                uint32_t stop = n_t;
+                if (last >= xtop) {  // every candidate of the chunk lies inside this tile: the
+                    uint32_t l = lo_t, h = n_t;  // cursor stops at the first element >= xtop
+                    while (l < h) {
+                        const uint32_t m = (l + h) >> 1;
+                        if (tile.v[m] < xtop) l = m + 1;
+                        else h = m;
+                    }
+                    stop = l;
+                }
+                T.sync();  // every lane is done with the tile before it is refilled
+                cur = base + stop;
+                if (last >= xtop) break;
             }
-            ++pos;
+            next = cur < hi ? cur : hi;
+            ok = ok && hit;
+        } else {
+            uint32_t at = hi;
+            bool hit = false;
+            if (ok) {
+                at = lower_bound_cnt(g.col, lo, hi, x, bytes, g.m2);
+                hit = edge_at(g, at, hi, x, want, bytes);
+            }
+            next = T.bcast(at, top);
+            ok = ok && hit;
         }
-        if (!hit) return false;
+        if (T.lane == 0) S.blo[d][b] = next;
     }
-    return true;
+    return ok;
 }
 
-// Unexplored anchor positions left at depth j of a search whose deepest open depth is `dcur`:
-// the not-yet-taken survivors of j's current chunk, then [pos[j], end[j]).  Survivors of a chunk
-// are taken lowest position first, so everything below the lowest pending one is explored.
+// Unexplored anchor positions left at depth j of a search that stopped at depth `dabort`: the
+// not-yet-taken candidates of j's current chunk, then [pos[j], end[j]).  Candidates of a chunk are
+// taken lowest position first, so everything below the lowest pending one is explored.
 template <int N>
-__device__ __forceinline__ void remainder_at(const State<N> &S, int j, int dcur, uint32_t &from, uint32_t &to) {
+__device__ __forceinline__ void remainder_at(const State<N> &S, int j, int dabort, uint32_t &from, uint32_t &to) {
     to = S.end[j];
     const uint32_t m = S.mask[j] | S.rest[j];
-    from = (j == dcur || m == 0) ? S.pos[j] : S.base[j] + (uint32_t)(__ffs(m) - 1);
+    from = (j == dabort || m == 0) ? S.pos[j] : S.base[j] + (uint32_t)(__ffs(m) - 1);
     if (from > to) from = to;
-}
-
-// Lane 0: a free group slot for v's split search (CAS 0 -> 1, the donor being its first unit), or
-// kNoGroup when none is found within a few tries.
-__device__ __forceinline__ uint32_t claim_group(const SearchParams &prm, uint32_t *cnt) {
-    for (int a = 0; a < 16; ++a) {
-        const uint32_t g = atomicAdd(&cnt[kCntGroupCursor * kCntStride], 1u) & (prm.gcap - 1);
-        if (atomicCAS(&prm.groups[g], 0u, 1u) == 0u) {
-            atomicAdd(&cnt[kCntGroups * kCntStride], 1u);
-            return g;
-        }
-    }
-    return kNoGroup;
-}
-
-// Team-uniform: reserves k consecutive ring positions (k <= G); returns the first, or ~0u when the
-// ring has no k free slots after them (or the claim keeps losing to other producers).
-template <int G>
-__device__ __forceinline__ uint32_t reserve_slots(const Team<G> &T, const SearchParams &prm, uint32_t k) {
-    const uint32_t m = prm.qcap - 1;
-    for (int a = 0; a < 8; ++a) {
-        uint32_t t = 0;
-        if (T.lane == 0) t = __ldcg(&prm.qctl[kQctlTail]);
-        t = T.bcast(t, 0);
-        int dif = 0;
-        if (T.lane < k) dif = (int)(ld_acquire(&prm.cells[(t + T.lane) & m].seq) - (t + T.lane));
-        if (T.any(dif < 0)) return ~0u;  // a slot still holds a task of the previous lap: full
-        if (T.any(dif > 0)) continue;    // another producer took these positions first
-        int won = 0;
-        if (T.lane == 0) won = atomicCAS(&prm.qctl[kQctlTail], t, t + k) == t;
-        if (T.bcast(won, 0)) return t;
-    }
-    return ~0u;
-}
-
-// Team-uniform: shares out the unexplored remainder of the shallowest open depth j (start <= j <=
-// dcur) as `demand` parts at most (at most G), each a task of the same group.  The current depth
-// keeps its first part; a shallower depth (whose pending branches lie above the search's current
-// path) is given away whole.  Returns true when tasks were queued; the local state then no longer
-// covers the donated positions.
-template <int G, int N>
-__device__ bool donate(const Team<G> &T, const Plan<N> &P, State<N> &S, const SearchParams &prm, uint32_t *cnt,
-                       Donor &dn, int start, int dcur, uint32_t demand) {
-    int j = -1;
-    uint32_t from = 0, to = 0;
-    for (int q = start; q <= dcur; ++q) {
-        uint32_t f, t;
-        remainder_at(S, q, dcur, f, t);
-        const uint32_t least = q == dcur ? prm.split_slice + 1 : 1;  // current depth: worth a part
-        if (t > f && t - f >= least) {
-            j = q;
-            from = f;
-            to = t;
-            break;
-        }
-    }
-    if (j < 0) return false;
-    const uint32_t R = to - from;
-    const uint32_t keep = j == dcur ? 1u : 0u;
-    uint32_t k = demand < (uint32_t)G ? demand : (uint32_t)G;
-    if (keep) {
-        const uint32_t fit = R / prm.split_slice;  // parts of at least split_slice positions, one kept
-        k = fit > 1 && k > fit - 1 ? fit - 1 : (fit > 1 ? k : 0u);
-    } else {
-        k = k < R ? k : R;
-    }
-    if (k == 0) return false;
-    // R positions in k + keep parts, the first `rem` of them one longer: part q is
-    // [from + q * base + min(q, rem), from + (q + 1) * base + min(q + 1, rem)), never empty
-    const uint32_t parts = k + keep, base = R / parts, rem = R % parts;
-    uint32_t ok = 1;
-    if (T.lane == 0 && dn.group == kNoGroup) {
-        dn.group = claim_group(prm, cnt);
-        ok = dn.group != kNoGroup;
-    }
-    dn.group = T.bcast(dn.group, 0);
-    if (!T.bcast(ok, 0)) {
-        if (T.lane == 0) atomicAdd(&cnt[kCntRefused * kCntStride], 1u);
-        return false;
-    }
-    const uint32_t t0 = reserve_slots(T, prm, k);
-    if (t0 == ~0u) {
-        if (T.lane == 0) atomicAdd(&cnt[kCntRefused * kCntStride], 1u);
-        return false;
-    }
-    if (T.lane == 0) {
-        // the units count before any of them can be taken (and finish)
-        atomicAdd(&prm.groups[dn.group], k);
-        atomicAdd(&cnt[kCntWork * kCntStride], k);
-        atomicAdd(&cnt[kCntTasks * kCntStride], k);
-        atomicMax(&cnt[kCntQueueMax * kCntStride], t0 + k - __ldcg(&prm.qctl[kQctlHead]));
-    }
-    const uint32_t cut = from + keep * base + (keep < rem ? keep : rem);
-    if (T.lane < k) {
-        const uint32_t q = T.lane + keep;
-        const uint32_t lo = from + q * base + (q < rem ? q : rem);
-        const uint32_t hi = from + (q + 1) * base + (q + 1 < rem ? q + 1 : rem);
-        QueueCell &c = prm.cells[(t0 + T.lane) & (prm.qcap - 1)];
-        SplitTask &task = c.task;
-        task.pat = dn.p;
-        task.u = (uint16_t)dn.u;
-        task.depth = (uint8_t)j;
-        task.pad = 0;
-        task.v = dn.v;
-        task.lo = lo;
-        task.hi = hi;
-        task.group = dn.group;
-        for (int q2 = 0; q2 < kMaxN; ++q2) task.prefix[q2] = q2 < j && q2 < N ? S.emb[P.order[q2]] : 0u;
-        __threadfence();
-        st_release(&c.seq, t0 + T.lane + 1);
-    }
-    T.sync();
-    if (T.lane == 0) {
-        // the donated positions leave this search: depth j ends at `cut`, and survivors of its
-        // current chunk at or past `cut` are dropped
-        S.end[j] = cut;
-        if (j != dcur) {
-            const uint32_t b0 = S.base[j];
-            const uint32_t keep_bits = cut <= b0 ? 0u : (cut - b0 >= 32 ? 0xffffffffu : (1u << (cut - b0)) - 1u);
-            S.mask[j] &= keep_bits;
-            S.rest[j] &= keep_bits;
-        }
-    }
-    T.sync();
-    return true;
 }
 
 // Depth-first search for one embedding that extends the partial embedding of depths < start
 // (S.emb[order[0..start-1]]).  With `slice`, depth `start` scans only anchor positions [lo, hi).
-// The search never backtracks above `start`.  Returns kCancel when `cancel` says the search no
-// longer matters, kAbandon when it reaches the pass's step budget (it is retried from the start
-// by the next pass, with a larger budget).  In the last pass (no budget) the search looks every
-// kCheckEvery chunk steps at the teams waiting for work and may share out part of its remainder
-// (donate); a first depth longer than hub_span is shared out at once.  A chunk is G consecutive
-// anchor positions.
+// The search never backtracks above `start`.  Returns kAbort once `budget` chunk evaluations are
+// exceeded (budget 0: unlimited), or at once when the first depth of an unsliced search is longer
+// than `hub_span` (hub_span 0: never); `abort_depth` then says where it stopped.  Returns kCancel
+// when `cancel` says the search no longer matters.  A chunk is G consecutive anchor positions.
 template <int G, int N>
-__device__ __forceinline__ int dfs(const Team<G> &T, const Graph &g, const Plan<N> &P, State<N> &S,
+__device__ __forceinline__ int dfs(const Team<G> &T, const Graph &g, const Plan<N> &P, State<N> &S, Tile<G> &tile,
                                    const uint32_t *__restrict__ dom, const uint32_t *found, const uint32_t *failed,
-                                   int start, bool slice, uint32_t lo, uint32_t hi, const Cancel &cancel,
-                                   const SearchParams &prm, uint32_t *cnt, Donor &dn, uint32_t &steps,
-                                   uint32_t &bytes, uint32_t &isects) {
+                                   int start, bool slice, uint32_t lo, uint32_t hi, uint32_t budget,
+                                   uint32_t hub_span, uint32_t ratio, const Cancel &cancel, uint32_t &steps,
+                                   int &abort_depth, uint32_t &bytes, uint32_t &isects) {
     const int n = P.n;
-    setup_depth(T, g, P, S, start, bytes);
+    setup_depth(T, g, P, S, start, ratio, bytes);
     if (slice) {
         if (T.lane == 0) {
             S.pos[start] = lo;
             S.end[start] = hi;
         }
         T.sync();
+    } else if (hub_span && S.end[start] - S.pos[start] > hub_span) {
+        abort_depth = start;  // a hub's first depth: split before any step
+        return kAbort;
     }
-    const bool share = prm.split && prm.budget == 0;
-    if (share && prm.hub_parts > 1 && !slice && S.end[start] - S.pos[start] > prm.hub_span) {
-        int room = 0;
-        if (T.lane == 0) room = __ldcg(&prm.qctl[kQctlTail]) - __ldcg(&prm.qctl[kQctlHead]) < prm.soft_cap;
-        if (T.bcast(room, 0)) donate(T, P, S, prm, cnt, dn, start, start, prm.hub_parts - 1);
-    }
-    // look at cancellation and demand every kCheckEvery chunk steps, or every share_steps steps
-    // when that is smaller (a test setting that makes short searches share work too)
-    const uint32_t every = share && prm.share_steps && prm.share_steps < kCheckEvery ? prm.share_steps : kCheckEvery;
-    uint32_t checked = 0;
+    const uint32_t every = budget && budget < kCheckEvery ? budget : kCheckEvery;
     int d = start;
     for (;;) {
         const uint32_t mk = S.mask[d], mr = S.rest[d];
@@ -716,29 +647,23 @@ __device__ __forceinline__ int dfs(const Team<G> &T, const Graph &g, const Plan<
                 --d;
                 continue;
             }
-            if (prm.budget && steps >= prm.budget) return kAbandon;
-            if (steps != checked && steps % every == 0) {
-                checked = steps;
+            if (budget && steps >= budget) {
+                abort_depth = d;
+                return kAbort;
+            }
+            if (steps && steps % every == 0) {
                 int c = 0;
-                uint32_t demand = 0;
                 if (T.lane == 0) {
                     c = (__ldcg(cancel.found_word) & cancel.bit) || __ldcg(&cancel.ps->state) != kRunning ||
                         (!cancel.exact && ((__ldcg(&cancel.ps->done_mask) >> cancel.u) & 1u));
-                    if (!c && share) {
-                        const uint32_t idle = __ldcg(&cnt[kCntIdle * kCntStride]);
-                        const uint32_t qd = __ldcg(&prm.qctl[kQctlTail]) - __ldcg(&prm.qctl[kQctlHead]);
-                        demand = idle > qd ? idle - qd : 0u;
-                        if (!demand && prm.share_steps && steps >= prm.share_steps && qd < prm.soft_cap) demand = 1;
-                    }
                 }
                 if (T.bcast(c, 0)) return kCancel;
-                demand = T.bcast(demand, 0);
-                if (demand && donate(T, P, S, prm, cnt, dn, start, d, demand)) continue;  // re-read the state
             }
             const uint32_t idx = pos + T.lane;
             uint32_t x = 0;
             bool known = false;
-            const bool ok = idx < end && check_candidate(g, P, S, dom, found, failed, d, idx, x, known, bytes);
+            bool ok = idx < end && check_candidate(g, P, S, dom, found, failed, d, idx, x, known, bytes);
+            ok = intersect_others(T, g, P, S, tile, d, x, ok, bytes);
             const uint32_t bal = T.ballot(ok);
             const uint32_t pref = kFoundFirst ? T.ballot(ok && known) : 0u;
             ++steps;
@@ -775,8 +700,94 @@ __device__ __forceinline__ int dfs(const Team<G> &T, const Graph &g, const Plan<
         bytes += 4;  // re-read of the chosen neighbour id
         if (!TFSM_IN(8, d + 1, n)) return kFail;
         ++d;
-        setup_depth(T, g, P, S, d, bytes);
+        setup_depth(T, g, P, S, d, ratio, bytes);
     }
+}
+
+// Claims `k` consecutive slots below `limit` with one atomicAdd (no retry loop, so no spurious
+// failure under contention); false when they do not all fit.  The counter may then pass `limit`
+// (readers clamp it to the buffer size); a failed claim [first, first + k) still owns its slots
+// that lie inside the buffer and must fill them (split tasks: with null tasks).  A counter already
+// at `limit` is not advanced, so it passes `limit` by at most one claim per running team.
+__device__ __forceinline__ bool reserve(uint32_t *counter, uint32_t k, uint32_t limit, uint32_t &first) {
+    if (__ldcg(counter) >= limit) {
+        first = 0xffffffffu;
+        return false;
+    }
+    first = atomicAdd(counter, k);
+    return first <= limit && k <= limit - first;
+}
+
+// Team-uniform claim of `k` slots below `limit`; the slots of a failed claim inside the buffer
+// (`cap`) become null tasks.
+template <int G>
+__device__ __forceinline__ bool claim_tasks(const Team<G> &T, SplitTask *out, uint32_t *out_count, uint32_t k,
+                                            uint32_t limit, uint32_t cap, uint32_t &t0) {
+    int ok = 0;
+    if (T.lane == 0) ok = reserve(out_count, k, limit, t0) ? 1 : 0;
+    ok = T.bcast(ok, 0);
+    t0 = T.bcast(t0, 0);
+    if (!ok && t0 < cap) {
+        const uint32_t e = (uint64_t)t0 + k < cap ? t0 + k : cap;
+        for (uint32_t q = t0 + T.lane; q < e; q += G) out[q].pat = kNullTask;
+    }
+    return ok != 0;
+}
+
+// Writes the unexplored remainder of the current search (depths start..dabort) as split tasks:
+// sliced (`slice` anchor positions each) below `limit`; when that does not fit, compact (one task
+// per depth, re-split by later rounds) below limit + slack.  Returns how many were written; 0 when
+// neither fits (then nothing is written).
+template <int G, int N>
+__device__ uint32_t emit_remainder(const Team<G> &T, const Plan<N> &P, const State<N> &S, uint32_t p, int u,
+                                   uint32_t v, int start, int dabort, uint32_t group, uint32_t slice, SplitTask *out,
+                                   uint32_t *out_count, uint32_t cap, uint32_t limit, uint32_t slack, uint64_t m2) {
+    uint32_t total = 0, depths = 0;
+    for (int j = start; j <= dabort; ++j) {
+        uint32_t f, t;
+        remainder_at(S, j, dabort, f, t);
+        total += t > f ? (t - f - 1) / slice + 1 : 0u;
+        depths += t > f ? 1u : 0u;
+    }
+    if (total == 0) return 0;
+    uint32_t t0 = 0;
+    if (!claim_tasks(T, out, out_count, total, limit, cap, t0)) {
+        if (!claim_tasks(T, out, out_count, depths, limit + slack, cap, t0)) return 0;
+        slice = 0xffffffffu;  // compact: one task per non-empty depth
+        total = depths;
+    }
+    for (uint32_t k = T.lane; k < total; k += G) {
+        uint32_t acc = 0, f = 0, t = 0, c = 0;
+        int j = start;
+        for (; j <= dabort; ++j) {
+            remainder_at(S, j, dabort, f, t);
+            c = t > f ? (t - f - 1) / slice + 1 : 0u;
+            if (k < acc + c) break;
+            acc += c;
+        }
+        SplitTask task;
+        task.pat = p;
+        task.u = (uint16_t)u;
+        task.depth = (uint8_t)j;
+        task.pad = 0;
+        task.v = v;
+        task.lo = f + (k - acc) * slice;  // k - acc is 0 when compact
+        task.hi = t - task.lo > slice ? task.lo + slice : t;
+        task.group = group;
+        for (int q = 0; q < kMaxN; ++q) task.prefix[q] = q < j && q < N ? S.emb[P.order[q]] : 0u;
+        if (TFSM_IN(14, t0 + k, cap) && TFSM_IN(48, task.hi, m2 + 1)) out[t0 + k] = task;
+    }
+    return total;
+}
+
+// Anchor positions per task when a search's remainder is split: split_slice, or, for a hub's first
+// depth split before any step, an even share among hub_parts tasks.
+__device__ __forceinline__ uint32_t slice_for(const SearchParams &prm, uint32_t steps, uint32_t first_len) {
+    if (steps == 0 && prm.hub_parts > 1) {
+        const uint32_t s = (first_len + prm.hub_parts - 1) / prm.hub_parts;
+        return s > prm.split_slice ? s : prm.split_slice;
+    }
+    return prm.split_slice;
 }
 
 // Lane 0: v has no embedding as u (nor as any vertex automorphic to u).
@@ -824,33 +835,6 @@ __device__ __forceinline__ void mark_found(const Team<G> &T, const Plan<N> &P, c
     T.sync();
 }
 
-// End of one unit of a search (the search itself, or one of its tasks), after mark_found when it
-// found an embedding.  Without a group the unit is the whole search: a failure is final.  In a
-// group, the unit that finishes last decides: v fails when no unit found an embedding and none
-// stopped without an answer.
-template <int G, int N>
-__device__ __forceinline__ void finish_unit(const Team<G> &T, const Plan<N> &P, const SearchParams &prm,
-                                            PatStatus &st, uint32_t *__restrict__ failed, const uint32_t *found,
-                                            const Donor &dn, int r, uint32_t fo, uint32_t fbit, bool exact) {
-    if (T.lane == 0) {
-        if (dn.group == kNoGroup) {
-            if (r == kFail) fail_vertex(P, st, failed, dn.u, dn.v, prm.tau, exact);
-        } else {
-            uint32_t *gw = &prm.groups[dn.group];
-            if ((r == kCancel || r == kAbandon) && !(__ldcg(found + fo) & fbit)) atomicOr(gw, kGroupIncomplete);
-            __threadfence();  // this unit's found / incomplete marks before its completion
-            const uint32_t old = atomicSub(gw, 1u);
-            if ((old & ~kGroupIncomplete) == 1u) {
-                __threadfence();
-                atomicExch(gw, 0u);  // the slot is free again
-                if (!(old & kGroupIncomplete) && !(__ldcg(found + fo) & fbit))
-                    fail_vertex(P, st, failed, dn.u, dn.v, prm.tau, exact);
-            }
-        }
-    }
-    T.sync();
-}
-
 // Team-uniform: lane 0 reads the shared flags and broadcasts the decision.
 template <int G>
 __device__ __forceinline__ bool pattern_stops(const Team<G> &T, const PatStatus &st, int u, bool exact) {
@@ -862,233 +846,239 @@ __device__ __forceinline__ bool pattern_stops(const Team<G> &T, const PatStatus 
     return T.bcast(stop, 0) != 0;
 }
 
-// Team-uniform: takes the oldest task off the ring into `t` (fields the team needs), or false
-// when the ring looks empty.
-template <int G>
-__device__ __forceinline__ bool pop_task(const Team<G> &T, const SearchParams &prm, SplitTask &t) {
-    const uint32_t m = prm.qcap - 1;
-    uint32_t pos = 0;
-    int got = 0;
-    if (T.lane == 0) {
-        for (int a = 0; a < 16; ++a) {
-            pos = __ldcg(&prm.qctl[kQctlHead]);
-            const int dif = (int)(ld_acquire(&prm.cells[pos & m].seq) - (pos + 1));
-            if (dif < 0) break;  // empty (or its producer has not finished writing it)
-            if (dif > 0) continue;
-            if (atomicCAS(&prm.qctl[kQctlHead], pos, pos + 1) == pos) {
-                got = 1;
-                break;
-            }
-        }
-    }
-    if (!T.bcast(got, 0)) return false;
-    pos = T.bcast(pos, 0);
-    QueueCell &c = prm.cells[pos & m];
-    (void)ld_acquire(&c.seq);  // every lane synchronises with the producer before reading
-    t.pat = __ldcg(&c.task.pat);
-    const uint32_t w1 = __ldcg(reinterpret_cast<const uint32_t *>(&c.task.u));
-    t.u = (uint16_t)(w1 & 0xffffu);
-    t.depth = (uint8_t)((w1 >> 16) & 0xffu);
-    t.v = __ldcg(&c.task.v);
-    t.lo = __ldcg(&c.task.lo);
-    t.hi = __ldcg(&c.task.hi);
-    t.group = __ldcg(&c.task.group);
-    // lane q % G keeps prefix[q] (a team of G lanes searches patterns of at most 2G vertices)
-    t.prefix[0] = T.lane < kMaxN ? __ldcg(&c.task.prefix[T.lane]) : 0u;
-    t.prefix[1] = T.lane + G < kMaxN ? __ldcg(&c.task.prefix[T.lane + G]) : 0u;
-    __threadfence();
-    T.sync();
-    if (T.lane == 0) st_release(&c.seq, pos + prm.qcap);  // the slot goes to the next lap
-    return true;
-}
-
 }  // namespace
 
-// The search launch.  Each team of G lanes takes, in this order: a task another team shared (it
-// completes a search already under way), the next work item (a run of bitmap words of one
-// representative's domain: one search per still-undecided candidate), or, when both are gone,
-// waits for a task while any unit of work is still outstanding.  Counters: kCnt* in
-// dev_common.cuh, zero on entry.
+// One search pass.  Split tasks of round 0 go to `splits` (the first buffer).  Each team of G lanes
+// claims its own items.  Outside the last pass, a search whose remainder finds no room is set aside
+// (neither found nor failed), and a team starts no more searches once the first round's share of
+// the buffer is full: the next pass, with larger budgets, takes up what is left.
 template <int G>
 __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const PatDesc *__restrict__ descs,
                                                               PatStatus *__restrict__ st,
                                                               const SearchItem *__restrict__ items, SearchParams prm,
-                                                              uint32_t *__restrict__ cnt,
+                                                              uint32_t *__restrict__ counters,
                                                               const uint32_t *__restrict__ dom,
                                                               uint32_t *__restrict__ found,
-                                                              uint32_t *__restrict__ failed) {
+                                                              uint32_t *__restrict__ failed,
+                                                              SplitTask *__restrict__ splits,
+                                                              SplitGroup *__restrict__ groups) {
     constexpr int N = TeamMaxN<G>::value;
     constexpr int kTeams = kSearchWarps * 32 / G;
     __shared__ Plan<N> plans[kTeams];
     __shared__ State<N> states[kTeams];
-    // a later pass whose predecessor set no search aside has nothing to do (uniform per block)
-    if (prm.prev && __ldcg(&prm.prev[kCntAbandoned * kCntStride]) == 0u) return;
+    __shared__ Tile<G> tiles[kTeams];
     const Team<G> T(threadIdx.x & 31);
     Plan<N> &P = plans[threadIdx.x / G];
     State<N> &S = states[threadIdx.x / G];
+    Tile<G> &tile = tiles[threadIdx.x / G];
     if (T.lane == 0) P.key = 0xffffffffu;
     T.sync();
     const bool exact = prm.exact != 0;
-    const bool share = prm.split && prm.budget == 0;  // only the last pass shares work
-    const uint32_t n_claims = prm.n_items << prm.parts_log2;
-    bool items_left = true, idle = false;
-    uint32_t waits = 0, nap = kNapMin;
+    const uint32_t budget = prm.split ? prm.step_budget : 0u;
+    const uint32_t hub_span = prm.split && prm.hub_parts > 1 ? prm.hub_span : 0u;
     for (;;) {
-        // ---- a shared task ----
-        SplitTask t;
-        if (share && pop_task(T, prm, t)) {
-            if (idle && T.lane == 0) atomicSub(&cnt[kCntIdle * kCntStride], 1u);
-            idle = false;
-            waits = 0;
-            nap = kNapMin;
-            const uint32_t p = t.pat;
-            const int u = t.u, depth = t.depth;
-            Donor dn{p, u, t.v, t.group};
-            // a task with fields out of range would be an engine fault: counted, never dereferenced
-            const bool sane = p < prm.n_pats && t.group < prm.gcap && u < N && depth < N && t.lo <= t.hi &&
-                              t.hi <= g.m2;
-            if (!sane && T.lane == 0) atomicAdd(&cnt[kCntBadTask * kCntStride], 1u);
-            if (sane && TFSM_IN(16, p, prm.n_pats) && TFSM_IN(17, t.group, prm.gcap) && TFSM_IN(21, u, N) &&
-                TFSM_IN(23, descs[p].n, N + 1)) {
-                load_plan(T, P, descs[p], p, u, prm.words);
-                PatStatus &ps = st[p];
-                const uint32_t xl = t.v - P.lstart[u];
-                const uint32_t o = P.off[u] + (xl >> 5);
-                const uint32_t bit = 1u << (xl & 31);
-                int r = kCancel;
-                if (TFSM_IN(18, o, prm.words) && TFSM_IN(44, depth, P.n) && TFSM_IN(45, t.lo, (uint64_t)t.hi + 1) &&
-                    TFSM_IN(47, t.hi, g.m2 + 1) && TFSM_IN(46, depth, N)) {
-                    if (!pattern_stops(T, ps, u, exact) && !(T.word(found + o) & bit)) {
-                        if ((int)T.lane < depth) S.emb[P.order[T.lane]] = t.prefix[0];
-                        if ((int)(T.lane + G) < depth) S.emb[P.order[T.lane + G]] = t.prefix[1];
-                        T.sync();
-                        uint32_t steps = 0, bytes = 12, isects = 0;
-                        const Cancel cancel{found + o, bit, &ps, u, exact};
-                        r = dfs(T, g, P, S, dom, found, failed, depth, true, t.lo, t.hi, cancel, prm, cnt, dn, steps,
-                                bytes, isects);
-                        if (r == kFound) mark_found(T, P, S, ps, found, prm.tau, exact);
-                        const unsigned long long wb = T.sum(bytes);
-                        if (T.lane == 0) {
-                            atomicAdd(&ps.steps, (unsigned long long)steps);
-                            atomicAdd(&ps.isects, (unsigned long long)isects);
-                            atomicAdd(&ps.bytes, wb);
-                            atomicMax(&ps.max_steps, (unsigned long long)steps);
-                            atomicAdd(&ps.steps_u[u], (unsigned long long)steps);
-                        }
-                    }
-                    finish_unit(T, P, prm, ps, failed, found, dn, r, o, bit, exact);
+        uint32_t it = 0;
+        if (T.lane == 0) it = atomicAdd(&counters[0], 1u);
+        it = T.bcast(it, 0);
+        if (it >= (prm.n_items << prm.parts_log2)) break;
+        const SearchItem item = items[it >> prm.parts_log2];
+        const uint32_t pmask = part_mask(it & ((1u << prm.parts_log2) - 1), prm.parts_log2);
+        const uint32_t p = item.pat;
+        const int u = item.u;
+        if (!TFSM_IN(12, p, prm.n_pats) || !TFSM_IN(20, u, N)) continue;
+        if (!TFSM_IN(22, descs[p].n, N + 1)) continue;
+        load_plan(T, P, descs[p], p, u, prm.words);
+        PatStatus &ps = st[p];
+        unsigned long long n_search = 0, n_steps = 0, n_bytes = 0, max_steps = 0, n_isects = 0;
+        bool stop = false, stopped = false;
+        for (uint32_t word = item.word_lo; word < item.word_hi && !stop; ++word) {
+            if (pattern_stops(T, ps, u, exact)) break;
+            const uint32_t o = P.off[u] + word;
+            if (!TFSM_IN(13, o, prm.words)) break;
+            uint32_t cand = T.word(dom + o) & ~T.word(found + o) & ~T.word(failed + o) & pmask;
+            while (cand) {
+                const int b = __ffs(cand) - 1;
+                cand &= cand - 1;
+                if ((T.word(found + o) >> b) & 1u) continue;
+                if (pattern_stops(T, ps, u, exact)) {
+                    stop = true;
+                    break;
                 }
-            }
-            if (T.lane == 0) atomicSub(&cnt[kCntWork * kCntStride], 1u);
-            T.sync();
-            continue;
-        }
-        // ---- the next work item ----
-        if (items_left) {
-            uint32_t it = 0;
-            if (T.lane == 0) {
-                atomicAdd(&cnt[kCntWork * kCntStride], 1u);  // before the claim: no team sees the launch idle meanwhile
-                it = atomicAdd(&cnt[kCntItem * kCntStride], 1u);
-                if (it >= n_claims) atomicSub(&cnt[kCntWork * kCntStride], 1u);
-            }
-            it = T.bcast(it, 0);
-            if (it >= n_claims) {
-                items_left = false;
-                continue;
-            }
-            const SearchItem item = items[it >> prm.parts_log2];
-            const uint32_t pmask = part_mask(it & ((1u << prm.parts_log2) - 1), prm.parts_log2);
-            const uint32_t p = item.pat;
-            const int u = item.u;
-            if (TFSM_IN(12, p, prm.n_pats) && TFSM_IN(20, u, N) && TFSM_IN(22, descs[p].n, N + 1)) {
-                load_plan(T, P, descs[p], p, u, prm.words);
-                PatStatus &ps = st[p];
-                unsigned long long n_search = 0, n_steps = 0, n_bytes = 0, max_steps = 0, n_isects = 0;
-                uint32_t n_abandoned = 0;
-                bool stop = false;
-                for (uint32_t word = item.word_lo; word < item.word_hi && !stop; ++word) {
-                    if (pattern_stops(T, ps, u, exact)) break;
-                    const uint32_t o = P.off[u] + word;
-                    if (!TFSM_IN(13, o, prm.words)) break;
-                    uint32_t cand = T.word(dom + o) & ~T.word(found + o) & ~T.word(failed + o) & pmask;
-                    while (cand) {
-                        const int b = __ffs(cand) - 1;
-                        cand &= cand - 1;
-                        if ((T.word(found + o) >> b) & 1u) continue;
-                        if (pattern_stops(T, ps, u, exact)) {
-                            stop = true;
-                            break;
-                        }
-                        const uint32_t v = P.lstart[u] + word * 32 + b;
-                        if (T.lane == 0) S.emb[u] = v;
-                        T.sync();
-                        uint32_t steps = 0, bytes = 12, isects = 0;  // + domain, found and failed words of v
-                        ++n_search;
-                        Donor dn{p, u, v, kNoGroup};
-                        const Cancel cancel{found + o, 1u << b, &ps, u, exact};
-                        const int r = dfs(T, g, P, S, dom, found, failed, 1, false, 0, 0, cancel, prm, cnt, dn, steps,
-                                          bytes, isects);
+                if (budget && !prm.last) {
+                    // the first split round's share of the buffer is full: this team starts no
+                    // more searches in this pass; the next pass takes up what is left
+                    int full = 0;
+                    if (T.lane == 0) full = __ldcg(&counters[2]) >= prm.search_fill;
+                    if (T.bcast(full, 0)) {
+                        stop = stopped = true;
+                        break;
+                    }
+                }
+                const uint32_t v = P.lstart[u] + word * 32 + b;
+                if (T.lane == 0) S.emb[u] = v;
+                T.sync();
+                uint32_t steps = 0, bytes = 12, isects = 0;  // + domain, found and failed words of v
+                int adepth = 0;
+                ++n_search;
+                const Cancel cancel{found + o, 1u << b, &ps, u, exact};
+                int r = dfs(T, g, P, S, tile, dom, found, failed, 1, false, 0, 0, budget, hub_span, prm.isect_ratio,
+                            cancel, steps, adepth, bytes, isects);
+                if (r == kAbort) {
+                    // The unexplored remainder becomes tasks for the split rounds, grouped so that
+                    // the last one to finish can decide v.
+                    const uint32_t first_len = S.end[1] - S.pos[1];
+                    uint32_t g0 = 0;
+                    int okg = 0;
+                    if (T.lane == 0)
+                        okg = reserve(&counters[1], 1, prm.group_cap, g0) && TFSM_IN(15, g0, prm.group_cap) ? 1 : 0;
+                    okg = T.bcast(okg, 0);
+                    g0 = T.bcast(g0, 0);
+                    uint32_t added = 0;
+                    if (okg)
+                        added = emit_remainder(T, P, S, p, u, v, 1, adepth, g0, slice_for(prm, steps, first_len),
+                                               splits, &counters[2], prm.split_cap, prm.search_fill, prm.split_slack,
+                                               g.m2);
+                    if (T.lane == 0 && okg) {  // read only by the split rounds, which run after this kernel
+                        groups[g0].pat = p;
+                        groups[g0].u = (uint16_t)u;
+                        groups[g0].v = v;
+                        groups[g0].pending = added;
+                        groups[g0].incomplete = 0;
+                    }
+                    if (added || !prm.last) {
+                        if (!added && T.lane == 0) atomicAdd(&counters[kCntAbandoned], 1u);  // buffers full
                         n_steps += steps;
                         n_isects += isects;
-                        max_steps = steps > max_steps ? steps : max_steps;
                         n_bytes += T.sum(bytes);
-                        if (r == kFound) mark_found(T, P, S, ps, found, prm.tau, exact);
-                        n_abandoned += r == kAbandon ? 1u : 0u;
-                        finish_unit(T, P, prm, ps, failed, found, dn, r, o, 1u << b, exact);
+                        continue;  // decided by the split rounds, or by the next pass
                     }
+                    // buffers full, last pass: finish this search here without a budget
+                    if (T.lane == 0) S.emb[u] = v;
+                    T.sync();
+                    r = dfs(T, g, P, S, tile, dom, found, failed, 1, false, 0, 0, 0, 0, prm.isect_ratio, cancel, steps,
+                            adepth, bytes, isects);
                 }
-                if (T.lane == 0 && n_abandoned) atomicAdd(&cnt[kCntAbandoned * kCntStride], n_abandoned);
-                if (T.lane == 0 && n_search) {
-                    atomicAdd(&ps.searches, n_search);
-                    atomicAdd(&ps.steps, n_steps);
-                    atomicAdd(&ps.isects, n_isects);
-                    atomicAdd(&ps.bytes, n_bytes);
-                    atomicMax(&ps.max_steps, max_steps);
-                    atomicAdd(&ps.steps_u[u], n_steps);
-                    atomicAdd(&ps.searches_u[u], (uint32_t)n_search);
-                }
+                n_steps += steps;
+                n_isects += isects;
+                max_steps = steps > max_steps ? steps : max_steps;
+                n_bytes += T.sum(bytes);
+                if (r == kFound) mark_found(T, P, S, ps, found, prm.tau, exact);
+                else if (r == kFail && T.lane == 0) fail_vertex(P, ps, failed, u, v, prm.tau, exact);
+                T.sync();
             }
-            if (T.lane == 0) atomicSub(&cnt[kCntWork * kCntStride], 1u);
-            T.sync();
-            continue;
         }
-        // ---- nothing to take: done when no unit is outstanding, else wait for a shared task (at
-        // most max_idle teams wait; the others end) ----
-        if (!share) break;
-        int done = 0;
-        if (T.lane == 0) done = __ldcg(&cnt[kCntWork * kCntStride]) == 0u;
-        if (T.bcast(done, 0)) break;
-        if (!idle) {
-            int over = 0;
-            if (T.lane == 0 && atomicAdd(&cnt[kCntIdle * kCntStride], 1u) >= prm.max_idle) {
-                atomicSub(&cnt[kCntIdle * kCntStride], 1u);
-                over = 1;
-            }
-            if (T.bcast(over, 0)) break;
+        if (T.lane == 0 && n_search) {
+            atomicAdd(&ps.searches, n_search);
+            atomicAdd(&ps.steps, n_steps);
+            atomicAdd(&ps.isects, n_isects);
+            atomicAdd(&ps.bytes, n_bytes);
+            atomicMax(&ps.max_steps, max_steps);
+            atomicAdd(&ps.steps_u[u], n_steps);
+            atomicAdd(&ps.searches_u[u], (uint32_t)n_search);
         }
-        idle = true;
-        if (++waits > kMaxWaits) {
-            if (T.lane == 0) atomicAdd(&cnt[kCntWaitExpired * kCntStride], 1u);
-            break;
+        if (stopped) {
+            if (T.lane == 0) atomicAdd(&counters[kCntAbandoned], 1u);
+            return;
         }
-#ifdef TFSM_SIMT_EMULATION
-        tfsm_emu_nap(nap);
-#else
-        __nanosleep(nap);
-#endif
-        nap = nap < kNapMax ? 2 * nap : kNapMax;
     }
-    if (idle && T.lane == 0) atomicSub(&cnt[kCntIdle * kCntStride], 1u);
 }
 
-// Sets every ring slot free for its first lap and both positions to zero (once per engine; the
-// ring is empty again after every launch).
-__global__ void k_queue_init(QueueCell *cells, uint32_t qcap, uint32_t *qctl, uint32_t *groups, uint32_t gcap) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t k = i; k < qcap; k += stride) cells[k].seq = k;
-    for (uint32_t k = i; k < gcap; k += stride) groups[k] = 0;
-    if (i == 0) qctl[kQctlHead] = qctl[kQctlTail] = 0;
+// One split round: processes the tasks of round `round` (in `in`), searching each below its
+// partial embedding; a task that exceeds `budget` (0: never, as in the last round) emits its own
+// unexplored remainder into `out` for the next round, inside the same group.  Outside the last
+// pass, a remainder without room is set aside (the group is marked incomplete, so v stays
+// undecided for the next pass).
+template <int G>
+__global__ void __launch_bounds__(kSearchWarps * 32) k_split(Graph g, const PatDesc *__restrict__ descs,
+                                                             PatStatus *__restrict__ st, SearchParams prm,
+                                                             uint32_t *__restrict__ counters, int round,
+                                                             uint32_t budget, const uint32_t *__restrict__ dom,
+                                                             uint32_t *__restrict__ found,
+                                                             uint32_t *__restrict__ failed,
+                                                             const SplitTask *__restrict__ in,
+                                                             SplitTask *__restrict__ out,
+                                                             SplitGroup *__restrict__ groups) {
+    constexpr int N = TeamMaxN<G>::value;
+    constexpr int kTeams = kSearchWarps * 32 / G;
+    __shared__ Plan<N> plans[kTeams];
+    __shared__ State<N> states[kTeams];
+    __shared__ Tile<G> tiles[kTeams];
+    const Team<G> T(threadIdx.x & 31);
+    Plan<N> &P = plans[threadIdx.x / G];
+    State<N> &S = states[threadIdx.x / G];
+    Tile<G> &tile = tiles[threadIdx.x / G];
+    if (T.lane == 0) P.key = 0xffffffffu;
+    T.sync();
+    const bool exact = prm.exact != 0;
+    const uint32_t n_tasks = min(counters[2 + round], prm.split_cap);
+    for (;;) {
+        uint32_t it = 0;
+        if (T.lane == 0) it = atomicAdd(&counters[kClaimBase + round], 1u);
+        it = T.bcast(it, 0);
+        if (it >= n_tasks) break;
+        const SplitTask &t = in[it];  // fields read one by one; the prefix stays in memory
+        const uint32_t p = t.pat;
+        if (p == kNullTask) continue;  // a slot of a claim that did not fit
+        const int u = t.u;
+        const int depth = t.depth;
+        if (!TFSM_IN(16, p, prm.n_pats) || !TFSM_IN(17, t.group, prm.group_cap) || !TFSM_IN(21, u, N)) continue;
+        if (!TFSM_IN(23, descs[p].n, N + 1)) continue;
+        load_plan(T, P, descs[p], p, u, prm.words);
+        PatStatus &ps = st[p];
+        SplitGroup &grp = groups[t.group];
+        const uint32_t xl = t.v - P.lstart[u];
+        const uint32_t o = P.off[u] + (xl >> 5);
+        const uint32_t bit = 1u << (xl & 31);
+        if (!TFSM_IN(18, o, prm.words) || !TFSM_IN(44, depth, P.n) || !TFSM_IN(45, t.lo, (uint64_t)t.hi + 1) ||
+            !TFSM_IN(47, t.hi, g.m2 + 1) || !TFSM_IN(46, depth, N))
+            continue;
+        bool searched = false;
+        uint32_t added = 0;
+        if (!pattern_stops(T, ps, u, exact) && !(T.word(found + o) & bit)) {
+            for (int q = (int)T.lane; q < depth; q += G) S.emb[P.order[q]] = t.prefix[q];
+            T.sync();
+            uint32_t steps = 0, bytes = 12, isects = 0;
+            int adepth = 0;
+            const Cancel cancel{found + o, bit, &ps, u, exact};
+            int r = dfs(T, g, P, S, tile, dom, found, failed, depth, true, t.lo, t.hi, budget, 0, prm.isect_ratio,
+                        cancel, steps, adepth, bytes, isects);
+            if (r == kAbort) {
+                added = emit_remainder(T, P, S, p, u, t.v, depth, adepth, t.group, prm.split_slice, out,
+                                       &counters[2 + round + 1], prm.split_cap, prm.split_cap - prm.split_slack,
+                                       prm.split_slack, g.m2);
+                if (!added && !prm.last) {  // no room: v stays undecided for the next pass
+                    if (T.lane == 0) atomicAdd(&counters[kCntAbandoned], 1u);
+                    r = kCancel;
+                } else if (!added) {  // no room, last pass: finish the task here
+                    r = dfs(T, g, P, S, tile, dom, found, failed, depth, true, t.lo, t.hi, 0, 0, prm.isect_ratio,
+                            cancel, steps, adepth, bytes, isects);
+                }
+            }
+            if (r == kFound) mark_found(T, P, S, ps, found, prm.tau, exact);
+            const unsigned long long wb = T.sum(bytes);
+            if (T.lane == 0) {
+                atomicAdd(&ps.steps, (unsigned long long)steps);
+                atomicAdd(&ps.isects, (unsigned long long)isects);
+                atomicAdd(&ps.bytes, wb);
+                atomicMax(&ps.max_steps, (unsigned long long)steps);
+                atomicAdd(&ps.steps_u[u], (unsigned long long)steps);
+            }
+            searched = r != kCancel;
+        }
+        if (T.lane == 0) {
+            if (!searched && !(__ldcg(found + o) & bit)) atomicOr(&grp.incomplete, 1u);
+            if (added) atomicAdd(&grp.pending, added);  // before this task's own completion below
+            __threadfence();
+            const uint32_t left = atomicSub(&grp.pending, 1u) - 1;
+            if (left == 0) {
+                __threadfence();
+                // every task of the search finished without an embedding: v fails as u
+                if (!(__ldcg(found + o) & bit) && __ldcg(&grp.incomplete) == 0)
+                    fail_vertex(P, ps, failed, u, t.v, prm.tau, exact);
+            }
+        }
+        T.sync();
+    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -1157,36 +1147,34 @@ cudaError_t launch_refine(const Graph &g, const PatDesc *descs, PatStatus *st, c
     return cudaGetLastError();
 }
 
-cudaError_t launch_queue_init(QueueCell *cells, uint32_t qcap, uint32_t *qctl, uint32_t *groups, uint32_t gcap,
-                              cudaStream_t s) {
-    if (qcap == 0 || (qcap & (qcap - 1)) || gcap == 0 || (gcap & (gcap - 1))) return cudaErrorInvalidValue;
-    const uint32_t n = qcap > gcap ? qcap : gcap;
-    uint32_t blocks = (n + 255) / 256;
-    const uint32_t cap = (uint32_t)num_sms() * 4;
-    if (blocks > cap) blocks = cap;
-    TFSM_LAUNCH(k_queue_init, blocks, 256, s, cells, qcap, qctl, groups, gcap);
-    return cudaGetLastError();
-}
-
 namespace {
 
 template <int G>
 cudaError_t launch_search_t(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchItem *items,
                             const SearchParams &prm, uint32_t *counters, const uint32_t *dom, uint32_t *found,
-                            uint32_t *failed, cudaStream_t s) {
+                            uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<G>, kSearchWarps * 32, 0);
     if (per_sm <= 0) per_sm = 1;
-    // persistent: at most one block per resident slot (a waiting team must not hold back a block
-    // that has not started); without sharing, no more teams than claims
     uint64_t blocks = (uint64_t)num_sms() * (uint64_t)per_sm;
-    if (!prm.split) {
-        const uint64_t teams = (uint64_t)kSearchWarps * 32 / G;
-        const uint64_t need = (((uint64_t)prm.n_items << prm.parts_log2) + teams - 1) / teams;
-        if (blocks > need) blocks = need;
-    }
+    const uint64_t teams = (uint64_t)kSearchWarps * 32 / G;
+    const uint64_t need = (((uint64_t)prm.n_items << prm.parts_log2) + teams - 1) / teams;
+    if (blocks > need) blocks = need;
     TFSM_LAUNCH(k_search<G>, (unsigned)blocks, kSearchWarps * 32, s, g, descs, st, items, prm, counters, dom, found,
-                failed);
+                failed, splits, groups);
+    return cudaGetLastError();
+}
+
+template <int G>
+cudaError_t launch_split_t(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchParams &prm,
+                           uint32_t *counters, int round, uint32_t budget, const uint32_t *dom, uint32_t *found,
+                           uint32_t *failed, const SplitTask *in, SplitTask *out, SplitGroup *groups,
+                           cudaStream_t s) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_split<G>, kSearchWarps * 32, 0);
+    if (per_sm <= 0) per_sm = 1;
+    TFSM_LAUNCH(k_split<G>, (unsigned)(num_sms() * per_sm), kSearchWarps * 32, s, g, descs, st, prm, counters, round,
+                budget, dom, found, failed, in, out, groups);
     return cudaGetLastError();
 }
 
@@ -1194,14 +1182,14 @@ cudaError_t launch_search_t(const Graph &g, const PatDesc *descs, PatStatus *st,
 
 cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchItem *items,
                           const SearchParams &prm, uint32_t *counters, const uint32_t *dom, uint32_t *found,
-                          uint32_t *failed, cudaStream_t s) {
+                          uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s) {
     if (prm.n_items == 0) return cudaSuccess;
-    if (prm.split && (!prm.cells || !prm.qctl || !prm.groups || prm.qcap == 0 || (prm.qcap & (prm.qcap - 1)) ||
-                      prm.gcap == 0 || (prm.gcap & (prm.gcap - 1)) || prm.split_slice == 0))
+    if (prm.split && (!splits || !groups || prm.split_cap == 0 || prm.group_cap == 0 || prm.split_slice == 0))
         return cudaErrorInvalidValue;
     cudaError_t e;
-    if (prm.team_lanes == 8) e = launch_search_t<8>(g, descs, st, items, prm, counters, dom, found, failed, s);
-    else if (prm.team_lanes == 32) e = launch_search_t<32>(g, descs, st, items, prm, counters, dom, found, failed, s);
+    if (prm.team_lanes == 8) e = launch_search_t<8>(g, descs, st, items, prm, counters, dom, found, failed, splits, groups, s);
+    else if (prm.team_lanes == 32)
+        e = launch_search_t<32>(g, descs, st, items, prm, counters, dom, found, failed, splits, groups, s);
     else return cudaErrorInvalidValue;
 #ifdef TFSM_BOUNDS_CHECK
     if (e == cudaSuccess && cudaStreamSynchronize(s) != cudaSuccess) {
@@ -1217,6 +1205,28 @@ uint32_t resident_search_warps() {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<32>, kSearchWarps * 32, 0);
     if (per_sm <= 0) per_sm = 1;
     return (uint32_t)(num_sms() * per_sm * kSearchWarps);
+}
+
+cudaError_t launch_split_round(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchParams &prm,
+                               uint32_t *counters, int round, uint32_t budget, const uint32_t *dom, uint32_t *found,
+                               uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s) {
+    if (round < 0 || round >= kMaxRounds) return cudaErrorInvalidValue;
+    const SplitTask *in = splits + (size_t)(round % 2) * prm.split_cap;
+    SplitTask *out = splits + (size_t)((round + 1) % 2) * prm.split_cap;
+    if (round + 1 == kMaxRounds) budget = 0;  // the last possible round completes every task
+    cudaError_t e;
+    if (prm.team_lanes == 8)
+        e = launch_split_t<8>(g, descs, st, prm, counters, round, budget, dom, found, failed, in, out, groups, s);
+    else if (prm.team_lanes == 32)
+        e = launch_split_t<32>(g, descs, st, prm, counters, round, budget, dom, found, failed, in, out, groups, s);
+    else return cudaErrorInvalidValue;
+#ifdef TFSM_BOUNDS_CHECK
+    if (e == cudaSuccess && cudaStreamSynchronize(s) != cudaSuccess) {
+        std::fprintf(stderr, "tfsm checked build: fault in k_split\n");
+        return cudaGetLastError();
+    }
+#endif
+    return e;
 }
 
 }  // namespace dev

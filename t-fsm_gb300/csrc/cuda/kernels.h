@@ -24,17 +24,18 @@ cudaError_t launch_refine(const Graph &g, const PatDesc *descs, PatStatus *st, c
                           const uint64_t *prefix, uint32_t n_items, uint64_t total_words, uint32_t *dom,
                           uint64_t chk_words, int round, uint32_t tau, bool exact, cudaStream_t s);
 
-// The search launch: k_search over `prm.n_items` items, with work sharing through the ring and
-// group table that `prm` names when prm.split is set.  `counters` (kNumCounters x u32) must be zero
-// on entry; the ring must be empty (it is again after every launch that returned normally).
+// One search pass: k_search over `prm.n_items` items.  `counters` (kNumCounters x u32) must be
+// zero on entry; `splits` holds two buffers of prm.split_cap tasks each.
 cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchItem *items,
                           const SearchParams &prm, uint32_t *counters, const uint32_t *dom, uint32_t *found,
-                          uint32_t *failed, cudaStream_t s);
+                          uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s);
 
-// Empties the ring (every slot free for its first lap, both positions zero) and frees every group
-// slot.  qcap and gcap are powers of two.
-cudaError_t launch_queue_init(QueueCell *cells, uint32_t qcap, uint32_t *qctl, uint32_t *groups, uint32_t gcap,
-                              cudaStream_t s);
+// Split round `round` (0 <= round < kMaxRounds) of the pass whose counters are `counters`: the tasks
+// written for it by the previous phase, each with a step budget of `budget` chunk evaluations (0:
+// none).  Rounds run in order on one stream; round kMaxRounds - 1 has no step budget.
+cudaError_t launch_split_round(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchParams &prm,
+                               uint32_t *counters, int round, uint32_t budget, const uint32_t *dom, uint32_t *found,
+                               uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s);
 
 // Warps of k_search resident on the device at once (SMs x blocks per SM x warps per block).
 uint32_t resident_search_warps();

@@ -211,11 +211,8 @@ struct GpuEngine::Impl {
     PinnedBuf<dev::SearchItem> hitems;  // staging of the search items (rewritten each call)
     DevBuf<dev::SourceLevel> srcs;      // the earlier calls' pools read by this call's domain init
     DevBuf<uint32_t> counters;
-    // work-sharing ring and group table of the search launches (kept across launches: the ring is
-    // empty and every group slot free after each one)
-    DevBuf<dev::QueueCell> cells;
-    DevBuf<uint32_t> qctl, groups;
-    uint32_t qcap = 0, gcap = 0;
+    DevBuf<dev::SplitTask> splits;  // two buffers of split tasks (ping-pong between rounds)
+    DevBuf<dev::SplitGroup> groups;
     std::vector<PatStatus> hstatus;
     int device = 0;
     std::shared_ptr<BufferCache> cache = std::make_shared<BufferCache>();
@@ -325,13 +322,14 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     TFSM_CK(cudaEventCreate(&I.ev1));
     TFSM_CK(cudaEventCreate(&I.ev_mid));
     I.row_off.ensure(off.size());
-    I.col.ensure(col.size());
+    I.col.ensure(col.size() + dev::kColPad);  // padded for the search's 128-bit loads
     I.elab.ensure(el.size());
     I.label_start.ensure(I.lstart.size());
     I.lab_off.ensure(lab_off.size());
     if (!lab_off.empty())
         TFSM_CK(cudaMemcpyAsync(I.lab_off.p, lab_off.data(), lab_off.size() * 4, cudaMemcpyHostToDevice, I.stream));
     TFSM_CK(cudaMemcpyAsync(I.row_off.p, off.data(), off.size() * 4, cudaMemcpyHostToDevice, I.stream));
+    TFSM_CK(cudaMemsetAsync(I.col.p + col.size(), 0xff, dev::kColPad * 4, I.stream));
     if (!col.empty()) {
         TFSM_CK(cudaMemcpyAsync(I.col.p, col.data(), col.size() * 4, cudaMemcpyHostToDevice, I.stream));
         TFSM_CK(cudaMemcpyAsync(I.elab.p, el.data(), el.size(), cudaMemcpyHostToDevice, I.stream));
@@ -349,23 +347,21 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     I.g.label_start = I.label_start.p;
     I.g.lab_off = I.lab_off.p;
     I.g.lab_stride = (uint32_t)stride;
-    I.counters.ensure((size_t)dev::kMaxPasses * dev::kPassCounters);
-    // Work-sharing ring (96 B per slot) and group table: 2^16 slots and 2^18 groups by default
-    // (6.3 MB + 1 MB).  A full ring or table only refuses a donation; TFSM_QUEUE_CAPACITY sets the
-    // ring's slot count (a power of two; tests use tiny ones to drive the refusal paths).
-    I.qcap = 1u << 16;
-    I.gcap = 1u << 18;
-    if (const char *env = std::getenv("TFSM_QUEUE_CAPACITY")) {
+    I.counters.ensure((size_t)dev::kMaxPasses * dev::kNumCounters);
+    // Two buffers of split tasks (88 B each) and as many groups (20 B each): one task per directed
+    // adjacency entry, 2 M to 16 M (at most 3.1 GB; searches that find no room are set aside for the
+    // next pass).  TFSM_SPLIT_CAPACITY sets both counts (tests use a tiny one to drive the
+    // buffer-full paths).
+    size_t task_cap = 2u << 20;
+    while (task_cap < (16u << 20) && task_cap < (size_t)lg.offs[lg.n]) task_cap *= 2;
+    size_t group_cap = task_cap;
+    if (const char *env = std::getenv("TFSM_SPLIT_CAPACITY")) {
         const long c = std::atol(env);
-        if (c < 1 || c > (1l << 24) || (c & (c - 1))) throw EngineError(1, "TFSM_QUEUE_CAPACITY must be a power of two in 1..2^24");
-        I.qcap = (uint32_t)c;
-        I.gcap = std::max<uint32_t>(1, I.qcap);
+        if (c < 1 || c > (1l << 26)) throw EngineError(1, "TFSM_SPLIT_CAPACITY must be in 1..2^26");
+        task_cap = group_cap = (size_t)c;
     }
-    if (const char *env = std::getenv("TFSM_SHARE_STEPS")) share_steps_ = (uint32_t)std::max(0, std::atoi(env));
-    I.cells.ensure(I.qcap);
-    I.qctl.ensure(2 * dev::kCntStride);
-    I.groups.ensure(I.gcap);
-    TFSM_CK(dev::launch_queue_init(I.cells.p, I.qcap, I.qctl.p, I.groups.p, I.gcap, I.stream));
+    I.splits.ensure(2 * task_cap);
+    I.groups.ensure(group_cap);
     // search-item staging for about 64 full-label domains (at most 1 M items, 16 MB)
     I.hitems.ensure(std::min<size_t>(1u << 20, ((size_t)lg.n / 32 + 1) * 64));
     checkpoint("buffers");
@@ -872,95 +868,80 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     prm.tau = tau;
     prm.exact = opt.exact ? 1 : 0;
     prm.n_items = (uint32_t)n_items;
-    prm.split = opt.split ? 1 : 0;
+    prm.split = opt.split && opt.step_budget ? 1 : 0;
     prm.split_slice = std::max<uint32_t>(1, opt.split_slice);
     prm.hub_span = opt.hub_span;
     prm.hub_parts = std::min<uint32_t>(std::max<uint32_t>(1, opt.hub_parts), 32);
+    prm.isect_ratio = std::max<uint32_t>(1, opt.isect_ratio);
+    prm.split_cap = (uint32_t)(I.splits.n / 2);
+    prm.split_slack = prm.split_cap / 8;
+    prm.search_fill = prm.split_cap / 2;
+    prm.group_cap = (uint32_t)I.groups.n;
     prm.parts_log2 = parts_log2;
     prm.team_lanes = team_lanes;
     prm.n_pats = (uint32_t)P;
     prm.words = total;
-    prm.qcap = I.qcap;
-    prm.gcap = I.gcap;
-    const uint32_t resident_teams = dev::resident_search_warps() * (32 / team_lanes);
-    // forced sharing of the last pass stops while the ring holds about one task per resident team
-    prm.soft_cap = std::max<uint32_t>(1, std::min<uint32_t>(I.qcap / 2, resident_teams));
-    // waiting teams poll the ring: four per SM are enough to take what is shared
-    prm.max_idle = std::max<uint32_t>(1, resident_teams / 8);
-    prm.share_steps = share_steps_;
-    prm.cells = I.cells.p;
-    prm.qctl = I.qctl.p;
-    prm.groups = I.groups.p;
-    // Passes: a search may take step_budget chunk steps in the first pass, 8x that in the next
-    // ones, without limit in the last; one it does not finish is set aside (neither found nor
-    // failed) and retried by the next pass, after the quick searches of every candidate have
-    // decided what they can.  A pass whose predecessor set nothing aside returns at once.
-    uint32_t budgets[dev::kMaxPasses];
-    int n_passes = 0;
-    if (opt.step_budget == 0) {
-        budgets[n_passes++] = 0;
-    } else {
-        uint64_t b = opt.step_budget;
-        for (; n_passes < dev::kMaxPasses - 1; ++n_passes, b *= 8) budgets[n_passes] = (uint32_t)std::min<uint64_t>(b, 1u << 30);
-        budgets[n_passes++] = 0;
-    }
     phase(3);
-    static_assert(sizeof(uint32_t) * dev::kMaxPasses * dev::kPassCounters <= 8192, "counter copy");
-    uint32_t hcnt[dev::kMaxPasses * dev::kPassCounters];
-    uint32_t hq[2 * dev::kCntStride];
+    // Passes.  In each, a search may take `budget` chunk steps before its unexplored remainder
+    // becomes split tasks; split rounds then work those off, each task again with a budget (twice
+    // the pass's, doubling per round up to 8x after the first `kFixedRounds`, none in the 64th
+    // round).  The first rounds are launched with the search as one sequence (a CUDA graph); the
+    // host launches further rounds while tasks remain.  Searches and tasks whose remainder found
+    // no room are set aside (neither found nor failed) and retried by the next pass with 8x the
+    // budgets; in the last pass they finish in place.
+    constexpr int kFixedRounds = 2;
+    const int n_passes = prm.split ? dev::kMaxPasses : 1;
+    uint32_t hcnt[dev::kNumCounters];
+    std::memset(hcnt, 0, sizeof(hcnt));
     TFSM_CK(cudaEventRecord(I.ev0, I.stream));
-    if (n_items != 0) {
+    uint64_t launches = 0;
+    for (int pass = 0; pass < n_passes && n_items != 0; ++pass) {
+        dev::SearchParams pk = prm;
+        pk.step_budget = (uint32_t)std::min<uint64_t>((uint64_t)opt.step_budget << (3 * pass), 1u << 28);
+        pk.last = pass + 1 == n_passes ? 1u : 0u;
+        const uint32_t round_budget = (uint32_t)std::min<uint64_t>(2ull * pk.step_budget, 1u << 28);
+        uint32_t *cnt = I.counters.p + (size_t)pass * dev::kNumCounters;
+        const int fixed = prm.split ? kFixedRounds : 0;
         run_captured(I.stream, I.exec_search, [&]() {
-            TFSM_CK(cudaMemsetAsync(I.counters.p, 0, (size_t)n_passes * dev::kPassCounters * sizeof(uint32_t),
-                                    I.stream));
-            for (int k = 0; k < n_passes; ++k) {
-                dev::SearchParams pk = prm;
-                pk.budget = budgets[k];
-                pk.prev = k ? I.counters.p + (size_t)(k - 1) * dev::kPassCounters : nullptr;
-                TFSM_CK(dev::launch_search(I.g, L.descs.p, I.status.p, I.items.p, pk,
-                                           I.counters.p + (size_t)k * dev::kPassCounters, L.dom.p, L.found.p,
-                                           L.failed.p, I.stream));
-            }
+            TFSM_CK(cudaMemsetAsync(cnt, 0, dev::kNumCounters * sizeof(uint32_t), I.stream));
+            TFSM_CK(dev::launch_search(I.g, L.descs.p, I.status.p, I.items.p, pk, cnt, L.dom.p, L.found.p,
+                                       L.failed.p, I.splits.p, I.groups.p, I.stream));
+            for (int r = 0; r < fixed; ++r)
+                TFSM_CK(dev::launch_split_round(I.g, L.descs.p, I.status.p, pk, cnt, r, round_budget, L.dom.p,
+                                                L.found.p, L.failed.p, I.splits.p, I.groups.p, I.stream));
         });
+        launches += 1 + (uint64_t)fixed;
+        for (int r = fixed; prm.split && r < dev::kMaxRounds; ++r) {
+            uint32_t pending = 0;
+            TFSM_CK(cudaMemcpyAsync(&pending, cnt + 2 + r, sizeof(pending), cudaMemcpyDeviceToHost, I.stream));
+            TFSM_CK(cudaStreamSynchronize(I.stream));
+            times_.d2h_bytes += sizeof(pending);
+            if (pending == 0) break;
+            const uint32_t budget = round_budget << std::min(r - fixed + 1, 3);
+            TFSM_CK(dev::launch_split_round(I.g, L.descs.p, I.status.p, pk, cnt, r, budget, L.dom.p, L.found.p,
+                                            L.failed.p, I.splits.p, I.groups.p, I.stream));
+            ++launches;
+        }
+        TFSM_CK(cudaMemcpyAsync(hcnt, cnt, sizeof(hcnt), cudaMemcpyDeviceToHost, I.stream));
+        TFSM_CK(cudaStreamSynchronize(I.stream));
+        times_.d2h_bytes += sizeof(hcnt);
+        times_.search_passes++;
+        times_.split_groups += std::min<uint32_t>(hcnt[1], prm.group_cap);
+        for (int r = 0; r < dev::kMaxRounds; ++r) times_.split_tasks += std::min(hcnt[2 + r], prm.split_cap);
+        times_.abandoned += hcnt[dev::kCntAbandoned];
+        if (hcnt[dev::kCntAbandoned] == 0) break;
     }
     TFSM_CK(cudaEventRecord(I.ev1, I.stream));
-    const size_t cnt_bytes = (size_t)n_passes * dev::kPassCounters * sizeof(uint32_t);
-    TFSM_CK(cudaMemcpyAsync(hcnt, I.counters.p, cnt_bytes, cudaMemcpyDeviceToHost, I.stream));
-    TFSM_CK(cudaMemcpyAsync(hq, I.qctl.p, sizeof(hq), cudaMemcpyDeviceToHost, I.stream));
     TFSM_CK(cudaMemcpyAsync(I.hstatus.data(), I.status.p, P * sizeof(PatStatus), cudaMemcpyDeviceToHost, I.stream));
     TFSM_CK(cudaStreamSynchronize(I.stream));
-    times_.d2h_bytes += cnt_bytes + sizeof(hq) + P * sizeof(PatStatus);
-    if (n_items == 0) std::memset(hcnt, 0, cnt_bytes);
+    times_.d2h_bytes += P * sizeof(PatStatus);
     {
         float ms = 0;
         TFSM_CK(cudaEventElapsedTime(&ms, I.ev0, I.ev1));
         times_.search_ms += ms;
     }
-    auto C = [&](int k, int c) { return hcnt[(size_t)k * dev::kPassCounters + (size_t)c * dev::kCntStride]; };
-    uint32_t outstanding = 0, bad = 0;
-    for (int k = 0; k < n_passes && n_items != 0; ++k) {
-        if (k > 0 && C(k - 1, dev::kCntAbandoned) == 0) break;  // this pass and the later ones returned at once
-        times_.search_launches++;
-        times_.search_passes++;
-        times_.split_groups += C(k, dev::kCntGroups);
-        times_.split_tasks += C(k, dev::kCntTasks);
-        times_.split_refused += C(k, dev::kCntRefused);
-        times_.wait_expired += C(k, dev::kCntWaitExpired);
-        times_.abandoned += C(k, dev::kCntAbandoned);
-        times_.queue_max = std::max<uint64_t>(times_.queue_max, C(k, dev::kCntQueueMax));
-        outstanding += C(k, dev::kCntWork);
-        bad += C(k, dev::kCntBadTask);
-    }
+    times_.search_launches += launches;
     times_.search_calls++;
-    if (hq[dev::kQctlHead] != hq[dev::kQctlTail] || outstanding != 0 || bad != 0) {
-        // every shared task is taken before a launch ends: anything else is an engine fault
-        TFSM_CK(dev::launch_queue_init(I.cells.p, I.qcap, I.qctl.p, I.groups.p, I.gcap, I.stream));
-        TFSM_CK(cudaStreamSynchronize(I.stream));
-        throw EngineError(11, "search launch ended with work outstanding (ring " +
-                                  std::to_string(hq[dev::kQctlHead]) + ".." + std::to_string(hq[dev::kQctlTail]) +
-                                  ", units " + std::to_string(outstanding) + ", malformed tasks " +
-                                  std::to_string(bad) + ")");
-    }
     {
         unsigned long long rec[4];
         if (dev::read_bounds_check(rec))

@@ -36,14 +36,13 @@ struct EvalResult {
 
 struct EngineOptions {
     bool exact = false;                // evaluate every candidate (exact MNI), no early exit
-    bool split = true;                 // long searches of the last pass share out work through the
-                                       //   device ring
-    uint32_t step_budget = 16;         // chunk evaluations a search may take in the first search pass
-                                       //   before it is set aside; 8x more in each later pass, no limit
-                                       //   in the last (0: one pass without limit)
-    uint32_t split_slice = 32;         // least anchor positions per shared part of the current depth
+    bool split = true;                 // long searches are split into tasks for the split rounds
+    uint32_t step_budget = 16;         // chunk evaluations before a search is split (0: never); split
+                                       //   tasks get twice that, doubling per later round up to 8x;
+                                       //   later passes (for what found no room) multiply it by 8
+    uint32_t split_slice = 64;         // anchor positions per split task
     uint32_t hub_span = 4096;          // a search whose first depth has more anchor positions ...
-    uint32_t hub_parts = 4;            //   ... shares it out at once in this many parts (1: off)
+    uint32_t hub_parts = 4;            //   ... is split at once into this many tasks (1: off)
     uint32_t isect_ratio = 16;         // merge a further backward neighbour's candidate run when it
                                        //   is at most this many times the step's survivors, else
                                        //   galloping search
@@ -77,13 +76,10 @@ struct KernelTimes {                   // accumulated device time (CUDA events),
     uint64_t search_bytes = 0;         // algorithmic bytes read by the search kernels
     uint64_t isects = 0;               // set intersections (chunk x backward neighbour) of the searches
     uint64_t h2d_bytes = 0, d2h_bytes = 0;      // host<->device copies of the evaluations
-    uint64_t split_groups = 0;                  // searches that shared work
-    uint64_t split_tasks = 0;                   // tasks shared through the ring
-    uint64_t split_refused = 0;                 // donations refused (ring or group table full)
-    uint64_t wait_expired = 0;                  // teams that stopped waiting for work at the limit
-    uint64_t queue_max = 0;                     // deepest ring seen
-    uint64_t abandoned = 0;                     // searches set aside at a pass's step budget
-    uint64_t search_passes = 0;                 // search passes that ran (launches that had work)
+    uint64_t split_groups = 0;                  // searches split into tasks
+    uint64_t split_tasks = 0;                   // split tasks written (all rounds)
+    uint64_t abandoned = 0;                     // searches / tasks set aside for a later pass (no room)
+    uint64_t search_passes = 0;                 // search passes that ran
     double order_ms = 0;                        // host + cost-model time spent choosing orders
 };
 
@@ -150,7 +146,6 @@ private:
     KernelTimes times_;
     double upload_ms_ = 0;
     std::string load_breakdown_;
-    uint32_t share_steps_ = 0;  // TFSM_SHARE_STEPS (tests): last-pass searches share work after this many steps
 };
 
 }  // namespace tfsm

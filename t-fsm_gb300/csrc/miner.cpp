@@ -295,15 +295,11 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                                  now.phase_ms[2] - before.phase_ms[2], now.phase_ms[3] - before.phase_ms[3],
                                  now.phase_ms[4] - before.phase_ms[4], now.phase_ms[5] - before.phase_ms[5]);
                     std::fprintf(stderr,
-                                 "          passes %llu (%llu searches set aside); shared: %llu searches, %llu tasks, "
-                                 "%llu refused, ring depth <= %llu, %llu waits expired\n",
+                                 "          passes %llu (%llu set aside), split: %llu searches, %llu tasks\n",
                                  (unsigned long long)(now.search_passes - before.search_passes),
                                  (unsigned long long)(now.abandoned - before.abandoned),
                                  (unsigned long long)(now.split_groups - before.split_groups),
-                                 (unsigned long long)(now.split_tasks - before.split_tasks),
-                                 (unsigned long long)(now.split_refused - before.split_refused),
-                                 (unsigned long long)now.queue_max,
-                                 (unsigned long long)(now.wait_expired - before.wait_expired));
+                                 (unsigned long long)(now.split_tasks - before.split_tasks));
                 }
                 for (size_t k = b0; k < b1; ++k) {
                     const size_t i = todo[k];

@@ -12,8 +12,8 @@
 // Limits and sharing:
 //   * the array holds kScratchBytes (16 MiB) on every GPU that loads the library, until exit;
 //   * a pattern whose domain bitmaps need more than that is rejected with TFSM_ERR_LIMIT;
-//   * work sharing is off on this path (its ring would need more scratch); automorphic vertices
-//     are searched separately — both change speed only, never results;
+//   * hub splitting is off on this path (its task buffers would need more scratch); automorphic
+//     vertices are searched separately — both change speed only, never results;
 //   * every call on a device reuses the same array and leaves its contents behind: the status block
 //     and counters are cleared at the start of each call and the kernels rewrite every bitmap word
 //     they read, but two calls whose work overlaps on the GPU race on the array, so calls must not
@@ -224,7 +224,7 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     const size_t o_desc = 0;
     const size_t o_status = align_up(o_desc + sizeof(PatDesc));
     const size_t o_counters = align_up(o_status + sizeof(PatStatus));
-    const size_t o_item_pu = align_up(o_counters + dev::kPassCounters * sizeof(uint32_t));
+    const size_t o_item_pu = align_up(o_counters + dev::kNumCounters * sizeof(uint32_t));
     const size_t o_prefix = align_up(o_item_pu + dev::kMaxN * sizeof(uint32_t));
     const size_t o_items = align_up(o_prefix + (dev::kMaxN + 1) * sizeof(uint64_t));
     const size_t o_pools = align_up(o_items + max_items * sizeof(dev::SearchItem));
@@ -267,7 +267,7 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     }
     NA_CK(cudaMemcpyAsync(d_desc, &D, sizeof(D), cudaMemcpyHostToDevice, s));
     NA_CK(cudaMemsetAsync(d_status, 0, sizeof(PatStatus), s));  // the previous call's status stays behind
-    NA_CK(cudaMemsetAsync(d_counters, 0, dev::kPassCounters * sizeof(uint32_t), s));
+    NA_CK(cudaMemsetAsync(d_counters, 0, dev::kNumCounters * sizeof(uint32_t), s));
     NA_CK(cudaMemcpyAsync(d_item_pu, item_pu, n * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     NA_CK(cudaMemcpyAsync(d_prefix, prefix, (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
     // every bitmap word of every vertex is written here, so no clearing of the pools is needed
@@ -340,11 +340,13 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     prm.tau = tau;
     prm.exact = exact ? 1 : 0;
     prm.n_items = (uint32_t)n_items;
-    prm.split = 0;  // no work sharing on this path (no ring or group table)
+    prm.split = 0;  // no hub splitting on this path (its task buffers would need more scratch)
+    prm.isect_ratio = 16;
     prm.team_lanes = 32;
     prm.n_pats = 1;
     prm.words = words;
-    NA_CK(dev::launch_search(g, d_desc, d_status, d_items, prm, d_counters, d_dom, d_found, d_failed, s));
+    NA_CK(dev::launch_search(g, d_desc, d_status, d_items, prm, d_counters, d_dom, d_found, d_failed, nullptr, nullptr,
+                             s));
     NA_CK(cudaMemcpyAsync(&st, d_status, sizeof(st), cudaMemcpyDeviceToHost, s));
     NA_CK(cudaStreamSynchronize(s));
     mn = UINT32_MAX;

@@ -1,6 +1,8 @@
 // C-ABI check of tfsm_evaluate_level under the SIMT emulation (test infrastructure only).
 //
 // usage: abi_emu GRAPH.lg TAU GOLDEN.mni.txt
+// The environment variables ISECT_RATIO and SEARCH_LANES, when set, become the handle's
+// isect_ratio and search_lanes options.
 // Evaluates the golden patterns level by level (by DFS-code length) with TFSM_FLAG_EXACT. Each
 // pattern whose DFS-code prefix (its code minus the last edge: the same vertex numbering, one edge
 // less) was evaluated by the previous level's call starts from that prefix's kept domains. Every
@@ -72,6 +74,15 @@ int main(int argc, char **argv) {
     if (tfsm_graph_load(argv[1], tau, &g) != TFSM_OK || tfsm_graph_load(argv[1], tau, &other) != TFSM_OK) {
         std::printf("FAIL load: %s\n", tfsm_last_error());
         return 1;
+    }
+    {
+        tfsm_options o;
+        o.struct_size = sizeof(o);
+        bool ok = tfsm_get_options(g, &o) == TFSM_OK;
+        if (const char *r = std::getenv("ISECT_RATIO")) o.isect_ratio = (uint32_t)std::atoi(r);
+        if (const char *l = std::getenv("SEARCH_LANES")) o.search_lanes = (uint32_t)std::atoi(l);
+        ok = ok && tfsm_set_options(g, &o) == TFSM_OK;
+        expect(ok, "options: " + std::string(tfsm_last_error()));
     }
     tfsm_domains *prev = nullptr, *first = nullptr;
     std::map<std::string, int> prev_index;

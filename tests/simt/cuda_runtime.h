@@ -266,6 +266,10 @@ inline unsigned __reduce_add_sync(unsigned mask, unsigned v, int at = __builtin_
 }
 
 inline int __ffs(unsigned x) { return __builtin_ffs((int)x); }
+inline int __clz(unsigned x) { return x ? __builtin_clz(x) : 32; }
+struct alignas(16) uint4 {
+    unsigned x, y, z, w;
+};
 inline int __popc(unsigned x) { return __builtin_popcount(x); }
 inline unsigned min(unsigned a, unsigned b) { return a < b ? a : b; }
 

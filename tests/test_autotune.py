@@ -21,14 +21,14 @@ spec.loader.exec_module(autotune)
 
 
 def test_per_level_choice_on_synthetic_costs():
-    # level 1 prefers chunk_words 2, level 2 prefers step_budget 16; everything else is flat
+    # level 1 prefers chunk_words 2, level 2 prefers step_budget 64; everything else is flat
     def run(per_level):
         t = [0.0] * 4
         for lv, o in per_level.items():
             t[lv] = 10.0
             if lv == 1 and o.get("chunk_words") == 2:
                 t[lv] -= 3
-            if lv == 2 and o.get("step_budget") == 16:
+            if lv == 2 and o.get("step_budget") == 64:
                 t[lv] -= 2
             if lv == 3 and o.get("split_slice") == 128:
                 t[lv] += 5
@@ -36,8 +36,8 @@ def test_per_level_choice_on_synthetic_costs():
 
     best, log = autotune.tune_levels(run, 3, repeats=1)
     assert best[1]["chunk_words"] == 2 and best[2]["chunk_words"] == 1
-    assert best[2]["step_budget"] == 16 and best[1]["step_budget"] == 64
-    assert best[3]["split_slice"] == 32  # default kept on ties and where others are worse
+    assert best[2]["step_budget"] == 64 and best[1]["step_budget"] == 16
+    assert best[3]["split_slice"] == 64  # default kept on ties and where others are worse
     assert log["runs"] == sum(len(v) for _, v in autotune.SPACE)
 
 

@@ -58,10 +58,10 @@ def test_mining_plain_matches_reference(tfsm, graphs, case, tmp_path):
     assert st["engine_calls"] == st["evaluations"] - st["pruned"]  # one engine call per searched candidate
 
 
-SPLIT_OPTS = [dict(step_budget=1, split_slice=1),          # passes with budgets 1, 8, 64, none
+SPLIT_OPTS = [dict(step_budget=1, split_slice=1),          # every search splits at its first step
               dict(step_budget=3, split_slice=32),
-              dict(step_budget=0, hub_span=0, hub_parts=8, split_slice=1),  # first depths shared at once
-              dict(step_budget=0, hub_parts=1)]                     # one pass, sharing with waiting teams
+              dict(step_budget=16, hub_span=0, hub_parts=8, split_slice=1),  # first depths split at once
+              dict(step_budget=0)]                                  # no splitting
 
 
 @pytest.mark.parametrize("case", ["cfg1", "el3", "star_hub", "clique"])
@@ -248,15 +248,15 @@ def test_cli_writes_reference_format(built, case_graph, tmp_path):
 
 
 @pytest.mark.parametrize("case", ["star_hub", "clique", "el3"])
-@pytest.mark.parametrize("ring", ["1", "4"])
-def test_work_ring_full_keeps_results(built, case_graph, case, ring, tmp_path):
-    """A work ring of 1 or 4 slots: most donations are refused and those searches go on in place."""
+def test_split_buffers_full_keep_results(built, case_graph, case, tmp_path):
+    """Split buffers of 5 tasks / 5 groups: claims straddle the end, searches and tasks without
+    room are set aside for later passes, and the last pass finishes them in place."""
     import os
     c = CASES[case]
     out = tmp_path / "grami_results.txt"
-    env = dict(os.environ, TFSM_QUEUE_CAPACITY=ring)
+    env = dict(os.environ, TFSM_SPLIT_CAPACITY="5")
     r = subprocess.run([str(built / "bin" / "run"), "-file", str(case_graph(case)), "-freq", str(c["tau"]),
-                        "-maxNodes", str(c["max_nodes"]), "-step-budget", "1", "-split-slice", "1", "-out", str(out)],
+                        "-maxNodes", str(c["max_nodes"]), "-step-budget", "1", "-split-slice", "32", "-out", str(out)],
                        capture_output=True, text=True, timeout=300, env=env)
     assert r.returncode == 0, r.stderr
     assert set(read_results(out)) == golden_pattern_set(case)

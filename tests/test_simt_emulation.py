@@ -2,7 +2,7 @@
 AddressSanitizer + UndefinedBehaviorSanitizer: every global/shared access in bounds, no UB, warp
 collectives executed uniformly (a divergent collective deadlocks the emulated warp and is reported
 with each lane's source line), and results equal to the reference on small graphs — including the
-work-sharing path forced on every search.  Test infrastructure only; the product has no CPU path.
+hub-splitting path forced on every search.  Test infrastructure only; the product has no CPU path.
 """
 from __future__ import annotations
 
@@ -28,26 +28,27 @@ def emu():
 
 
 OPTS = {"default": [],
-        # one unlimited pass whose searches share out work at every chunk step (TFSM_SHARE_STEPS),
-        # one position per part at least
-        "split": ["-step-budget", "0", "-split-slice", "1", "-chunk-words", "1"],
-        # passes with budgets 1, 8, 64 and none: most searches are set aside and retried
-        "deepen": ["-step-budget", "1"],
-        # every search's first depth is shared out at once in four parts
-        "hub": ["-hub-span", "0", "-hub-parts", "4", "-split-slice", "1", "-step-budget", "0"],
+        # every search splits at its first chunk step; split tasks of one position each
+        "split": ["-step-budget", "1", "-split-slice", "1", "-chunk-words", "1"],
+        # every search's first depth is split at once into four tasks
+        "hub": ["-hub-span", "0", "-hub-parts", "4", "-split-slice", "1"],
         "no_split": ["-no-split"],
+        "merge_all": ["-isect-ratio", "1000000", "-step-budget", "2"],
+        "probe_all": ["-isect-ratio", "1"],
         "plain": ["-plain", "-refine-rounds", "1"], "exact": ["-exact"], "batch3": ["-max-batch", "3"],
         "random_orders": ["-random-orders", "7", "-step-budget", "2"],
         "lanes8": ["-search-lanes", "8"],
-        "lanes8_split": ["-search-lanes", "8", "-step-budget", "0", "-split-slice", "1"],
-        "lanes8_exact": ["-search-lanes", "8", "-exact", "-step-budget", "0", "-split-slice", "1"],
+        "lanes8_split": ["-search-lanes", "8", "-step-budget", "1", "-split-slice", "1"],
+        "lanes8_exact": ["-search-lanes", "8", "-exact", "-step-budget", "1", "-split-slice", "1"],
         "rank_window2": ["-rank-window", "2", "-step-budget", "2"],
         # every emulated call is slower than 1 us: calls shrink to 4 patterns after the first
         "adaptive_calls": ["-call-ms", "0.001"]}
 # (the quirk case's many-call variants are the slowest to emulate; its other variants cover it)
 RUNS = [(c, o) for c in SMALL for o in OPTS if not (o in ("plain", "batch3") and c == "quirk_elabels")]
-RUNS += [(c, "tiny_ring") for c in ("clique", "star_hub")]
-OPTS["tiny_ring"] = OPTS["split"]  # with TFSM_QUEUE_CAPACITY=2: most donations are refused
+RUNS += [(c, "tiny_buffers") for c in ("clique", "star_hub", "quirk_elabels")]
+# with TFSM_SPLIT_CAPACITY=5: claims straddle the end, searches are set aside and retried by later
+# passes, the last pass finishes them in place
+OPTS["tiny_buffers"] = OPTS["split"]
 
 
 @pytest.mark.parametrize("case,opt", RUNS)
@@ -58,10 +59,8 @@ def test_emulated_kernels_match_reference(emu, case, opt, tmp_path):
     # emulated kernels run on the host cores: keep the host growth (which overlaps them) small
     env = dict(os.environ, ASAN_OPTIONS="detect_leaks=1:abort_on_error=1", UBSAN_OPTIONS="halt_on_error=1",
                TFSM_HOST_THREADS="3")
-    if opt in ("split", "lanes8_split", "lanes8_exact", "tiny_ring"):
-        env["TFSM_SHARE_STEPS"] = "1"
-    if opt == "tiny_ring":
-        env["TFSM_QUEUE_CAPACITY"] = "2"
+    if opt == "tiny_buffers":
+        env["TFSM_SPLIT_CAPACITY"] = "5"
     r = subprocess.run([str(emu), "-file", str(GOLDEN / c["file"]), "-freq", str(c["tau"]), "-maxNodes",
                         str(c["max_nodes"]), "-out", str(out), *opts, "-call-ms", "0"], capture_output=True,
                        text=True, timeout=600,
