@@ -20,6 +20,7 @@
 #include <memory_resource>
 #include <set>
 #include <string>
+#include <tuple>
 #include <vector>
 
 namespace tfsm {
@@ -179,6 +180,21 @@ struct FwdKey {
 using Trans = std::pmr::vector<const PEdge *>;  // edges of one projection, in MIN code order
 using ProjDB = std::pmr::vector<Trans>;
 
+// root[k] of a map ordered by FwdKey, done as std::map::operator[] does it (lower_bound, then
+// emplace_hint when the key is not found) so that the tree sees the same operations in the same
+// order as the reference's map.  Because FwdKey is not a strict weak ordering, that sequence can
+// end at end() (the hint step finds an "equal" key at the end): std::map::operator[] then hands out
+// the map's header as if it were an element — undefined behaviour, in the reference's program too,
+// whose push into it lands in the map object's own memory and is never seen again by begin().
+// Here that case returns nullptr and the caller drops the projection: the defined form of what the
+// reference observes, without writing outside the map.
+inline ProjDB *fwd_slot(std::pmr::map<FwdKey, ProjDB> &root, const FwdKey &k) {
+    auto it = root.lower_bound(k);
+    if (it == root.end() || root.key_comp()(k, it->first))
+        it = root.emplace_hint(it, std::piecewise_construct, std::forward_as_tuple(k), std::forward_as_tuple());
+    return it == root.end() ? nullptr : &it->second;
+}
+
 struct History {
     std::vector<const PEdge *> edges;
     std::vector<char> has_edge, has_vertex;
@@ -302,7 +318,7 @@ struct Checker {
                         new_fromlabel = lab(it->from);
                         Trans t(cur, &arena);
                         t.push_back(it);
-                        root[k].push_back(std::move(t));
+                        if (ProjDB *db = fwd_slot(root, k)) db->push_back(std::move(t));
                     }
                 }
             }
@@ -317,7 +333,7 @@ struct Checker {
                             new_fromlabel = lab(it->from);
                             Trans t(cur, &arena);
                             t.push_back(it);
-                            root[k].push_back(std::move(t));
+                            if (ProjDB *db = fwd_slot(root, k)) db->push_back(std::move(t));
                         }
                     }
                 }

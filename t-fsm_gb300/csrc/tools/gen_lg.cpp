@@ -18,7 +18,10 @@
 // they were made from the same graph.
 //
 // usage: gen_lg --out G.lg --n N --mean D --gamma G --max-degree X --labels L --zipf S
-//               --elabels E --seed K
+//               --elabels E --seed K [--arrays PREFIX]
+// --arrays also writes the same graph as raw little-endian arrays, in the .lg file's order:
+// PREFIX.vlabel (int32 per vertex), PREFIX.src / PREFIX.dst (uint32 per edge), PREFIX.elabel
+// (int32 per edge) — the host buffers of tfsm_graph_from_edges without parsing text.
 
 #include <algorithm>
 #include <cmath>
@@ -96,6 +99,7 @@ double det_pow(double base, double expo) { return det_exp(expo * det_log(base));
 
 struct Args {
     std::string out;
+    std::string arrays;  // prefix of the raw array files, or empty
     long n = 5000;
     double mean = 8.0;
     double gamma = 2.5;
@@ -111,6 +115,7 @@ bool parse(int argc, char **argv, Args &a) {
         const char *k = argv[i];
         const char *v = argv[i + 1];
         if (!std::strcmp(k, "--out")) a.out = v;
+        else if (!std::strcmp(k, "--arrays")) a.arrays = v;
         else if (!std::strcmp(k, "--n")) a.n = std::atol(v);
         else if (!std::strcmp(k, "--mean")) a.mean = std::atof(v);
         else if (!std::strcmp(k, "--gamma")) a.gamma = std::atof(v);
@@ -251,6 +256,25 @@ int main(int argc, char **argv) {
     }
     for (long i = 0; i < n; ++i) mix((uint64_t)vlabel[i]);
     std::fclose(f);
+    if (!a.arrays.empty()) {
+        auto dump = [&](const char *ext, const void *data, size_t bytes) {
+            FILE *g = std::fopen((a.arrays + ext).c_str(), "wb");
+            const bool ok = g && std::fwrite(data, 1, bytes, g) == bytes;
+            if (g) std::fclose(g);
+            return ok;
+        };
+        std::vector<uint32_t> src(keys.size()), dst(keys.size());
+        for (size_t e = 0; e < keys.size(); ++e) {
+            src[e] = (uint32_t)(keys[e] >> 32);
+            dst[e] = (uint32_t)(keys[e] & 0xffffffffu);
+        }
+        if (!dump(".vlabel", vlabel.data(), vlabel.size() * sizeof(vlabel[0])) ||
+            !dump(".src", src.data(), src.size() * 4) || !dump(".dst", dst.data(), dst.size() * 4) ||
+            !dump(".elabel", elabel.data(), elabel.size() * sizeof(elabel[0]))) {
+            std::fprintf(stderr, "cannot write the arrays %s.*\n", a.arrays.c_str());
+            return 1;
+        }
+    }
     uint32_t maxdeg = 0;
     for (long i = 0; i < n; ++i) maxdeg = deg[i] > maxdeg ? deg[i] : maxdeg;
     std::printf("{\"n\": %ld, \"m\": %zu, \"max_degree\": %u, \"fnv64\": \"%016llx\"}\n", n, keys.size(), maxdeg,
