@@ -51,7 +51,7 @@ def test_mining_batched_matches_reference(tfsm, graphs, case, tmp_path):
     assert pats == golden_pattern_set(case)
 
 
-@pytest.mark.parametrize("case", SMALL + ["cfg2_t9000"])
+@pytest.mark.parametrize("case", SMALL + ["cfg2_t9000", "cfg4_m3"])
 def test_mining_plain_matches_reference(tfsm, graphs, case, tmp_path):
     pats, st = mine_set(tfsm, graphs(case), case, tmp_path, flags=tfsm.FLAG_PLAIN)
     assert pats == golden_pattern_set(case)
@@ -311,5 +311,20 @@ def test_team_sizes_keep_results(tfsm, graphs, case, lanes, tmp_path):
             keys = list(want)[:300]
             res = g.evaluate([tfsm.parse_key(k) for k in keys], flags=tfsm.FLAG_EXACT)
             assert [r.mni for r in res] == [want[k] for k in keys]
+    finally:
+        g.set_options(**saved)
+
+
+@pytest.mark.parametrize("opts", [dict(isect_ratio=1), dict(isect_ratio=1000000, search_lanes=32),
+                                  dict(hub_span=512, hub_parts=8), dict(step_budget=0)])
+def test_hub_graph_knobs_keep_reference_set(tfsm, graphs, opts, tmp_path):
+    """The 2M-vertex hub graph (three edge labels, hubs of ~35k neighbours): every intersection
+    form, team size, hub split and no splitting at all give the reference's pattern set."""
+    g = graphs("cfg4_m3")
+    saved = g.options()
+    try:
+        g.set_options(**opts)
+        pats, _ = mine_set(tfsm, g, "cfg4_m3", tmp_path)
+        assert pats == golden_pattern_set("cfg4_m3")
     finally:
         g.set_options(**saved)
