@@ -30,6 +30,9 @@ CXXFLAGS = ["-std=c++17", "-O3", "-fPIC", "-Wall", "-Wno-unused-function"]
 # TFSM_HOST_DEBUG=1: host code keeps frame pointers and debug information (crash reports with
 # symbolised stacks); device code is unchanged.
 HOST_DEBUG = ["-g", "-fno-omit-frame-pointer"] if os.environ.get("TFSM_HOST_DEBUG") == "1" else []
+# TFSM_SEARCH_MIN_BLOCKS=N: resident blocks per SM the search kernels are compiled for (register budget)
+DEVICE_DEFS = ([f"-DTFSM_SEARCH_MIN_BLOCKS={int(os.environ['TFSM_SEARCH_MIN_BLOCKS'])}"]
+               if os.environ.get("TFSM_SEARCH_MIN_BLOCKS") else [])
 
 
 def _cuda_home() -> Path:
@@ -76,7 +79,7 @@ def build(verbose: bool = False) -> Path:
         if _stale(obj, [src] + headers):
             jobs.append([nvcc, *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
                          *(["-Xcompiler", ",".join(HOST_DEBUG)] if HOST_DEBUG else []), "-I", str(CSRC),
-                         *(["-DTFSM_BOUNDS_CHECK"] if CHECKED else []), "-c", str(src), "-o", str(obj)])
+                         *(["-DTFSM_BOUNDS_CHECK"] if CHECKED else []), *DEVICE_DEFS, "-c", str(src), "-o", str(obj)])
     for src in cpp:
         obj = BUILD / (src.stem + ".o")
         objs.append(obj)

@@ -853,7 +853,7 @@ __device__ __forceinline__ bool pattern_stops(const Team<G> &T, const PatStatus 
 // (neither found nor failed), and a team starts no more searches once the first round's share of
 // the buffer is full: the next pass, with larger budgets, takes up what is left.
 template <int G>
-__global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const PatDesc *__restrict__ descs,
+__global__ void __launch_bounds__(kSearchWarps * 32, kSearchMinBlocks) k_search(Graph g, const PatDesc *__restrict__ descs,
                                                               PatStatus *__restrict__ st,
                                                               const SearchItem *__restrict__ items, SearchParams prm,
                                                               uint32_t *__restrict__ counters,
@@ -989,7 +989,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_search(Graph g, const Pat
 // pass, a remainder without room is set aside (the group is marked incomplete, so v stays
 // undecided for the next pass).
 template <int G>
-__global__ void __launch_bounds__(kSearchWarps * 32) k_split(Graph g, const PatDesc *__restrict__ descs,
+__global__ void __launch_bounds__(kSearchWarps * 32, kSearchMinBlocks) k_split(Graph g, const PatDesc *__restrict__ descs,
                                                              PatStatus *__restrict__ st, SearchParams prm,
                                                              uint32_t *__restrict__ counters, int round,
                                                              uint32_t budget, const uint32_t *__restrict__ dom,

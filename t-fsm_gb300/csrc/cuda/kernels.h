@@ -9,6 +9,12 @@ namespace tfsm {
 namespace dev {
 
 constexpr int kSearchWarps = 8;  // warps per block of the search kernels
+// Blocks of the search kernels that must fit on one SM at once (the register budget follows from
+// it: 65536 / (256 x blocks)); the build may set it with -DTFSM_SEARCH_MIN_BLOCKS.
+#ifndef TFSM_SEARCH_MIN_BLOCKS
+#define TFSM_SEARCH_MIN_BLOCKS 4
+#endif
+constexpr int kSearchMinBlocks = TFSM_SEARCH_MIN_BLOCKS;
 
 // LDF + NLF bitmaps of the items' (pattern, vertex) pairs, intersected with the final domains of
 // the sources that PatDesc::parent_off / push_off reference in the table `srcs` (n_srcs pools of
