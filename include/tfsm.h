@@ -73,6 +73,8 @@ typedef struct {
     uint32_t max_degree;
     uint64_t device_bytes; /* device copy of the graph */
     double load_ms;        /* parse + prune + device upload */
+    uint64_t load_h2d_bytes; /* host -> device bytes the load copied (file bytes or input arrays with
+                                GPU ingestion, the built graph with the host loader) */
 } tfsm_graph_info_t;
 
 typedef struct {
@@ -98,8 +100,10 @@ typedef struct {
 } tfsm_mine_stats;
 
 /* Load a .lg graph and prune it for threshold `tau` (label frequency, edge-label frequency and
- * the frequent 1-edge pattern table), then upload it to CUDA device 0, or to the device whose
- * index the environment variable TFSM_DEVICE holds.
+ * the frequent 1-edge pattern table) on CUDA device 0, or on the device whose index the
+ * environment variable TFSM_DEVICE holds.  The file's bytes are copied to the device, which
+ * parses them and builds the pruned, renumbered graph; TFSM_INGEST=host selects the host loader
+ * instead (same graph, same errors).
  * Replaces Graph::load_graph (parallel/graph.h:557-570, serial/graph.h:485-494). */
 int tfsm_graph_load(const char *path, int32_t tau, tfsm_graph **out);
 
@@ -111,6 +115,33 @@ int tfsm_graph_from_edges(uint32_t n_vertices, const int32_t *vlabels, uint64_t 
 void tfsm_graph_free(tfsm_graph *g);
 
 int tfsm_graph_info(const tfsm_graph *g, tfsm_graph_info_t *info);
+
+/* A frequent 1-edge pattern (min label, edge label, max label) with its two endpoint-set sizes:
+ * one entry of the reference's 1-edge table (parallel/graph.h:685-803, `hashedEdges`). */
+typedef struct {
+    int32_t la, el, lb;
+    uint32_t cand_a, cand_b;
+} tfsm_edge_pattern;
+
+/* Destinations of tfsm_graph_export; a NULL member is not copied.  n, m, L, E and P are
+ * tfsm_graph_info's n_vertices, n_edges, n_frequent_vertex_labels, n_frequent_edge_labels and
+ * n_frequent_edge_patterns.  Vertex ids are the engine's: each frequent label L owns the ids
+ * [label_start[L], label_start[L+1]); inside it vertices are ranked by descending degree. */
+typedef struct {
+    uint32_t *row_off;            /* [n + 1] adjacency offsets */
+    uint32_t *col;                /* [2m] neighbour ids, ascending per vertex (ties: edge label) */
+    uint8_t *elab;                /* [2m] edge labels as indices into elabels */
+    uint32_t *label_start;        /* [L + 1] */
+    uint32_t *lab_off;            /* [(L + 1) * n], label-major: the first position of vertex x's
+                                     neighbours with label >= l is at l * n + x */
+    int32_t *vlabels;             /* [L] frequent vertex labels, ascending */
+    int32_t *elabels;             /* [E] frequent edge labels, ascending */
+    tfsm_edge_pattern *edge_patterns; /* [P] ascending (la, el, lb) */
+    float *label_mean_degree;     /* [L] mean degree of each frequent label's vertices */
+} tfsm_graph_arrays;
+
+/* Copies the graph as the device holds it (for checks and external tools). */
+int tfsm_graph_export(const tfsm_graph *g, const tfsm_graph_arrays *arrays);
 
 /* MNI support evaluation of one pattern: is MNI(P) >= tau?  With TFSM_FLAG_EXACT, mni[] holds
  * the exact per-vertex MNI domain sizes.  Replaces GraMi::frequency (serial/grami.h:261-328) and

@@ -69,7 +69,8 @@ def build(verbose: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     BIN.mkdir(exist_ok=True)
     headers = list(CSRC.rglob("*.h")) + list(CSRC.rglob("*.hpp")) + list(CSRC.rglob("*.cuh")) + [ROOT / "include" / "tfsm.h"]
-    cu = [CSRC / "cuda" / "kernels.cu", CSRC / "engine.cu", CSRC / "noalloc.cu", CSRC / "costmodel" / "mlp.cu"]
+    cu = [CSRC / "cuda" / "kernels.cu", CSRC / "cuda" / "ingest.cu", CSRC / "engine.cu", CSRC / "noalloc.cu",
+          CSRC / "costmodel" / "mlp.cu"]
     cpp = [CSRC / "miner.cpp", CSRC / "capi.cpp"]
     jobs = []
     objs = []

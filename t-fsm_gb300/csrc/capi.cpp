@@ -14,6 +14,9 @@
 
 #include "../../include/tfsm.h"
 #include "engine.hpp"
+#if !defined(TFSM_SIMT_EMULATION)
+#include "cuda/ingest.hpp"
+#endif
 #include "host/lg_fast.hpp"
 #include "miner.hpp"
 #include "noalloc.hpp"
@@ -29,6 +32,7 @@ struct tfsm_graph {
     tfsm::EngineOptions opt;  // tuning knobs (tfsm_set_options), order policy and cost model
     int tau = 0;
     double load_ms = 0;
+    bool device_ingest = false;  // the device graph was built on the GPU (lg holds no adjacency)
     bool recording = false;
     std::vector<std::pair<bool, tfsm_options>> level_opt;  // tfsm_set_level_options, by level
     mutable std::vector<float> records;  // tfsm_record_orders: 33 floats per record
@@ -195,14 +199,35 @@ int finish_graph(std::unique_ptr<tfsm_graph> &g, int tau, std::chrono::steady_cl
                  tfsm_graph **out) {
     g->tau = tau;
     const auto t_prune = std::chrono::steady_clock::now();
-    g->eng.reset(new tfsm::GpuEngine(g->lg, 0));
+    if (!g->eng) g->eng.reset(new tfsm::GpuEngine(g->lg, 0));
     g->load_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (std::getenv("TFSM_VERBOSE"))
-        std::fprintf(stderr, "[load] parse + prune %.3f ms, engine %.3f ms (%s)\n",
+        std::fprintf(stderr, "[load] %s: parse + prune %.3f ms, engine %.3f ms (%s)\n",
+                     g->device_ingest ? "device" : "host",
                      std::chrono::duration<double, std::milli>(t_prune - t0).count(), g->eng->upload_ms(),
                      g->eng->load_breakdown().c_str());
     *out = g.release();
     return TFSM_OK;
+}
+
+// Graph ingestion runs on the GPU (cuda/ingest.hpp) unless TFSM_INGEST=host selects the host
+// loader (host/lg_fast.hpp, then renumbering and upload in the engine); both build the same
+// device graph.
+// Without a CUDA device the host loader runs, so that malformed input is still reported as such
+// before the engine reports the missing device.
+bool device_ingest() {
+#if defined(TFSM_SIMT_EMULATION)
+    return false;
+#else
+    const char *e = std::getenv("TFSM_INGEST");
+    if (e && std::strcmp(e, "host") == 0) return false;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return true;
+#endif
 }
 
 }  // namespace
@@ -215,6 +240,15 @@ int tfsm_graph_load(const char *path, int32_t tau, tfsm_graph **out) {
         *out = nullptr;
         auto t0 = std::chrono::steady_clock::now();
         std::unique_ptr<tfsm_graph> g(new tfsm_graph);
+#if !defined(TFSM_SIMT_EMULATION)
+        if (device_ingest()) {
+            g->device_ingest = true;
+            const std::string file(path);
+            g->eng.reset(new tfsm::GpuEngine(
+                [&](CUstream_st *s, tfsm::DeviceGraphBuild &b) { tfsm::ingest_lg_file(file, tau, s, b); }, g->lg, 0));
+            return finish_graph(g, tau, t0, out);
+        }
+#endif
         g->lg = tfsm::load_lg_fast(path, tau);
         return finish_graph(g, tau, t0, out);
     });
@@ -227,6 +261,18 @@ int tfsm_graph_from_edges(uint32_t n_vertices, const int32_t *vlabels, uint64_t 
             return fail(TFSM_ERR_ARG, "null argument");
         *out = nullptr;
         auto t0 = std::chrono::steady_clock::now();
+#if !defined(TFSM_SIMT_EMULATION)
+        if (device_ingest()) {
+            std::unique_ptr<tfsm_graph> g(new tfsm_graph);
+            g->device_ingest = true;
+            g->eng.reset(new tfsm::GpuEngine(
+                [&](CUstream_st *s, tfsm::DeviceGraphBuild &b) {
+                    tfsm::ingest_edge_arrays(n_vertices, vlabels, n_edges, src, dst, elabels, tau, s, b);
+                },
+                g->lg, 0));
+            return finish_graph(g, tau, t0, out);
+        }
+#endif
         std::atomic<bool> bad(false);
         tfsm::fast::parallel_ranges((size_t)n_edges, tfsm::fast::default_threads(), [&](int, size_t k0, size_t k1) {
             for (size_t k = k0; k < k1 && !bad.load(std::memory_order_relaxed); ++k)
@@ -251,11 +297,26 @@ int tfsm_graph_info(const tfsm_graph *g, tfsm_graph_info_t *info) {
         info->n_frequent_vertex_labels = (uint32_t)g->lg.freq_vlabels.size();
         info->n_frequent_edge_labels = (uint32_t)g->lg.freq_elabels.size();
         info->n_frequent_edge_patterns = (uint32_t)g->lg.edge_pairs.size();
-        uint32_t md = 0;
-        for (uint32_t v = 0; v < g->lg.n; ++v) md = std::max(md, g->lg.degree(v));
-        info->max_degree = md;
+        info->max_degree = g->lg.max_degree;
         info->device_bytes = g->eng->graph_bytes();
         info->load_ms = g->load_ms;
+        info->load_h2d_bytes = g->eng->load_h2d_bytes();
+        return TFSM_OK;
+    });
+}
+
+int tfsm_graph_export(const tfsm_graph *g, const tfsm_graph_arrays *a) {
+    return guarded([&]() -> int {
+        if (!g || !a) return fail(TFSM_ERR_ARG, "null argument");
+        std::lock_guard<std::mutex> lk(const_cast<tfsm_graph *>(g)->mu);
+        g->eng->export_graph(a->row_off, a->col, a->elab, a->label_start, a->lab_off, a->label_mean_degree);
+        if (a->vlabels) std::copy(g->lg.freq_vlabels.begin(), g->lg.freq_vlabels.end(), a->vlabels);
+        if (a->elabels) std::copy(g->lg.freq_elabels.begin(), g->lg.freq_elabels.end(), a->elabels);
+        if (a->edge_patterns)
+            for (size_t i = 0; i < g->lg.edge_pairs.size(); ++i) {
+                const tfsm::EdgePair &e = g->lg.edge_pairs[i];
+                a->edge_patterns[i] = tfsm_edge_pattern{e.la, e.el, e.lb, e.cand_a, e.cand_b};
+            }
         return TFSM_OK;
     });
 }

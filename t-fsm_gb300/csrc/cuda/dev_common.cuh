@@ -30,11 +30,13 @@ struct Graph {
     const uint32_t *col = nullptr;
     const uint8_t *elab = nullptr;
     const uint32_t *label_start = nullptr;  // [n_labels + 1]
-    // lab_off[v * lab_stride + L] = position in col of v's first neighbour with label >= L, for
-    // L = 0..n_labels: the neighbours of v with label L are [lab_off[.. + L], lab_off[.. + L + 1]).
+    // Label-major: lab_off[L * n + v] = position in col of v's first neighbour with label >= L, for
+    // L = 0..n_labels; the neighbours of v with label L are [lab_off[L * n + v],
+    // lab_off[(L + 1) * n + v]).  The candidates of one bitmap word are consecutive ids, so a
+    // warp's lookups of one label coalesce, and the rows of the few labels a pattern uses stay in L2.
     const uint32_t *lab_off = nullptr;
-    uint32_t lab_stride = 0;                // n_labels + 1
 };
+
 
 // One pattern of a batch.  Plain old data, copied to the device once per batch.
 constexpr int kMaxPush = 4;  // sub-patterns besides the parent whose domains bound a child's

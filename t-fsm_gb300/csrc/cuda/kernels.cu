@@ -102,6 +102,13 @@ __device__ __forceinline__ uint32_t find_item(const uint64_t *__restrict__ prefi
 
 }  // namespace
 
+// The adjacency positions [lo, hi) of v's neighbours with dense label L (label-major table).
+__device__ __forceinline__ void label_range(const Graph &g, uint32_t v, uint32_t L, uint32_t &lo, uint32_t &hi) {
+    const uint32_t *p = g.lab_off + (size_t)L * g.n + v;
+    lo = __ldg(p);
+    hi = __ldg(p + g.n);
+}
+
 // ------------------------------------------------------------------------------------------------
 // K1: LDF + NLF filter.  One warp per bitmap word, one lane per vertex of the word.
 // ------------------------------------------------------------------------------------------------
@@ -155,10 +162,10 @@ __global__ void __launch_bounds__(256) k_domain_init(Graph g, const PatDesc *__r
                 pass = (int32_t)(e - b) >= D.deg[u];
             }
             const int nn = D.nlf_n[u];
-            const uint32_t *lo_x = g.lab_off + (size_t)x * g.lab_stride;
             for (int k = 0; k < nn && pass; ++k) {
-                const int L = D.nlf_lab[u][k];
-                pass = (__ldg(lo_x + L + 1) - __ldg(lo_x + L)) >= (uint32_t)D.nlf_cnt[u][k];
+                uint32_t lo, hi;
+                label_range(g, x, D.nlf_lab[u][k], lo, hi);
+                pass = hi - lo >= (uint32_t)D.nlf_cnt[u][k];
             }
         }
         const uint32_t mask = __ballot_sync(0xffffffffu, pass);
@@ -221,12 +228,12 @@ __global__ void __launch_bounds__(256) k_refine(Graph g, const PatDesc *__restri
         if ((w0 >> lane) & 1u) {
             const uint32_t v = D.lstart[u] + word * 32 + lane;
             if (TFSM_IN(38, v, g.n)) {
-                const uint32_t *lo_v = g.lab_off + (size_t)v * g.lab_stride;
                 uint32_t nb = D.adj[u];
                 while (nb && keep_lane && !hard_lane) {
                     const int w = __ffs(nb) - 1;
                     nb &= nb - 1;
-                    const uint32_t lo = __ldg(lo_v + D.lab[w]), hi = __ldg(lo_v + D.lab[w] + 1);
+                    uint32_t lo, hi;
+                    label_range(g, v, D.lab[w], lo, hi);
                     if (hi - lo > kLaneScan) {
                         hard_lane = 1;
                         break;
@@ -255,14 +262,14 @@ __global__ void __launch_bounds__(256) k_refine(Graph g, const PatDesc *__restri
             bits &= bits - 1;
             const uint32_t v = D.lstart[u] + word * 32 + bit;
             if (!TFSM_IN(35, v, g.n)) continue;
-            const uint32_t *lo_v = g.lab_off + (size_t)v * g.lab_stride;
             uint32_t nb = D.adj[u];
             bool ok = true;
             while (nb && ok) {
                 const int w = __ffs(nb) - 1;
                 nb &= nb - 1;
                 const uint32_t ls = D.lstart[w];
-                const uint32_t lo = __ldg(lo_v + D.lab[w]), hi = __ldg(lo_v + D.lab[w] + 1);
+                uint32_t lo, hi;
+                label_range(g, v, D.lab[w], lo, hi);
                 const uint8_t el = D.el[u][w];
                 const uint32_t *dw = dom + D.off[w];
                 bool sup = false;
@@ -437,9 +444,7 @@ __device__ __forceinline__ void setup_depth(const Team<G> &T, const Graph &g, co
         b = __ffs(m) - 1;
         const uint32_t y = S.emb[b];
         if (TFSM_IN(2, y, g.n)) {
-            const uint32_t *lo_y = g.lab_off + (size_t)y * g.lab_stride + P.lab[w];
-            lo = __ldg(lo_y);
-            hi = __ldg(lo_y + 1);
+            label_range(g, y, P.lab[w], lo, hi);
             bytes += 8;
         }
         S.blo[d][b] = lo;  // lane k owns backward neighbour b's slot

@@ -28,6 +28,9 @@
 #include "engine.hpp"
 #include "costmodel/features.hpp"
 #include "host/lg_fast.hpp"
+#if !defined(TFSM_SIMT_EMULATION)
+#include "cuda/ingest.hpp"
+#endif
 
 namespace tfsm {
 
@@ -81,6 +84,14 @@ struct DevBuf {
         p = nullptr;
         n = 0;
         bytes = 0;
+    }
+    // takes over a plain cudaMalloc allocation of `b` bytes
+    void adopt(void *q, size_t b) {
+        release();
+        cache.reset();
+        p = static_cast<T *>(q);
+        bytes = b;
+        n = b / sizeof(T);
     }
     void ensure(size_t k) {
         if (k <= n && p) return;
@@ -216,10 +227,20 @@ struct GpuEngine::Impl {
     std::vector<PatStatus> hstatus;
     int device = 0;
     std::shared_ptr<BufferCache> cache = std::make_shared<BufferCache>();
+    // also runs when a constructor throws after open()
+    ~Impl() {
+        if (stream) cudaStreamSynchronize(stream);
+        if (exec_init) cudaGraphExecDestroy(exec_init);
+        if (exec_search) cudaGraphExecDestroy(exec_search);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (ev_mid) cudaEventDestroy(ev_mid);
+        if (stream) cudaStreamDestroy(stream);
+    }
 };
 
-GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
-    auto t0 = std::chrono::steady_clock::now();
+// The device and the engine's stream and events.
+void GpuEngine::open(int device) {
     if (const char *env = std::getenv("TFSM_DEVICE")) device = std::atoi(env);
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device)
@@ -227,6 +248,44 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     TFSM_CK(cudaSetDevice(device));
     Impl &I = *impl_;
     I.device = device;
+    TFSM_CK(cudaStreamCreateWithFlags(&I.stream, cudaStreamNonBlocking));
+    TFSM_CK(cudaEventCreate(&I.ev0));
+    TFSM_CK(cudaEventCreate(&I.ev1));
+    TFSM_CK(cudaEventCreate(&I.ev_mid));
+}
+
+#if !defined(TFSM_SIMT_EMULATION)  // the CPU emulation builds its graphs on the host only
+GpuEngine::GpuEngine(const std::function<void(CUstream_st *, DeviceGraphBuild &)> &build, LgGraph &summary,
+                     int device)
+    : impl_(new Impl) {
+    auto t0 = std::chrono::steady_clock::now();
+    open(device);
+    Impl &I = *impl_;
+    DeviceGraphBuild b;
+    build(I.stream, b);
+    load_breakdown_ = b.breakdown;
+    load_h2d_bytes_ = b.h2d_bytes;
+    summary = std::move(b.summary);
+    const LgGraph &lg = summary;
+    for (size_t i = 0; i < lg.freq_vlabels.size(); ++i) I.vdense[lg.freq_vlabels[i]] = (int)i;
+    for (size_t i = 0; i < lg.freq_elabels.size(); ++i) I.edense[lg.freq_elabels[i]] = (int)i;
+    I.lstart = std::move(b.lstart);
+    I.label_mean_deg = std::move(b.label_mean_deg);
+    I.n = lg.n;
+    I.m2 = b.m2;
+    I.row_off.adopt(b.row_off.release(), b.row_off.bytes);
+    I.col.adopt(b.col.release(), b.col.bytes);
+    I.elab.adopt(b.elab.release(), b.elab.bytes);
+    I.label_start.adopt(b.label_start.release(), b.label_start.bytes);
+    I.lab_off.adopt(b.lab_off.release(), b.lab_off.bytes);
+    finish(t0);
+}
+#endif
+
+GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
+    auto t0 = std::chrono::steady_clock::now();
+    open(device);
+    Impl &I = *impl_;
     if (lg.offs[lg.n] >= (1ull << 32)) throw EngineError(5, "graph has >= 2^32 adjacency entries");
     // dense labels
     for (size_t i = 0; i < lg.freq_vlabels.size(); ++i) I.vdense[lg.freq_vlabels[i]] = (int)i;
@@ -288,7 +347,7 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     for (uint32_t x = 0; x < lg.n; ++x) off[(size_t)x + 1] = off[x] + lg.degree(from_int[x]);
     std::vector<uint32_t> col(off[lg.n]);
     std::vector<uint8_t> el(off[lg.n]);
-    // per-vertex label offsets: lab_off[x * (NL + 1) + L] = first position of a neighbour >= label L
+    // label offsets, label-major: lab_off[L * n + x] = first position of x's neighbours >= label L
     const size_t stride = (size_t)NL + 1;
     if ((size_t)lg.n * stride >= (1ull << 34)) throw EngineError(5, "label-offset table too large");
     std::vector<uint32_t> lab_off((size_t)lg.n * stride);
@@ -310,17 +369,13 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
             for (int L = 0; L <= NL; ++L) {
                 const uint32_t first = I.lstart[(size_t)L];  // lstart[NL] == n: past every id
                 while (pos < end && col[pos] < first) ++pos;
-                lab_off[x * stride + (size_t)L] = L == NL ? end : pos;
+                lab_off[(size_t)L * lg.n + x] = L == NL ? end : pos;
             }
         }
     });
     checkpoint("csr+labels");
     I.n = lg.n;
     I.m2 = off[lg.n];
-    TFSM_CK(cudaStreamCreateWithFlags(&I.stream, cudaStreamNonBlocking));
-    TFSM_CK(cudaEventCreate(&I.ev0));
-    TFSM_CK(cudaEventCreate(&I.ev1));
-    TFSM_CK(cudaEventCreate(&I.ev_mid));
     I.row_off.ensure(off.size());
     I.col.ensure(col.size() + dev::kColPad);  // padded for the search's 128-bit loads
     I.elab.ensure(el.size());
@@ -338,7 +393,15 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
                             I.stream));
     TFSM_CK(cudaStreamSynchronize(I.stream));
     checkpoint("upload");
-    I.g.n = lg.n;
+    load_h2d_bytes_ = (lab_off.size() + off.size() + col.size() + I.lstart.size()) * 4 + el.size();
+    finish(t0);
+}
+
+// Device graph view, counters, split buffers and staging, once the graph arrays are in place.
+void GpuEngine::finish(std::chrono::steady_clock::time_point t0) {
+    Impl &I = *impl_;
+    const int NL = (int)I.lstart.size() - 1;
+    I.g.n = I.n;
     I.g.m2 = I.m2;
     I.g.n_labels = NL;
     I.g.row_off = I.row_off.p;
@@ -346,14 +409,13 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     I.g.elab = I.elab.p;
     I.g.label_start = I.label_start.p;
     I.g.lab_off = I.lab_off.p;
-    I.g.lab_stride = (uint32_t)stride;
     I.counters.ensure((size_t)dev::kMaxPasses * dev::kNumCounters);
     // Two buffers of split tasks (88 B each) and as many groups (20 B each): one task per directed
     // adjacency entry, 2 M to 16 M (at most 3.1 GB; searches that find no room are set aside for the
     // next pass).  TFSM_SPLIT_CAPACITY sets both counts (tests use a tiny one to drive the
     // buffer-full paths).
     size_t task_cap = 2u << 20;
-    while (task_cap < (16u << 20) && task_cap < (size_t)lg.offs[lg.n]) task_cap *= 2;
+    while (task_cap < (16u << 20) && task_cap < (size_t)I.m2) task_cap *= 2;
     size_t group_cap = task_cap;
     if (const char *env = std::getenv("TFSM_SPLIT_CAPACITY")) {
         const long c = std::atol(env);
@@ -363,22 +425,11 @@ GpuEngine::GpuEngine(const LgGraph &lg, int device) : impl_(new Impl) {
     I.splits.ensure(2 * task_cap);
     I.groups.ensure(group_cap);
     // search-item staging for about 64 full-label domains (at most 1 M items, 16 MB)
-    I.hitems.ensure(std::min<size_t>(1u << 20, ((size_t)lg.n / 32 + 1) * 64));
-    checkpoint("buffers");
+    I.hitems.ensure(std::min<size_t>(1u << 20, ((size_t)I.n / 32 + 1) * 64));
     upload_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
-GpuEngine::~GpuEngine() {
-    if (impl_) {
-        if (impl_->stream) cudaStreamSynchronize(impl_->stream);
-        if (impl_->exec_init) cudaGraphExecDestroy(impl_->exec_init);
-        if (impl_->exec_search) cudaGraphExecDestroy(impl_->exec_search);
-        if (impl_->ev0) cudaEventDestroy(impl_->ev0);
-        if (impl_->ev1) cudaEventDestroy(impl_->ev1);
-        if (impl_->ev_mid) cudaEventDestroy(impl_->ev_mid);
-        if (impl_->stream) cudaStreamDestroy(impl_->stream);
-    }
-}
+GpuEngine::~GpuEngine() = default;
 
 uint64_t GpuEngine::graph_bytes() const {
     return (uint64_t)(impl_->n + 1) * 4 + impl_->m2 * 5 + (uint64_t)impl_->n * impl_->lstart.size() * 4;
@@ -403,6 +454,23 @@ int GpuEngine::dense_edge_label(int label) const {
     auto it = impl_->edense.find(label);
     return it == impl_->edense.end() ? -1 : it->second;
 }
+void GpuEngine::export_graph(uint32_t *row_off, uint32_t *col, uint8_t *elab, uint32_t *label_start,
+                             uint32_t *lab_off, float *label_mean_degree) const {
+    const Impl &I = *impl_;
+    const size_t stride = I.lstart.size();
+    auto get = [&](void *dst, const void *src, size_t bytes) {
+        if (dst && bytes) TFSM_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, I.stream));
+    };
+    get(row_off, I.row_off.p, ((size_t)I.n + 1) * 4);
+    get(col, I.col.p, I.m2 * 4);
+    get(elab, I.elab.p, I.m2);
+    get(label_start, I.label_start.p, stride * 4);
+    get(lab_off, I.lab_off.p, (size_t)I.n * stride * 4);
+    TFSM_CK(cudaStreamSynchronize(I.stream));
+    if (label_mean_degree)
+        std::copy(I.label_mean_deg.begin(), I.label_mean_deg.end(), label_mean_degree);
+}
+
 uint32_t GpuEngine::label_first(int dense) const { return impl_->lstart[(size_t)dense]; }
 uint32_t GpuEngine::label_size(int dense) const {
     return impl_->lstart[(size_t)dense + 1] - impl_->lstart[(size_t)dense];

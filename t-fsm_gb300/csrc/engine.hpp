@@ -1,7 +1,9 @@
 // GPU support-evaluation engine: device graph, batch evaluation of patterns, level memory.
 #pragma once
 
+#include <chrono>
 #include <cstdint>
+#include <functional>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -18,6 +20,7 @@ namespace tfsm {
 namespace dev {
 struct Graph;
 }
+struct DeviceGraphBuild;  // cuda/ingest.hpp
 
 struct EngineError : std::runtime_error {
     int code;
@@ -111,7 +114,11 @@ struct PushSource {
 
 class GpuEngine {
 public:
+    // The device graph of a host-built graph (renumbered and uploaded here).
     GpuEngine(const LgGraph &g, int device = 0);
+    // The device graph built on the GPU (cuda/ingest.hpp): `build` runs on the engine's stream;
+    // the graph's host-side facts (labels, 1-edge patterns, statistics) are moved into `summary`.
+    GpuEngine(const std::function<void(CUstream_st *, DeviceGraphBuild &)> &build, LgGraph &summary, int device = 0);
     ~GpuEngine();
     GpuEngine(const GpuEngine &) = delete;
     GpuEngine &operator=(const GpuEngine &) = delete;
@@ -128,6 +135,7 @@ public:
     void reset_times() { times_ = KernelTimes(); }
     uint64_t graph_bytes() const;
     double upload_ms() const { return upload_ms_; }
+    uint64_t load_h2d_bytes() const { return load_h2d_bytes_; }  // host -> device bytes of the graph's construction
     const std::string &load_breakdown() const { return load_breakdown_; }  // engine construction phases
     int dense_label(int label) const;  // -1 when the label is not frequent
     uint32_t n_vertices() const;
@@ -139,12 +147,19 @@ public:
     int dense_edge_label(int label) const;           // -1 when the edge label is not frequent
     uint32_t label_first(int dense) const;           // first vertex id of a dense label
     uint32_t label_size(int dense) const;            // vertices of a dense label
+    // Copies of the device graph (any pointer may be null): row_off [n+1], col / elab [m2],
+    // label_start [NL+1], lab_off [n*(NL+1)]; and the per-label mean degree [NL].
+    void export_graph(uint32_t *row_off, uint32_t *col, uint8_t *elab, uint32_t *label_start, uint32_t *lab_off,
+                      float *label_mean_degree) const;
 
 private:
+    void open(int device);
+    void finish(std::chrono::steady_clock::time_point t0);
     struct Impl;
     std::unique_ptr<Impl> impl_;
     KernelTimes times_;
     double upload_ms_ = 0;
+    uint64_t load_h2d_bytes_ = 0;
     std::string load_breakdown_;
 };
 

@@ -384,7 +384,10 @@ LgGraph build_pruned_edges(const std::vector<int> &vlabel_in, const Edges &edges
     });
     for (uint64_t c : kept_t) g.m += c;
     g.offs.assign((size_t)g.n + 1, 0);
-    for (uint32_t v = 0; v < g.n; ++v) g.offs[v + 1] = g.offs[v] + deg[v];
+    for (uint32_t v = 0; v < g.n; ++v) {
+        g.offs[v + 1] = g.offs[v] + deg[v];
+        g.max_degree = std::max(g.max_degree, deg[v]);
+    }
     g.nbr.assign(g.offs[g.n], 0);
     g.elab.assign(g.offs[g.n], 0);
     std::vector<uint32_t> src_edge(g.offs[g.n]);  // input edge of each entry

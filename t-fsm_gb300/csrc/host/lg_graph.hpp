@@ -52,6 +52,7 @@ struct LgGraph {
     std::vector<int> freq_elabels;   // ascending
     std::vector<EdgePair> edge_pairs;  // frequent 1-edge patterns, ascending (la, el, lb)
     uint32_t max_label_freq = 0;     // largest label class after pruning
+    uint32_t max_degree = 0;         // largest degree after pruning
     // ---- input statistics ----
     uint64_t input_vertices = 0, input_edges = 0;
 
@@ -235,6 +236,7 @@ inline LgGraph build_pruned(const RawLg &raw, int tau) {
             g.elab[i] = tmp[i - b].second;
         }
     }
+    for (uint32_t v = 0; v < g.n; ++v) g.max_degree = std::max(g.max_degree, g.degree(v));
     std::map<int, uint32_t> lcount;
     for (int l : g.vlabel) lcount[l]++;
     for (auto &kv : lcount) g.max_label_freq = std::max(g.max_label_freq, kv.second);

@@ -36,6 +36,7 @@ EXPORTED = (
     "tfsm_graph_from_edges",
     "tfsm_graph_free",
     "tfsm_graph_info",
+    "tfsm_graph_export",
     "tfsm_evaluate_support",
     "tfsm_evaluate_batch",
     "tfsm_evaluate_level",
@@ -91,7 +92,19 @@ class ResultC(C.Structure):
 class GraphInfoC(C.Structure):
     _fields_ = [("n_vertices", C.c_uint32), ("n_edges", C.c_uint64), ("n_frequent_vertex_labels", C.c_uint32),
                 ("n_frequent_edge_labels", C.c_uint32), ("n_frequent_edge_patterns", C.c_uint32),
-                ("max_degree", C.c_uint32), ("device_bytes", C.c_uint64), ("load_ms", C.c_double)]
+                ("max_degree", C.c_uint32), ("device_bytes", C.c_uint64), ("load_ms", C.c_double),
+                ("load_h2d_bytes", C.c_uint64)]
+
+
+class EdgePatternC(C.Structure):
+    _fields_ = [("la", C.c_int32), ("el", C.c_int32), ("lb", C.c_int32), ("cand_a", C.c_uint32),
+                ("cand_b", C.c_uint32)]
+
+
+class GraphArraysC(C.Structure):
+    _fields_ = [("row_off", C.c_void_p), ("col", C.c_void_p), ("elab", C.c_void_p), ("label_start", C.c_void_p),
+                ("lab_off", C.c_void_p), ("vlabels", C.c_void_p), ("elabels", C.c_void_p),
+                ("edge_patterns", C.c_void_p), ("label_mean_degree", C.c_void_p)]
 
 
 class OptionsC(C.Structure):
@@ -136,6 +149,7 @@ def lib() -> C.CDLL:
         L.tfsm_graph_free.argtypes = [C.c_void_p]
         L.tfsm_graph_free.restype = None
         L.tfsm_graph_info.argtypes = [C.c_void_p, C.POINTER(GraphInfoC)]
+        L.tfsm_graph_export.argtypes = [C.c_void_p, C.POINTER(GraphArraysC)]
         L.tfsm_evaluate_support.argtypes = [C.c_void_p, C.POINTER(PatternC), C.c_int32, C.c_uint32,
                                             C.POINTER(ResultC)]
         L.tfsm_evaluate_batch.argtypes = [C.c_void_p, C.POINTER(PatternC), C.c_int32, C.c_int32, C.c_uint32,
@@ -291,6 +305,25 @@ class Graph:
         gi = GraphInfoC()
         _check(lib().tfsm_graph_info(self._h, C.byref(gi)))
         return {f: getattr(gi, f) for f, _ in GraphInfoC._fields_}
+
+    def export(self) -> dict:
+        """The graph as the device holds it (tfsm_graph_export): numpy arrays row_off, col, elab,
+        label_start, lab_off, vlabels, elabels, label_mean_degree, and edge_patterns as a list of
+        (la, el, lb, cand_a, cand_b)."""
+        import numpy as np
+
+        gi = self.info()
+        n, m2 = gi["n_vertices"], 2 * gi["n_edges"]
+        nl, ne, npat = gi["n_frequent_vertex_labels"], gi["n_frequent_edge_labels"], gi["n_frequent_edge_patterns"]
+        out = dict(row_off=np.zeros(n + 1, np.uint32), col=np.zeros(m2, np.uint32), elab=np.zeros(m2, np.uint8),
+                   label_start=np.zeros(nl + 1, np.uint32), lab_off=np.zeros(n * (nl + 1), np.uint32),
+                   vlabels=np.zeros(nl, np.int32), elabels=np.zeros(ne, np.int32),
+                   label_mean_degree=np.zeros(nl, np.float32))
+        pats = (EdgePatternC * max(npat, 1))()
+        a = GraphArraysC(**{k: v.ctypes.data for k, v in out.items()}, edge_patterns=C.cast(pats, C.c_void_p))
+        _check(lib().tfsm_graph_export(self._h, C.byref(a)))
+        out["edge_patterns"] = [(p.la, p.el, p.lb, p.cand_a, p.cand_b) for p in pats[:npat]]
+        return out
 
     def evaluate(self, patterns: Iterable[Sequence[Code]], tau: int | None = None, flags: int = 0) -> list[Result]:
         arr, n, _keep = _pattern_array(patterns)

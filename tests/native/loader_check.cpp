@@ -20,7 +20,7 @@ static int compare(const LgGraph &a, const LgGraph &b) {
         return 1;                                                 \
     }
     SAME(n) SAME(m) SAME(vlabel) SAME(offs) SAME(nbr) SAME(elab) SAME(freq_vlabels) SAME(freq_elabels)
-    SAME(max_label_freq) SAME(input_vertices) SAME(input_edges)
+    SAME(max_label_freq) SAME(max_degree) SAME(input_vertices) SAME(input_edges)
     if (a.edge_pairs.size() != b.edge_pairs.size()) {
         std::printf("differ: edge_pairs size %zu vs %zu\n", a.edge_pairs.size(), b.edge_pairs.size());
         return 1;
