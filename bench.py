@@ -271,11 +271,25 @@ TRAINING = [(dict(WORKLOADS["cfg1"]["gen"], seed=s), 200, 4) for s in (10, 11, 1
            [(dict(CFG2_GEN, seed=s), 9000, 5) for s in (10, 11, 12)]
 
 
-def train_cost_model(tfsm):
+def training_set(w: dict) -> list:
+    """Graphs the cost model learns from: configuration 1 and 2 shapes (seeds 10-12) and, for a
+    hub-graph workload (several edge labels or hubs past 10k neighbours), two graphs of the
+    workload's own shape at a quarter of its size (seeds 10, 11; tau / 4, at most 4 vertices):
+    never the timed graph."""
+    g = w["gen"]
+    extra = []
+    if g["elabels"] > 1 or g["max_degree"] >= 10000:
+        small = dict(g, n=g["n"] // 4, max_degree=max(1, g["max_degree"] // 4))
+        extra = [(dict(small, seed=s), max(1, w["tau"] // 4), min(4, w["max_nodes"])) for s in (10, 11)]
+    return TRAINING + extra
+
+
+def train_cost_model(tfsm, w: dict):
     import numpy as np
 
     feats, costs = [], []
-    for k, (gen, tau, mn) in enumerate(TRAINING):
+    train = training_set(w)
+    for k, (gen, tau, mn) in enumerate(train):
         with tfsm.Graph.load(make_graph(dict(gen=gen)), tau) as gt:
             gt.set_order_policy(tfsm.ORDER_RANDOM, seed=k + 1)
             gt.record_orders(True)
@@ -287,8 +301,11 @@ def train_cost_model(tfsm):
     model = tfsm.CostModel(seed=1)
     t0 = time.perf_counter()
     mse = model.train(x, t, epochs=60, batch=64, lr=2e-3, seed=2)
+    what = "configuration 1 and 2 shapes, seeds 10-12"
+    if len(train) > len(TRAINING):
+        what += "; the workload's shape at a quarter of its size, seeds 10-11, tau / 4"
     return model, {"training_records": int(len(x)), "train_mse": mse, "train_s": time.perf_counter() - t0,
-                   "training_graphs": "configuration 1 and 2 shapes, seeds 10-12, plain miner, random orders"}
+                   "training_graphs": what + "; plain miner, random orders"}
 
 
 def gpu_arm(args, w, world, rank):
@@ -360,18 +377,18 @@ def gpu_arm(args, w, world, rank):
     nop_ms, nruns = timed(tfsm.FLAG_NO_SUBPATTERN_PRUNING, 1, few)
 
     # ---- learned matching orders: a cost model trained on records of other graphs ----
-    model, mlp_info = train_cost_model(tfsm)
+    model, mlp_info = train_cost_model(tfsm, w)
+    tuned = None
     try:
         g.set_order_policy(tfsm.ORDER_MODEL, model=model)
         identical_mlp = outputs(0) == batched_set
         mlp_ms, mruns = timed(0, 1, max(1, args.steps // 2))
         g.set_order_policy(tfsm.ORDER_GQL)
+        if args.tuned:
+            tuned = tuned_arm(args, w, g, tfsm, timed, outputs, batched_set, model)
     finally:
+        g.set_order_policy(tfsm.ORDER_GQL)
         model.close()
-
-    tuned = None
-    if args.tuned:
-        tuned = tuned_arm(args, w, g, tfsm, timed, outputs, batched_set)
 
     # ---- roofline of the dominant kernel (the search): algorithmic bytes / device time ----
     s_ms = sum(st["search_ms"] for st in stats)
@@ -454,9 +471,9 @@ def gpu_arm(args, w, world, rank):
     return 0 if same else 1
 
 
-def tuned_arm(args, w, g, tfsm, timed, outputs, batched_set) -> dict:
+def tuned_arm(args, w, g, tfsm, timed, outputs, batched_set, model) -> dict:
     """Batched path with the knobs the autotuner picks per level on a held-out graph of the same
-    shape (seed + 10), then applied to the benchmarked graph."""
+    shape (seed + 10), then applied to the benchmarked graph; alone and with the learned orders."""
     import importlib.util
 
     spec = importlib.util.spec_from_file_location("autotune", PKG / "autotune.py")
@@ -472,11 +489,17 @@ def tuned_arm(args, w, g, tfsm, timed, outputs, batched_set) -> dict:
             g.set_level_options(int(lv), o)
         identical = outputs(0) == batched_set
         ms, _ = timed(0, 1, max(1, args.steps // 2))
+        g.set_order_policy(tfsm.ORDER_MODEL, model=model)
+        identical_mlp = outputs(0) == batched_set
+        ms_mlp, _ = timed(0, 1, max(1, args.steps // 2))
     finally:
+        g.set_order_policy(tfsm.ORDER_GQL)
         g.set_level_options(0, None)
     evals = g.mine(max_nodes=w["max_nodes"])["evaluations"]
     return {"value": evals * 1e3 / ms, "ms_per_step": ms, "identical_output": identical, "tune_s": tune_s,
             "tuned_on": "held-out graph of the same shape (seed + 10)",
+            "with_learned_orders": {"value": evals * 1e3 / ms_mlp, "ms_per_step": ms_mlp,
+                                    "identical_output": identical_mlp, "over_tuned": ms / ms_mlp},
             "levels": {str(k): v for k, v in best.items()}}
 
 

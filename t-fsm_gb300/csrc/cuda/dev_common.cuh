@@ -107,6 +107,62 @@ struct SearchItem {
     uint32_t word_hi;
 };
 
+// The search work of one call, decoded by the search kernel from two small tables instead of an
+// item array.  The call's (pattern, representative vertex) pairs form groups (in the engine: the
+// k-th representative of every pattern of a window); the items of a group run round by round,
+// round t holding run t (of `chunk_words` bitmap words) of every entry with more than t runs.
+// Entries are sorted by run count, descending, so the entries active in a round are a prefix and
+// item k of a group is found by a binary search over `before`.
+struct ItemEntry {
+    uint32_t pat;
+    uint16_t u;
+    uint16_t pad;
+    uint32_t words;      // bitmap words of u's domain
+    uint32_t runs;       // ceil(words / chunk_words), >= 1
+    uint64_t before;     // items of the group in rounds [0, runs)
+};
+struct ItemGroup {
+    uint64_t first_item;  // items of the earlier groups
+    uint32_t first_entry;
+    uint32_t n_entries;   // >= 1
+};
+
+// Item `k` (< the items of all groups).
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline SearchItem item_at(const ItemGroup *gr, uint32_t n_groups, const ItemEntry *en, uint32_t chunk_words,
+                          uint64_t k) {
+    uint32_t lo = 0, hi = n_groups;  // the last group whose first item is <= k
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (gr[mid].first_item <= k) lo = mid;
+        else hi = mid;
+    }
+    const ItemGroup G = gr[lo];
+    const ItemEntry *e = en + G.first_entry;
+    const uint64_t kk = k - G.first_item;
+    // the last entry i with before > kk: rounds [runs of i + 1, runs of i) hold entries 0..i
+    uint32_t a = 0, b = G.n_entries;
+    while (b - a > 1) {
+        const uint32_t mid = (a + b) >> 1;
+        if (e[mid].before > kk) a = mid;
+        else b = mid;
+    }
+    const uint64_t below = a + 1 < G.n_entries ? e[a + 1].before : 0;
+    const uint32_t r0 = a + 1 < G.n_entries ? e[a + 1].runs : 0;
+    const uint64_t off = kk - below;
+    const uint32_t t = r0 + (uint32_t)(off / (a + 1));
+    const ItemEntry &E = e[off % (a + 1)];
+    SearchItem it;
+    it.pat = E.pat;
+    it.u = E.u;
+    it.pad = 0;
+    it.word_lo = t * chunk_words;
+    it.word_hi = it.word_lo + chunk_words < E.words ? it.word_lo + chunk_words : E.words;
+    return it;
+}
+
 // Bits of a 32-candidate word that belong to part `part` of 2^log2 interleaved parts.
 #ifdef __CUDACC__
 __host__ __device__
@@ -188,6 +244,8 @@ struct SearchParams {
     uint32_t parts_log2;     // every item is claimed 2^parts_log2 times, claim k searching the bits b of
                              //    its words with b % 2^parts_log2 == k (small calls: more warps busy)
     uint32_t n_pats;         // patterns of the batch
+    uint32_t n_groups;       // item groups (ItemGroup) of the call
+    uint32_t chunk_words;    // bitmap words per item
     uint64_t words;          // size of each level bitmap pool (32-bit words)
 };
 

@@ -860,7 +860,8 @@ __device__ __forceinline__ bool pattern_stops(const Team<G> &T, const PatStatus 
 template <int G>
 __global__ void __launch_bounds__(kSearchWarps * 32, kSearchMinBlocks) k_search(Graph g, const PatDesc *__restrict__ descs,
                                                               PatStatus *__restrict__ st,
-                                                              const SearchItem *__restrict__ items, SearchParams prm,
+                                                              const ItemGroup *__restrict__ igroups,
+                                                              const ItemEntry *__restrict__ ientries, SearchParams prm,
                                                               uint32_t *__restrict__ counters,
                                                               const uint32_t *__restrict__ dom,
                                                               uint32_t *__restrict__ found,
@@ -886,7 +887,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32, kSearchMinBlocks) k_search(
         if (T.lane == 0) it = atomicAdd(&counters[0], 1u);
         it = T.bcast(it, 0);
         if (it >= (prm.n_items << prm.parts_log2)) break;
-        const SearchItem item = items[it >> prm.parts_log2];
+        const SearchItem item = item_at(igroups, prm.n_groups, ientries, prm.chunk_words, it >> prm.parts_log2);
         const uint32_t pmask = part_mask(it & ((1u << prm.parts_log2) - 1), prm.parts_log2);
         const uint32_t p = item.pat;
         const int u = item.u;
@@ -1155,9 +1156,10 @@ cudaError_t launch_refine(const Graph &g, const PatDesc *descs, PatStatus *st, c
 namespace {
 
 template <int G>
-cudaError_t launch_search_t(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchItem *items,
-                            const SearchParams &prm, uint32_t *counters, const uint32_t *dom, uint32_t *found,
-                            uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s) {
+cudaError_t launch_search_t(const Graph &g, const PatDesc *descs, PatStatus *st, const ItemGroup *igroups,
+                            const ItemEntry *ientries, const SearchParams &prm, uint32_t *counters,
+                            const uint32_t *dom, uint32_t *found, uint32_t *failed, SplitTask *splits,
+                            SplitGroup *groups, cudaStream_t s) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<G>, kSearchWarps * 32, 0);
     if (per_sm <= 0) per_sm = 1;
@@ -1165,8 +1167,8 @@ cudaError_t launch_search_t(const Graph &g, const PatDesc *descs, PatStatus *st,
     const uint64_t teams = (uint64_t)kSearchWarps * 32 / G;
     const uint64_t need = (((uint64_t)prm.n_items << prm.parts_log2) + teams - 1) / teams;
     if (blocks > need) blocks = need;
-    TFSM_LAUNCH(k_search<G>, (unsigned)blocks, kSearchWarps * 32, s, g, descs, st, items, prm, counters, dom, found,
-                failed, splits, groups);
+    TFSM_LAUNCH(k_search<G>, (unsigned)blocks, kSearchWarps * 32, s, g, descs, st, igroups, ientries, prm, counters,
+                dom, found, failed, splits, groups);
     return cudaGetLastError();
 }
 
@@ -1185,16 +1187,18 @@ cudaError_t launch_split_t(const Graph &g, const PatDesc *descs, PatStatus *st, 
 
 }  // namespace
 
-cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchItem *items,
-                          const SearchParams &prm, uint32_t *counters, const uint32_t *dom, uint32_t *found,
-                          uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s) {
+cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, const ItemGroup *igroups,
+                          const ItemEntry *ientries, const SearchParams &prm, uint32_t *counters, const uint32_t *dom,
+                          uint32_t *found, uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s) {
     if (prm.n_items == 0) return cudaSuccess;
+    if (prm.n_groups == 0 || prm.chunk_words == 0 || !igroups || !ientries) return cudaErrorInvalidValue;
     if (prm.split && (!splits || !groups || prm.split_cap == 0 || prm.group_cap == 0 || prm.split_slice == 0))
         return cudaErrorInvalidValue;
     cudaError_t e;
-    if (prm.team_lanes == 8) e = launch_search_t<8>(g, descs, st, items, prm, counters, dom, found, failed, splits, groups, s);
+    if (prm.team_lanes == 8)
+        e = launch_search_t<8>(g, descs, st, igroups, ientries, prm, counters, dom, found, failed, splits, groups, s);
     else if (prm.team_lanes == 32)
-        e = launch_search_t<32>(g, descs, st, items, prm, counters, dom, found, failed, splits, groups, s);
+        e = launch_search_t<32>(g, descs, st, igroups, ientries, prm, counters, dom, found, failed, splits, groups, s);
     else return cudaErrorInvalidValue;
 #ifdef TFSM_BOUNDS_CHECK
     if (e == cudaSuccess && cudaStreamSynchronize(s) != cudaSuccess) {

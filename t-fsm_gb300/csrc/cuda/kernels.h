@@ -32,9 +32,9 @@ cudaError_t launch_refine(const Graph &g, const PatDesc *descs, PatStatus *st, c
 
 // One search pass: k_search over `prm.n_items` items.  `counters` (kNumCounters x u32) must be
 // zero on entry; `splits` holds two buffers of prm.split_cap tasks each.
-cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchItem *items,
-                          const SearchParams &prm, uint32_t *counters, const uint32_t *dom, uint32_t *found,
-                          uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s);
+cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, const ItemGroup *igroups,
+                          const ItemEntry *ientries, const SearchParams &prm, uint32_t *counters, const uint32_t *dom,
+                          uint32_t *found, uint32_t *failed, SplitTask *splits, SplitGroup *groups, cudaStream_t s);
 
 // Split round `round` (0 <= round < kMaxRounds) of the pass whose counters are `counters`: the tasks
 // written for it by the previous phase, each with a step budget of `budget` chunk evaluations (0:

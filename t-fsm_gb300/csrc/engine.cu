@@ -93,10 +93,18 @@ struct DevBuf {
         bytes = b;
         n = b / sizeof(T);
     }
+    // Room for at least k elements.  Cache-backed buffers come in power-of-two sizes (64 KiB at
+    // least), so that pools freed by earlier calls fit later ones; other buffers grow to at least
+    // twice their size.  A reallocation (cudaMalloc synchronises the device) is then rare.
     void ensure(size_t k) {
         if (k <= n && p) return;
+        size_t want = sizeof(T) * std::max<size_t>(k, cache ? 1 : 2 * n);
+        if (cache) {
+            size_t b = 64u << 10;
+            while (b < want) b *= 2;
+            want = b;
+        }
         release();
-        const size_t want = sizeof(T) * std::max<size_t>(k, 1);
         size_t got = 0;
         void *q = cache ? cache->take(want, got) : nullptr;
         if (!q) {
@@ -106,28 +114,6 @@ struct DevBuf {
         p = static_cast<T *>(q);
         bytes = got;
         n = got / sizeof(T);
-    }
-};
-
-// Page-locked host staging buffer (grows, never shrinks): copies from it are true DMA transfers.
-template <class T>
-struct PinnedBuf {
-    T *p = nullptr;
-    size_t n = 0;
-    PinnedBuf() = default;
-    PinnedBuf(const PinnedBuf &) = delete;
-    PinnedBuf &operator=(const PinnedBuf &) = delete;
-    ~PinnedBuf() {
-        if (p) cudaFreeHost(p);
-    }
-    void ensure(size_t k) {
-        if (k <= n && p) return;
-        const size_t want = std::max<size_t>(k + k / 2, 1024);
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        n = 0;
-        TFSM_CK(cudaHostAlloc((void **)&p, want * sizeof(T), cudaHostAllocDefault));
-        n = want;
     }
 };
 
@@ -218,8 +204,8 @@ struct GpuEngine::Impl {
     DevBuf<PatStatus> status;
     DevBuf<uint32_t> item_pu;
     DevBuf<uint64_t> prefix;
-    DevBuf<dev::SearchItem> items;
-    PinnedBuf<dev::SearchItem> hitems;  // staging of the search items (rewritten each call)
+    DevBuf<dev::ItemGroup> igroups;    // the call's search work (dev::item_at)
+    DevBuf<dev::ItemEntry> ientries;
     DevBuf<dev::SourceLevel> srcs;      // the earlier calls' pools read by this call's domain init
     DevBuf<uint32_t> counters;
     DevBuf<dev::SplitTask> splits;  // two buffers of split tasks (ping-pong between rounds)
@@ -424,8 +410,7 @@ void GpuEngine::finish(std::chrono::steady_clock::time_point t0) {
     }
     I.splits.ensure(2 * task_cap);
     I.groups.ensure(group_cap);
-    // search-item staging for about 64 full-label domains (at most 1 M items, 16 MB)
-    I.hitems.ensure(std::min<size_t>(1u << 20, ((size_t)I.n / 32 + 1) * 64));
+
     upload_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
@@ -617,6 +602,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         D.express = express[p];
     }
     if (total >= (1ull << 32)) throw EngineError(6, "batch needs more than 2^32 bitmap words");
+    phase(0);
     L.words = total;
     L.dom.ensure(total);
     L.found.ensure(total);
@@ -675,7 +661,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         return ms;
     };
 
-    phase(0);
+    phase(1);
     // ---- domain init and the first arc-consistency rounds: one launch sequence (a CUDA graph),
     // then one status read.  k_refine itself skips patterns that can no longer reach tau or that
     // the previous round left unchanged.
@@ -739,7 +725,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         for (size_t p = 0; p < P; ++p)
             if (express[p] && ((I.hstatus[p].changed >> 31) & 1u)) express[p] = 0;
 
-    phase(1);
+    phase(2);
     // ---- decisions from domain sizes; plans for the rest ----
     std::vector<char> need_search(P, 0);
     bool any_search = false;
@@ -841,7 +827,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     TFSM_CK(cudaMemcpyAsync(L.descs.p, L.hdescs.data(), P * sizeof(PatDesc), cudaMemcpyHostToDevice, I.stream));
     times_.h2d_bytes += P * sizeof(PatDesc);
 
-    phase(2);
+    phase(3);
     // ---- search items ----
     // Vertex-major, as the reference evaluates one pattern vertex after another
     // (parallel/comper.h:1181-1239): every pattern first searches its representative with the
@@ -849,7 +835,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     // candidates are by then largely marked found by the earlier embeddings.  Within one rank the
     // chunks of all patterns are interleaved so that every pattern progresses and early exit cuts
     // the rest.
-    size_t n_items = 0;  // search items, written into the pinned staging buffer I.hitems
+    uint64_t n_items = 0;  // search items of the call (decoded on the device from its groups)
     uint32_t parts_log2 = 0;
     // lanes per search: teams of 8 when asked for, when the call has several patterns to search
     // (single-pattern calls measured faster with whole warps) and every one fits a team's state
@@ -863,34 +849,22 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
             }
         if (max_n <= 8 && searched > 1) team_lanes = 8;
     }
+    const uint32_t cw = std::max<uint32_t>(1, opt.chunk_words);
+    std::vector<dev::ItemGroup> igroups;
+    std::vector<dev::ItemEntry> ientries;
     {
         // The search kernel claims items in order, so the order is the order in time.  With one
         // vertex-major order over a call of hundreds of patterns, a pattern's second vertex waits
         // until the first vertex of every pattern has been searched, although it is often the one
         // that shows the pattern infrequent and would have cut the first vertex's failing
         // searches: windows of `rank_window` patterns bound that wait (vertex-major inside each).
-        struct Q {
-            uint32_t p, u, w, words;
-        };
+        // One item group per (window, rank): the rank-k representative of each of the window's
+        // patterns, whose runs of words are interleaved round by round (dev::item_at).
         std::vector<uint32_t> searched;
         for (size_t p = 0; p < P; ++p)
             if (need_search[p]) searched.push_back((uint32_t)p);
-        const uint32_t cw = std::max<uint32_t>(1, opt.chunk_words);
-        // Calls with few words (a level of a few patterns) split every item into interleaved parts
-        // of its 32 candidates, so that enough warps search in parallel: about four items per
-        // resident warp of the search kernel (152 SMs x 40 warps on GB300).
-        uint64_t n_plain = 0;
-        for (uint32_t p : searched) {
-            const PatDesc &D = L.hdescs[p];
-            for (int u = 0; u < D.n; ++u)
-                if (D.rep[u] == u) n_plain += (D.words[u] + cw - 1) / cw;
-        }
-        const uint64_t want = 4ull * (uint64_t)dev::resident_search_warps() * (32u / team_lanes);
-        while (parts_log2 < 5 && (n_plain << parts_log2) < want) ++parts_log2;
-        I.hitems.ensure((size_t)n_plain);
-        dev::SearchItem *out = I.hitems.p;
         const size_t win = opt.rank_window ? opt.rank_window : std::max<size_t>(1, searched.size());
-        std::vector<std::vector<Q>> ranks;  // ranks[k]: the k-th smallest representative of each pattern
+        std::vector<std::vector<dev::ItemEntry>> ranks;  // ranks[k]: the k-th smallest representative of each pattern
         for (size_t a = 0; a < searched.size(); a += win) {
             for (auto &r : ranks) r.clear();
             for (size_t i = a; i < std::min(searched.size(), a + win); ++i) {
@@ -899,43 +873,66 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
                 std::vector<int> reps;
                 for (int u = 0; u < D.n; ++u)
                     if (D.rep[u] == u) reps.push_back(u);
-                const PatStatus &s = I.hstatus[p];
+                const PatStatus &st = I.hstatus[p];
                 std::stable_sort(reps.begin(), reps.end(),
-                                 [&](int x, int y) { return s.dom_size[x] < s.dom_size[y]; });
+                                 [&](int x, int y) { return st.dom_size[x] < st.dom_size[y]; });
                 for (size_t k = 0; k < reps.size(); ++k) {
+                    const uint32_t words = D.words[reps[k]];
+                    if (!words) continue;
                     if (ranks.size() <= k) ranks.emplace_back();
-                    ranks[k].push_back({p, (uint32_t)reps[k], 0, D.words[reps[k]]});
+                    dev::ItemEntry e;
+                    std::memset(&e, 0, sizeof(e));
+                    e.pat = p;
+                    e.u = (uint16_t)reps[k];
+                    e.words = words;
+                    e.runs = (words + cw - 1) / cw;
+                    ranks[k].push_back(e);
                 }
             }
-            for (auto &qs : ranks) {
-                bool more = true;
-                while (more) {
-                    more = false;
-                    for (Q &q : qs) {
-                        if (q.w >= q.words) continue;
-                        dev::SearchItem it;
-                        it.pat = q.p;
-                        it.u = (uint16_t)q.u;
-                        it.pad = 0;
-                        it.word_lo = q.w;
-                        it.word_hi = std::min(q.words, q.w + cw);
-                        q.w = it.word_hi;
-                        out[n_items++] = it;
-                        more = true;
-                    }
+            for (auto &es : ranks) {
+                if (es.empty()) continue;
+                std::stable_sort(es.begin(), es.end(),
+                                 [](const dev::ItemEntry &x, const dev::ItemEntry &y) { return x.runs > y.runs; });
+                // before[i] = sum over j of min(runs[j], runs[i])
+                const size_t m = es.size();
+                uint64_t acc = 0;
+                for (size_t i = m; i-- > 0;) {
+                    const uint32_t below = i + 1 < m ? es[i + 1].runs : 0;
+                    acc += (uint64_t)(i + 1) * (es[i].runs - below);
+                    es[i].before = acc;
                 }
+                dev::ItemGroup gr;
+                gr.first_item = n_items;
+                gr.first_entry = (uint32_t)ientries.size();
+                gr.n_entries = (uint32_t)m;
+                igroups.push_back(gr);
+                ientries.insert(ientries.end(), es.begin(), es.end());
+                n_items += es[0].before;
             }
         }
+        // Calls with few words (a level of a few patterns) split every item into interleaved parts
+        // of its 32 candidates, so that enough warps search in parallel: about four items per
+        // resident warp of the search kernel (152 SMs x 40 warps on GB300).
+        const uint64_t want = 4ull * (uint64_t)dev::resident_search_warps() * (32u / team_lanes);
+        while (parts_log2 < 5 && (n_items << parts_log2) < want) ++parts_log2;
     }
-    I.items.ensure(n_items);
-    TFSM_CK(cudaMemcpyAsync(I.items.p, I.hitems.p, n_items * sizeof(dev::SearchItem), cudaMemcpyHostToDevice,
-                            I.stream));
-    times_.h2d_bytes += n_items * sizeof(dev::SearchItem);
+    if (n_items >= (1ull << 32) >> parts_log2) throw EngineError(6, "call has more than 2^32 search items");
+    I.igroups.ensure(std::max<size_t>(1, igroups.size()));
+    I.ientries.ensure(std::max<size_t>(1, ientries.size()));
+    if (!igroups.empty()) {
+        TFSM_CK(cudaMemcpyAsync(I.igroups.p, igroups.data(), igroups.size() * sizeof(dev::ItemGroup),
+                                cudaMemcpyHostToDevice, I.stream));
+        TFSM_CK(cudaMemcpyAsync(I.ientries.p, ientries.data(), ientries.size() * sizeof(dev::ItemEntry),
+                                cudaMemcpyHostToDevice, I.stream));
+    }
+    times_.h2d_bytes += igroups.size() * sizeof(dev::ItemGroup) + ientries.size() * sizeof(dev::ItemEntry);
     dev::SearchParams prm;
     std::memset(&prm, 0, sizeof(prm));
     prm.tau = tau;
     prm.exact = opt.exact ? 1 : 0;
     prm.n_items = (uint32_t)n_items;
+    prm.n_groups = (uint32_t)igroups.size();
+    prm.chunk_words = cw;
     prm.split = opt.split && opt.step_budget ? 1 : 0;
     prm.split_slice = std::max<uint32_t>(1, opt.split_slice);
     prm.hub_span = opt.hub_span;
@@ -949,7 +946,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     prm.team_lanes = team_lanes;
     prm.n_pats = (uint32_t)P;
     prm.words = total;
-    phase(3);
+    phase(4);
     // Passes.  In each, a search may take `budget` chunk steps before its unexplored remainder
     // becomes split tasks; split rounds then work those off, each task again with a budget (twice
     // the pass's, doubling per round up to 8x after the first `kFixedRounds`, none in the 64th
@@ -972,8 +969,8 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         const int fixed = prm.split ? kFixedRounds : 0;
         run_captured(I.stream, I.exec_search, [&]() {
             TFSM_CK(cudaMemsetAsync(cnt, 0, dev::kNumCounters * sizeof(uint32_t), I.stream));
-            TFSM_CK(dev::launch_search(I.g, L.descs.p, I.status.p, I.items.p, pk, cnt, L.dom.p, L.found.p,
-                                       L.failed.p, I.splits.p, I.groups.p, I.stream));
+            TFSM_CK(dev::launch_search(I.g, L.descs.p, I.status.p, I.igroups.p, I.ientries.p, pk, cnt, L.dom.p,
+                                       L.found.p, L.failed.p, I.splits.p, I.groups.p, I.stream));
             for (int r = 0; r < fixed; ++r)
                 TFSM_CK(dev::launch_split_round(I.g, L.descs.p, I.status.p, pk, cnt, r, round_budget, L.dom.p,
                                                 L.found.p, L.failed.p, I.splits.p, I.groups.p, I.stream));
@@ -1018,7 +1015,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
                                       " (" + std::to_string(rec[0]) + " violations)");
     }
 
-    phase(4);
+    phase(5);
     if (opt.records)
         for (auto &pl : planned) {
             const PatStatus &s = I.hstatus[pl.p];
@@ -1049,7 +1046,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         if (opt.exact) r.frequent = mn >= tau;
         else r.frequent = s.state == dev::kFrequent || (s.state == dev::kRunning && all_reps);
     }
-    phase(5);
+    phase(6);
 }
 
 }  // namespace tfsm

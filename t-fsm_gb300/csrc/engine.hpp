@@ -72,7 +72,8 @@ struct EngineOptions {
 struct KernelTimes {                   // accumulated device time (CUDA events), milliseconds
     double init_ms = 0, refine_ms = 0, search_ms = 0;
     double engine_ms = 0;              // host wall time inside evaluate() (device phases included)
-    double phase_ms[6] = {};           // of which: descriptors, init+refine, plans, items, search, results
+    double phase_ms[7] = {};           // of which: descriptors, pools+upload, init+refine, plans, items,
+                                       //   search, results
     uint64_t init_launches = 0, refine_launches = 0, search_launches = 0;  // kernel launches
     uint64_t search_calls = 0;         // search phases (k_search, plus k_split when splitting)
     uint64_t init_words = 0, refine_words = 0;  // bitmap words processed

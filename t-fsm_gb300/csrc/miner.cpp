@@ -290,10 +290,13 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                                  eng.times().search_ms - search_before, (unsigned long long)srch,
                                  (unsigned long long)mx);
                     const KernelTimes &now = eng.times();
-                    std::fprintf(stderr, "          host phases ms: desc %.3f init+refine %.3f plans %.3f items %.3f search %.3f results %.3f\n",
+                    std::fprintf(stderr,
+                                 "          host phases ms: desc %.3f pools %.3f init+refine %.3f plans %.3f items %.3f "
+                                 "search %.3f results %.3f\n",
                                  now.phase_ms[0] - before.phase_ms[0], now.phase_ms[1] - before.phase_ms[1],
                                  now.phase_ms[2] - before.phase_ms[2], now.phase_ms[3] - before.phase_ms[3],
-                                 now.phase_ms[4] - before.phase_ms[4], now.phase_ms[5] - before.phase_ms[5]);
+                                 now.phase_ms[4] - before.phase_ms[4], now.phase_ms[5] - before.phase_ms[5],
+                                 now.phase_ms[6] - before.phase_ms[6]);
                     std::fprintf(stderr,
                                  "          passes %llu (%llu set aside), split: %llu searches, %llu tasks\n",
                                  (unsigned long long)(now.search_passes - before.search_passes),

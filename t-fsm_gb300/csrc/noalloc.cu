@@ -6,7 +6,7 @@
 // whom the implicit device-wide synchronisation of cudaMalloc/cudaFree is unacceptable, or code that
 // has run out of device memory and still has to finish its work.  Those callers get the same
 // kernels as tfsm_evaluate_support, but every per-call buffer (pattern descriptor, status,
-// work items, the three domain bitmaps) is carved out of one file-scope device array of fixed size,
+// work-item tables, the three domain bitmaps) is carved out of one file-scope device array of fixed size,
 // so the call itself allocates nothing on the device and calls no allocating library routine.
 //
 // Limits and sharing:
@@ -26,6 +26,7 @@
 //     device is restored before the call returns.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -219,15 +220,14 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
         words += D.words[u];
     }
     // ---- scratch layout ----
-    size_t max_items = 0;
-    for (int u = 0; u < n; ++u) max_items += (D.words[u] + kChunkWords - 1) / kChunkWords;
     const size_t o_desc = 0;
     const size_t o_status = align_up(o_desc + sizeof(PatDesc));
     const size_t o_counters = align_up(o_status + sizeof(PatStatus));
     const size_t o_item_pu = align_up(o_counters + dev::kNumCounters * sizeof(uint32_t));
     const size_t o_prefix = align_up(o_item_pu + dev::kMaxN * sizeof(uint32_t));
-    const size_t o_items = align_up(o_prefix + (dev::kMaxN + 1) * sizeof(uint64_t));
-    const size_t o_pools = align_up(o_items + max_items * sizeof(dev::SearchItem));
+    const size_t o_igroup = align_up(o_prefix + (dev::kMaxN + 1) * sizeof(uint64_t));
+    const size_t o_ientries = align_up(o_igroup + sizeof(dev::ItemGroup));
+    const size_t o_pools = align_up(o_ientries + dev::kMaxN * sizeof(dev::ItemEntry));
     const size_t need = o_pools + 3 * words * sizeof(uint32_t);
     if (need > kScratchBytes) {
         msg = "pattern too large for the allocation-free path: its domain bitmaps and work items need more than "
@@ -251,7 +251,8 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     uint32_t *d_counters = reinterpret_cast<uint32_t *>(base + o_counters);
     uint32_t *d_item_pu = reinterpret_cast<uint32_t *>(base + o_item_pu);
     uint64_t *d_prefix = reinterpret_cast<uint64_t *>(base + o_prefix);
-    dev::SearchItem *d_items = reinterpret_cast<dev::SearchItem *>(base + o_items);
+    dev::ItemGroup *d_igroup = reinterpret_cast<dev::ItemGroup *>(base + o_igroup);
+    dev::ItemEntry *d_ientries = reinterpret_cast<dev::ItemEntry *>(base + o_ientries);
     uint32_t *d_dom = reinterpret_cast<uint32_t *>(base + o_pools);
     uint32_t *d_found = d_dom + words;
     uint32_t *d_failed = d_found + words;
@@ -305,48 +306,48 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     // ---- search ----
     for (int u = 0; u < n; ++u) plan_from(n, adj, deg, st.dom_size, u, D.order[u], D.bn[u]);
     NA_CK(cudaMemcpyAsync(d_desc, &D, sizeof(D), cudaMemcpyHostToDevice, s));
-    // Staged through a small pageable buffer: cudaMemcpyAsync from pageable memory returns once the
-    // source has been copied out, so the buffer can be refilled without waiting for the device.
-    constexpr size_t kBuf = 1024;
-    dev::SearchItem buf[kBuf];
-    size_t n_items = 0, fill = 0;
-    uint32_t next_word[dev::kMaxN] = {0};
-    for (bool more = true; more;) {  // round-robin over vertices, as the engine interleaves its items
-        more = false;
-        for (int u = 0; u < n; ++u) {
-            if (next_word[u] >= D.words[u]) continue;
-            dev::SearchItem it;
-            it.pat = 0;
-            it.u = (uint16_t)u;
-            it.pad = 0;
-            it.word_lo = next_word[u];
-            it.word_hi = next_word[u] + kChunkWords < D.words[u] ? next_word[u] + kChunkWords : D.words[u];
-            next_word[u] = it.word_hi;
-            buf[fill++] = it;
-            more = true;
-            if (fill == kBuf) {
-                NA_CK(cudaMemcpyAsync(d_items + n_items, buf, fill * sizeof(it), cudaMemcpyHostToDevice, s));
-                n_items += fill;
-                fill = 0;
-            }
-        }
+    // One item group over every vertex: their runs of words interleaved round by round, as the
+    // engine interleaves its items (dev::item_at decodes them on the device).
+    dev::ItemEntry ent[dev::kMaxN];
+    size_t m = 0;
+    for (int u = 0; u < n; ++u) {
+        if (!D.words[u]) continue;
+        dev::ItemEntry &e = ent[m++];
+        std::memset(&e, 0, sizeof(e));
+        e.pat = 0;
+        e.u = (uint16_t)u;
+        e.words = D.words[u];
+        e.runs = (D.words[u] + kChunkWords - 1) / kChunkWords;
     }
-    if (fill) {
-        NA_CK(cudaMemcpyAsync(d_items + n_items, buf, fill * sizeof(dev::SearchItem), cudaMemcpyHostToDevice, s));
-        n_items += fill;
+    std::stable_sort(ent, ent + m, [](const dev::ItemEntry &x, const dev::ItemEntry &y) { return x.runs > y.runs; });
+    uint64_t n_items = 0;
+    for (size_t i = m; i-- > 0;) {
+        const uint32_t below = i + 1 < m ? ent[i + 1].runs : 0;
+        n_items += (uint64_t)(i + 1) * (ent[i].runs - below);
+        ent[i].before = n_items;
+    }
+    dev::ItemGroup grp;
+    grp.first_item = 0;
+    grp.first_entry = 0;
+    grp.n_entries = (uint32_t)m;
+    if (m) {
+        NA_CK(cudaMemcpyAsync(d_igroup, &grp, sizeof(grp), cudaMemcpyHostToDevice, s));
+        NA_CK(cudaMemcpyAsync(d_ientries, ent, m * sizeof(dev::ItemEntry), cudaMemcpyHostToDevice, s));
     }
     dev::SearchParams prm;
     std::memset(&prm, 0, sizeof(prm));
     prm.tau = tau;
     prm.exact = exact ? 1 : 0;
     prm.n_items = (uint32_t)n_items;
+    prm.n_groups = 1;
+    prm.chunk_words = kChunkWords;
     prm.split = 0;  // no hub splitting on this path (its task buffers would need more scratch)
     prm.isect_ratio = 16;
     prm.team_lanes = 32;
     prm.n_pats = 1;
     prm.words = words;
-    NA_CK(dev::launch_search(g, d_desc, d_status, d_items, prm, d_counters, d_dom, d_found, d_failed, nullptr, nullptr,
-                             s));
+    NA_CK(dev::launch_search(g, d_desc, d_status, d_igroup, d_ientries, prm, d_counters, d_dom, d_found, d_failed,
+                             nullptr, nullptr, s));
     NA_CK(cudaMemcpyAsync(&st, d_status, sizeof(st), cudaMemcpyDeviceToHost, s));
     NA_CK(cudaStreamSynchronize(s));
     mn = UINT32_MAX;

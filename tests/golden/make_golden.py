@@ -180,9 +180,9 @@ def main(names: list[str]) -> None:
                 pats = ser
             else:
                 pats = par  # parallel prints multi-edge patterns only: add 1-edge ones from the port
-                port_out = tmp / "port.txt"
-                run([PORT, "-file", graph, "-freq", tau, "-maxNodes", mn, "-thread", os.cpu_count() or 4, "-out",
-                     port_out])
+                port_out = tmp / "port.txt"  # (mined to 2 vertices: the 1-edge patterns are all it gives)
+                run([PORT, "-file", graph, "-freq", tau, "-maxNodes", 2 if int(mn) < 0 else min(int(mn), 2), "-thread",
+                     os.cpu_count() or 4, "-out", port_out])
                 one_edge = sorted(k for k in read_results(port_out) if " " not in k)
                 pats = sorted(one_edge + par)
                 n_one_edge = len(one_edge)
