@@ -208,7 +208,8 @@ typedef struct {
                                is retried by a later pass with 8x the budgets (0: never split) */
     uint32_t split_slice;   /* adjacency positions per split task (>= 1) */
     uint32_t chunk_words;   /* 32-bit domain-bitmap words per search work item (>= 1) */
-    uint32_t refine_rounds; /* arc-consistency passes for patterns that need a search (>= 1) */
+    uint32_t refine_rounds; /* arc-consistency passes for patterns that need a search (0..32; 0: none,
+                               distinct-label trees still run to their fixpoint) */
     uint32_t max_batch;     /* tfsm_mine: most patterns per engine call (>= 1) */
     uint32_t hub_span;      /* a search whose first depth has more adjacency positions than this
                                (a hub vertex's label range) is split at once ... */

@@ -26,7 +26,7 @@ SPACE = [
     ("hub_parts", [4, 1, 2, 8]),  # teams that search one hub candidate's first depth together
     ("step_budget", [16, 8, 32, 64]),
     ("split_slice", [64, 32, 128]),
-    ("refine_rounds", [1, 2]),
+    ("refine_rounds", [1, 2, 0]),
 ]
 
 

@@ -42,14 +42,43 @@ namespace {
         if (e_ != cudaSuccess) throw EngineError(10, std::string(#x) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-// Device buffers released by the levels of one engine, handed to its later levels: a mining run
-// allocates each level's bitmap pools once instead of a cudaMalloc / cudaFree (which synchronises
-// the device) per engine call.  Shared by the levels, so it outlives the engine if they do.
+// Device buffers of the levels of one engine (bitmap pools, descriptors).  Blocks are carved from
+// slabs of at least 64 MiB and handed back to the cache when their level dies, for later levels:
+// a mining run calls cudaMalloc (which synchronises the device) once per slab instead of once per
+// pool of every engine call, although the calls of a growth level all keep their pools (they are
+// the next level's push-down sources).  Shared by the levels, so it outlives the engine if they do.
 struct BufferCache {
+    static constexpr size_t kSlab = 64u << 20;
     std::mutex mu;
-    std::multimap<size_t, void *> free;  // bytes -> buffer
+    std::multimap<size_t, void *> free;  // bytes -> block
+    std::vector<void *> slabs;
+    char *cur = nullptr;                 // unused tail of the newest slab
+    size_t left = 0;
     ~BufferCache() {
-        for (auto &kv : free) cudaFree(kv.second);
+        for (void *p : slabs) cudaFree(p);
+    }
+    // a new block of `bytes` (a multiple of 64 KiB keeps every block 64 KiB-aligned)
+    void *carve(size_t bytes) {
+        std::lock_guard<std::mutex> lk(mu);
+#if defined(TFSM_SIMT_EMULATION)  // one allocation per block: the sanitizers see each block's bounds
+        left = 0;
+#endif
+        if (bytes > left) {
+            void *p = nullptr;
+#if defined(TFSM_SIMT_EMULATION)
+            const size_t sz = bytes;
+#else
+            const size_t sz = std::max(bytes, kSlab);
+#endif
+            TFSM_CK(cudaMalloc(&p, sz));
+            slabs.push_back(p);
+            cur = static_cast<char *>(p);
+            left = sz;
+        }
+        void *q = cur;
+        cur += bytes;
+        left -= bytes;
+        return q;
     }
     void *take(size_t bytes, size_t &got) {  // best fit, at most twice the size asked for
         std::lock_guard<std::mutex> lk(mu);
@@ -107,13 +136,74 @@ struct DevBuf {
         release();
         size_t got = 0;
         void *q = cache ? cache->take(want, got) : nullptr;
-        if (!q) {
+        if (!q && cache) {
+            q = cache->carve(want);
+            got = want;
+        } else if (!q) {
             TFSM_CK(cudaMalloc(&q, want));
             got = want;
         }
         p = static_cast<T *>(q);
         bytes = got;
         n = got / sizeof(T);
+    }
+};
+
+// Page-locked staging of a call's small host -> device copies (descriptors, source table, item
+// tables): a copy from it is an asynchronous DMA, where one from pageable memory waits for a staging
+// copy inside the driver.  A bump allocator, rewound at the start of each engine call (every call
+// ends with a synchronisation); when full, it synchronises the stream and starts over (growing if
+// one copy does not fit).
+struct Staging {
+    unsigned char *p = nullptr;
+    size_t cap = 0, used = 0;
+    Staging() = default;
+    Staging(const Staging &) = delete;
+    Staging &operator=(const Staging &) = delete;
+    ~Staging() {
+        if (p) cudaFreeHost(p);
+    }
+    void h2d(void *dst, const void *src, size_t bytes, cudaStream_t s) {
+        if (!bytes) return;
+        const size_t at = (used + 255) & ~(size_t)255;
+        if (at + bytes > cap) {
+            TFSM_CK(cudaStreamSynchronize(s));  // earlier copies out of the buffer are done
+            used = 0;
+            if (bytes > cap) {
+                if (p) cudaFreeHost(p);
+                p = nullptr;
+                cap = 0;
+                const size_t want = std::max<size_t>(bytes, 4u << 20);
+                TFSM_CK(cudaHostAlloc((void **)&p, want, cudaHostAllocDefault));
+                cap = want;
+            }
+            return h2d(dst, src, bytes, s);
+        }
+        std::memcpy(p + at, src, bytes);
+        TFSM_CK(cudaMemcpyAsync(dst, p + at, bytes, cudaMemcpyHostToDevice, s));
+        used = at + bytes;
+    }
+};
+
+// Page-locked landing buffer of device -> host reads (the batch's status records).
+template <class T>
+struct PinnedBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf &) = delete;
+    PinnedBuf &operator=(const PinnedBuf &) = delete;
+    ~PinnedBuf() {
+        if (p) cudaFreeHost(p);
+    }
+    void ensure(size_t k) {
+        if (k <= n && p) return;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        const size_t want = std::max<size_t>(k, 2 * n) + 16;
+        TFSM_CK(cudaHostAlloc((void **)&p, want * sizeof(T), cudaHostAllocDefault));
+        n = want;
     }
 };
 
@@ -211,6 +301,8 @@ struct GpuEngine::Impl {
     DevBuf<dev::SplitTask> splits;  // two buffers of split tasks (ping-pong between rounds)
     DevBuf<dev::SplitGroup> groups;
     std::vector<PatStatus> hstatus;
+    Staging stage;                     // this call's host -> device copies
+    PinnedBuf<PatStatus> status_land;  // status reads land here, then go to hstatus
     int device = 0;
     std::shared_ptr<BufferCache> cache = std::make_shared<BufferCache>();
     // also runs when a constructor throws after open()
@@ -610,14 +702,15 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     L.descs.ensure(P);
     I.status.ensure(P);
     I.hstatus.assign(P, PatStatus());
-    TFSM_CK(cudaMemcpyAsync(L.descs.p, L.hdescs.data(), P * sizeof(PatDesc), cudaMemcpyHostToDevice, I.stream));
+    I.status_land.ensure(P);
+    I.stage.used = 0;  // the previous call ended with a synchronisation
+    I.stage.h2d(L.descs.p, L.hdescs.data(), P * sizeof(PatDesc), I.stream);
     times_.h2d_bytes += P * sizeof(PatDesc);
     TFSM_CK(cudaMemsetAsync(I.status.p, 0, P * sizeof(PatStatus), I.stream));
 
     I.srcs.ensure(std::max<size_t>(1, srcs.size()));
     if (!srcs.empty()) {
-        TFSM_CK(cudaMemcpyAsync(I.srcs.p, srcs.data(), srcs.size() * sizeof(dev::SourceLevel), cudaMemcpyHostToDevice,
-                                I.stream));
+        I.stage.h2d(I.srcs.p, srcs.data(), srcs.size() * sizeof(dev::SourceLevel), I.stream);
         times_.h2d_bytes += srcs.size() * sizeof(dev::SourceLevel);
     }
 
@@ -638,24 +731,24 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         I.item_pu.ensure(item_pu.size());
         I.prefix.ensure(prefix.size());
         if (!item_pu.empty()) {
-            TFSM_CK(cudaMemcpyAsync(I.item_pu.p, item_pu.data(), item_pu.size() * 4, cudaMemcpyHostToDevice, I.stream));
-            TFSM_CK(cudaMemcpyAsync(I.prefix.p, prefix.data(), prefix.size() * 8, cudaMemcpyHostToDevice, I.stream));
+            I.stage.h2d(I.item_pu.p, item_pu.data(), item_pu.size() * 4, I.stream);
+            I.stage.h2d(I.prefix.p, prefix.data(), prefix.size() * 8, I.stream);
             times_.h2d_bytes += item_pu.size() * 4 + prefix.size() * 8;
         }
     };
-    auto read_status = [&]() {
-        TFSM_CK(cudaMemcpyAsync(I.hstatus.data(), I.status.p, P * sizeof(PatStatus), cudaMemcpyDeviceToHost,
+    // the batch's status records: DMA into page-locked memory, one synchronisation, then a copy
+    auto land_status = [&]() {
+        TFSM_CK(cudaMemcpyAsync(I.status_land.p, I.status.p, P * sizeof(PatStatus), cudaMemcpyDeviceToHost,
                                 I.stream));
         TFSM_CK(cudaStreamSynchronize(I.stream));
+        std::memcpy(I.hstatus.data(), I.status_land.p, P * sizeof(PatStatus));
         times_.d2h_bytes += P * sizeof(PatStatus);
     };
+    auto read_status = [&]() { land_status(); };
     // end of a timed phase followed by a status read: one host round trip for both
     auto time_and_read_status = [&]() -> double {
         TFSM_CK(cudaEventRecord(I.ev1, I.stream));
-        TFSM_CK(cudaMemcpyAsync(I.hstatus.data(), I.status.p, P * sizeof(PatStatus), cudaMemcpyDeviceToHost,
-                                I.stream));
-        TFSM_CK(cudaStreamSynchronize(I.stream));
-        times_.d2h_bytes += P * sizeof(PatStatus);
+        land_status();
         float ms = 0;
         TFSM_CK(cudaEventElapsedTime(&ms, I.ev0, I.ev1));
         return ms;
@@ -668,7 +761,9 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     std::vector<char> active(P, 0);
     for (size_t p = 0; p < P; ++p) active[p] = !trivial[p];
     build_items(active);
-    const int fixed_refine = (int)std::min<uint32_t>(std::max<uint32_t>(1, opt.refine_rounds), 32);
+    // refine_rounds 0: no arc consistency before the search (express patterns still run to their
+    // fixpoint below: their domains are their result)
+    const int fixed_refine = (int)std::min<uint32_t>(opt.refine_rounds, 32);
     if (!item_pu.empty()) {
         const uint32_t n_it = (uint32_t)item_pu.size();
         const uint64_t words = prefix.back();
@@ -710,7 +805,8 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     int last_round = fixed_refine - 1;
     for (int round = fixed_refine; round < 32; ++round) {
         for (size_t p = 0; p < P; ++p)
-            active[p] = !trivial[p] && express[p] && viable(p) && ((I.hstatus[p].changed >> (round - 1)) & 1u);
+            active[p] = !trivial[p] && express[p] && viable(p) &&
+                        (round == 0 || ((I.hstatus[p].changed >> (round - 1)) & 1u));
         if (std::find(active.begin(), active.end(), 1) == active.end()) break;
         build_items(active);
         TFSM_CK(cudaEventRecord(I.ev0, I.stream));
@@ -824,7 +920,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         times_.order_ms +=
             std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_ord).count();
     }
-    TFSM_CK(cudaMemcpyAsync(L.descs.p, L.hdescs.data(), P * sizeof(PatDesc), cudaMemcpyHostToDevice, I.stream));
+    I.stage.h2d(L.descs.p, L.hdescs.data(), P * sizeof(PatDesc), I.stream);
     times_.h2d_bytes += P * sizeof(PatDesc);
 
     phase(3);
@@ -920,10 +1016,8 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     I.igroups.ensure(std::max<size_t>(1, igroups.size()));
     I.ientries.ensure(std::max<size_t>(1, ientries.size()));
     if (!igroups.empty()) {
-        TFSM_CK(cudaMemcpyAsync(I.igroups.p, igroups.data(), igroups.size() * sizeof(dev::ItemGroup),
-                                cudaMemcpyHostToDevice, I.stream));
-        TFSM_CK(cudaMemcpyAsync(I.ientries.p, ientries.data(), ientries.size() * sizeof(dev::ItemEntry),
-                                cudaMemcpyHostToDevice, I.stream));
+        I.stage.h2d(I.igroups.p, igroups.data(), igroups.size() * sizeof(dev::ItemGroup), I.stream);
+        I.stage.h2d(I.ientries.p, ientries.data(), ientries.size() * sizeof(dev::ItemEntry), I.stream);
     }
     times_.h2d_bytes += igroups.size() * sizeof(dev::ItemGroup) + ientries.size() * sizeof(dev::ItemEntry);
     dev::SearchParams prm;
@@ -997,9 +1091,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         if (hcnt[dev::kCntAbandoned] == 0) break;
     }
     TFSM_CK(cudaEventRecord(I.ev1, I.stream));
-    TFSM_CK(cudaMemcpyAsync(I.hstatus.data(), I.status.p, P * sizeof(PatStatus), cudaMemcpyDeviceToHost, I.stream));
-    TFSM_CK(cudaStreamSynchronize(I.stream));
-    times_.d2h_bytes += P * sizeof(PatStatus);
+    land_status();
     {
         float ms = 0;
         TFSM_CK(cudaEventElapsedTime(&ms, I.ev0, I.ev1));

@@ -58,7 +58,7 @@ def test_mining_plain_matches_reference(tfsm, graphs, case, tmp_path):
     assert st["engine_calls"] == st["evaluations"] - st["pruned"]  # one engine call per searched candidate
 
 
-SPLIT_OPTS = [dict(step_budget=1, split_slice=1),          # every search splits at its first step
+SPLIT_OPTS = [dict(step_budget=1, split_slice=1, refine_rounds=0),  # every search splits at its first step
               dict(step_budget=3, split_slice=32),
               dict(step_budget=16, hub_span=0, hub_parts=8, split_slice=1),  # first depths split at once
               dict(step_budget=0)]                                  # no splitting
@@ -190,7 +190,7 @@ def test_forced_splits_keep_exact_supports(tfsm, graphs):
     g = graphs(case)
     saved = g.options()
     try:
-        for opts in (dict(step_budget=1, split_slice=1, chunk_words=1),
+        for opts in (dict(step_budget=1, split_slice=1, chunk_words=1, refine_rounds=0),
                      dict(step_budget=2, split_slice=8, chunk_words=7, refine_rounds=1, hub_span=0, hub_parts=3)):
             g.set_options(**opts)
             res = g.evaluate([tfsm.parse_key(k) for k in keys], flags=tfsm.FLAG_EXACT)
