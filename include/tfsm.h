@@ -31,7 +31,7 @@ extern "C" {
 #define TFSM_ERR_CUDA 10      /* CUDA runtime error */
 #define TFSM_ERR_INTERNAL 11
 
-#define TFSM_MAX_PATTERN_VERTICES 16
+#define TFSM_MAX_PATTERN_VERTICES 32
 
 /* flags */
 #define TFSM_FLAG_EXACT 1u    /* exact MNI per vertex: no early exit at tau */

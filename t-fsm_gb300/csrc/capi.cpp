@@ -108,7 +108,7 @@ bool build_pattern(const tfsm_pattern *tp, tfsm::Pattern &p, std::string &why) {
                 return false;
             }
             if (fwd && n >= TFSM_MAX_PATTERN_VERTICES) {
-                why = "pattern has more than 16 vertices";
+                why = "pattern has more than 32 vertices";
                 return false;
             }
         }
@@ -375,7 +375,7 @@ int tfsm_evaluate_level(tfsm_graph *g, const tfsm_pattern *patterns, int32_t n, 
                 }
             }
             if (!ok) {
-                results[i].status = why.find("16 vertices") != std::string::npos ? TFSM_ERR_PATTERN : TFSM_ERR_ARG;
+                results[i].status = why.find("32 vertices") != std::string::npos ? TFSM_ERR_PATTERN : TFSM_ERR_ARG;
                 if (g_err.empty()) g_err = why;  // per-pattern errors are reported in results[i].status
                 continue;
             }

@@ -18,7 +18,12 @@
 namespace tfsm {
 namespace dev {
 
-constexpr int kMaxN = 16;          // pattern vertices supported by the device path
+constexpr int kMaxN = 32;          // pattern vertices supported by the device path (the reference's
+                                   //   MAX_PATTERN_SIZE, parallel/global.h:36)
+constexpr int kTaskMaxN = 16;      // largest pattern whose searches split into tasks (larger ones
+                                   //   finish each search in place)
+constexpr int kMaxNlf = 8;         // neighbour-label requirements kept per pattern vertex (any
+                                   //   subset is a sound filter)
 constexpr uint8_t kNoEdge = 0xff;  // edge-label matrix entry for "not adjacent"
 constexpr uint32_t kColPad = 128;  // padding entries after col (at least 4 x the widest team)
 
@@ -72,10 +77,11 @@ struct PatDesc {
                                         //   growth level: source reference of their bitmaps for
                                         //   u's image, or -1
     int32_t nlf_n[kMaxN];               // neighbour-label-frequency requirements of u
-    uint8_t nlf_lab[kMaxN][kMaxN];
-    uint8_t nlf_cnt[kMaxN][kMaxN];
+    uint8_t nlf_lab[kMaxN][kMaxNlf];
+    uint8_t nlf_cnt[kMaxN][kMaxNlf];
     uint8_t order[kMaxN][kMaxN];        // [start vertex][depth] -> pattern vertex
-    uint32_t bn[kMaxN][kMaxN];          // [start vertex][depth] -> backward-neighbour mask
+    // (the backward-neighbour mask of depth d, adj[order[d]] & {order[0..d-1]}, is derived on the
+    // device when a search loads its plan)
 };
 
 // Mutable per-pattern state, updated with atomics by the kernels.
@@ -188,7 +194,7 @@ struct SplitTask {
     uint32_t v;              // candidate of u: the search this task belongs to
     uint32_t lo, hi;         // anchor positions at `depth`
     uint32_t group;          // index of the group that decides v
-    uint32_t prefix[kMaxN];  // prefix[k] = data vertex of order[k], k < depth
+    uint32_t prefix[kTaskMaxN];  // prefix[k] = data vertex of order[k], k < depth
 };
 
 // All tasks of one (u, v) search; the last task to finish decides v when none found an embedding
@@ -244,6 +250,7 @@ struct SearchParams {
     uint32_t parts_log2;     // every item is claimed 2^parts_log2 times, claim k searching the bits b of
                              //    its words with b % 2^parts_log2 == k (small calls: more warps busy)
     uint32_t n_pats;         // patterns of the batch
+    uint32_t max_n;          // vertices of the batch's largest searched pattern (> kTaskMaxN: no splits)
     uint32_t n_groups;       // item groups (ItemGroup) of the call
     uint32_t chunk_words;    // bitmap words per item
     uint64_t words;          // size of each level bitmap pool (32-bit words)

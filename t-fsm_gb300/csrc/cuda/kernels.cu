@@ -335,10 +335,13 @@ struct Team {
     }
 };
 
-// Largest pattern a team of G lanes searches (its per-depth state is sized for it).
-template <int G>
-struct TeamMaxN {
-    static constexpr int value = G == 32 ? kMaxN : 8;
+// Block shape of a search kernel whose teams hold state for patterns of up to N vertices: the
+// 32-vertex state (about 11 KB per team) fits four whole-warp teams per block in static shared
+// memory; smaller states keep kSearchWarps warps.
+template <int N>
+struct SearchBlock {
+    static constexpr int warps = N > kTaskMaxN ? 4 : kSearchWarps;
+    static constexpr int min_blocks = N > kTaskMaxN ? 2 * kSearchMinBlocks : kSearchMinBlocks;
 };
 
 template <int N>
@@ -407,7 +410,9 @@ __device__ __forceinline__ void load_plan(const Team<G> &T, Plan<N> &P, const Pa
         P.lstart[i] = D.lstart[i];
         P.lend[i] = D.lstart[i] + D.lsize[i];
         P.orbit[i] = D.orbit_mask[i];
-        P.bn[i] = D.bn[u][i];
+        uint32_t before = 0;  // the pattern vertices matched before depth i
+        for (uint32_t k = 0; k < i; ++k) before |= 1u << D.order[u][k];
+        P.bn[i] = i < (uint32_t)D.n ? D.adj[D.order[u][i]] & before : 0u;
         P.order[i] = D.order[u][i];
         P.lab[i] = (uint8_t)D.lab[i];
     }
@@ -779,7 +784,7 @@ __device__ uint32_t emit_remainder(const Team<G> &T, const Plan<N> &P, const Sta
         task.lo = f + (k - acc) * slice;  // k - acc is 0 when compact
         task.hi = t - task.lo > slice ? task.lo + slice : t;
         task.group = group;
-        for (int q = 0; q < kMaxN; ++q) task.prefix[q] = q < j && q < N ? S.emb[P.order[q]] : 0u;
+        for (int q = 0; q < kTaskMaxN; ++q) task.prefix[q] = q < j && q < N ? S.emb[P.order[q]] : 0u;
         if (TFSM_IN(14, t0 + k, cap) && TFSM_IN(48, task.hi, m2 + 1)) out[t0 + k] = task;
     }
     return total;
@@ -857,8 +862,11 @@ __device__ __forceinline__ bool pattern_stops(const Team<G> &T, const PatStatus 
 // claims its own items.  Outside the last pass, a search whose remainder finds no room is set aside
 // (neither found nor failed), and a team starts no more searches once the first round's share of
 // the buffer is full: the next pass, with larger budgets, takes up what is left.
-template <int G>
-__global__ void __launch_bounds__(kSearchWarps * 32, kSearchMinBlocks) k_search(Graph g, const PatDesc *__restrict__ descs,
+// Instances: teams of 8 lanes for patterns of at most 8 vertices, whole warps for at most 16, and
+// whole warps for at most 32 (these searches never split: split tasks hold 16-vertex prefixes).
+template <int G, int N>
+__global__ void __launch_bounds__(SearchBlock<N>::warps * 32, SearchBlock<N>::min_blocks)
+    k_search(Graph g, const PatDesc *__restrict__ descs,
                                                               PatStatus *__restrict__ st,
                                                               const ItemGroup *__restrict__ igroups,
                                                               const ItemEntry *__restrict__ ientries, SearchParams prm,
@@ -868,8 +876,8 @@ __global__ void __launch_bounds__(kSearchWarps * 32, kSearchMinBlocks) k_search(
                                                               uint32_t *__restrict__ failed,
                                                               SplitTask *__restrict__ splits,
                                                               SplitGroup *__restrict__ groups) {
-    constexpr int N = TeamMaxN<G>::value;
-    constexpr int kTeams = kSearchWarps * 32 / G;
+    constexpr int kTeams = SearchBlock<N>::warps * 32 / G;
+    constexpr bool kSplits = N <= kTaskMaxN;
     __shared__ Plan<N> plans[kTeams];
     __shared__ State<N> states[kTeams];
     __shared__ Tile<G> tiles[kTeams];
@@ -880,8 +888,9 @@ __global__ void __launch_bounds__(kSearchWarps * 32, kSearchMinBlocks) k_search(
     if (T.lane == 0) P.key = 0xffffffffu;
     T.sync();
     const bool exact = prm.exact != 0;
-    const uint32_t budget = prm.split ? prm.step_budget : 0u;
-    const uint32_t hub_span = prm.split && prm.hub_parts > 1 ? prm.hub_span : 0u;
+    // without a budget or a hub span no search aborts, so no split task is ever written
+    const uint32_t budget = kSplits && prm.split ? prm.step_budget : 0u;
+    const uint32_t hub_span = kSplits && prm.split && prm.hub_parts > 1 ? prm.hub_span : 0u;
     for (;;) {
         uint32_t it = 0;
         if (T.lane == 0) it = atomicAdd(&counters[0], 1u);
@@ -994,8 +1003,9 @@ __global__ void __launch_bounds__(kSearchWarps * 32, kSearchMinBlocks) k_search(
 // unexplored remainder into `out` for the next round, inside the same group.  Outside the last
 // pass, a remainder without room is set aside (the group is marked incomplete, so v stays
 // undecided for the next pass).
-template <int G>
-__global__ void __launch_bounds__(kSearchWarps * 32, kSearchMinBlocks) k_split(Graph g, const PatDesc *__restrict__ descs,
+template <int G, int N>
+__global__ void __launch_bounds__(SearchBlock<N>::warps * 32, SearchBlock<N>::min_blocks)
+    k_split(Graph g, const PatDesc *__restrict__ descs,
                                                              PatStatus *__restrict__ st, SearchParams prm,
                                                              uint32_t *__restrict__ counters, int round,
                                                              uint32_t budget, const uint32_t *__restrict__ dom,
@@ -1004,8 +1014,8 @@ __global__ void __launch_bounds__(kSearchWarps * 32, kSearchMinBlocks) k_split(G
                                                              const SplitTask *__restrict__ in,
                                                              SplitTask *__restrict__ out,
                                                              SplitGroup *__restrict__ groups) {
-    constexpr int N = TeamMaxN<G>::value;
-    constexpr int kTeams = kSearchWarps * 32 / G;
+    static_assert(N <= kTaskMaxN, "split tasks hold prefixes of at most kTaskMaxN vertices");
+    constexpr int kTeams = SearchBlock<N>::warps * 32 / G;
     __shared__ Plan<N> plans[kTeams];
     __shared__ State<N> states[kTeams];
     __shared__ Tile<G> tiles[kTeams];
@@ -1155,32 +1165,34 @@ cudaError_t launch_refine(const Graph &g, const PatDesc *descs, PatStatus *st, c
 
 namespace {
 
-template <int G>
+template <int G, int N>
 cudaError_t launch_search_t(const Graph &g, const PatDesc *descs, PatStatus *st, const ItemGroup *igroups,
                             const ItemEntry *ientries, const SearchParams &prm, uint32_t *counters,
                             const uint32_t *dom, uint32_t *found, uint32_t *failed, SplitTask *splits,
                             SplitGroup *groups, cudaStream_t s) {
+    constexpr int kThreads = SearchBlock<N>::warps * 32;
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<G>, kSearchWarps * 32, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<G, N>, kThreads, 0);
     if (per_sm <= 0) per_sm = 1;
     uint64_t blocks = (uint64_t)num_sms() * (uint64_t)per_sm;
-    const uint64_t teams = (uint64_t)kSearchWarps * 32 / G;
+    const uint64_t teams = (uint64_t)kThreads / G;
     const uint64_t need = (((uint64_t)prm.n_items << prm.parts_log2) + teams - 1) / teams;
     if (blocks > need) blocks = need;
-    TFSM_LAUNCH(k_search<G>, (unsigned)blocks, kSearchWarps * 32, s, g, descs, st, igroups, ientries, prm, counters,
-                dom, found, failed, splits, groups);
+    TFSM_LAUNCH((k_search<G, N>), (unsigned)blocks, kThreads, s, g, descs, st, igroups, ientries, prm, counters, dom,
+                found, failed, splits, groups);
     return cudaGetLastError();
 }
 
-template <int G>
+template <int G, int N>
 cudaError_t launch_split_t(const Graph &g, const PatDesc *descs, PatStatus *st, const SearchParams &prm,
                            uint32_t *counters, int round, uint32_t budget, const uint32_t *dom, uint32_t *found,
                            uint32_t *failed, const SplitTask *in, SplitTask *out, SplitGroup *groups,
                            cudaStream_t s) {
+    constexpr int kThreads = SearchBlock<N>::warps * 32;
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_split<G>, kSearchWarps * 32, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_split<G, N>, kThreads, 0);
     if (per_sm <= 0) per_sm = 1;
-    TFSM_LAUNCH(k_split<G>, (unsigned)(num_sms() * per_sm), kSearchWarps * 32, s, g, descs, st, prm, counters, round,
+    TFSM_LAUNCH((k_split<G, N>), (unsigned)(num_sms() * per_sm), kThreads, s, g, descs, st, prm, counters, round,
                 budget, dom, found, failed, in, out, groups);
     return cudaGetLastError();
 }
@@ -1194,11 +1206,18 @@ cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, c
     if (prm.n_groups == 0 || prm.chunk_words == 0 || !igroups || !ientries) return cudaErrorInvalidValue;
     if (prm.split && (!splits || !groups || prm.split_cap == 0 || prm.group_cap == 0 || prm.split_slice == 0))
         return cudaErrorInvalidValue;
+    if (prm.max_n > (uint32_t)kMaxN || (prm.team_lanes == 8 && prm.max_n > 8)) return cudaErrorInvalidValue;
+    if (prm.split && prm.max_n > (uint32_t)kTaskMaxN) return cudaErrorInvalidValue;
     cudaError_t e;
     if (prm.team_lanes == 8)
-        e = launch_search_t<8>(g, descs, st, igroups, ientries, prm, counters, dom, found, failed, splits, groups, s);
+        e = launch_search_t<8, 8>(g, descs, st, igroups, ientries, prm, counters, dom, found, failed, splits, groups,
+                                  s);
+    else if (prm.team_lanes == 32 && prm.max_n <= (uint32_t)kTaskMaxN)
+        e = launch_search_t<32, kTaskMaxN>(g, descs, st, igroups, ientries, prm, counters, dom, found, failed, splits,
+                                           groups, s);
     else if (prm.team_lanes == 32)
-        e = launch_search_t<32>(g, descs, st, igroups, ientries, prm, counters, dom, found, failed, splits, groups, s);
+        e = launch_search_t<32, kMaxN>(g, descs, st, igroups, ientries, prm, counters, dom, found, failed, splits,
+                                       groups, s);
     else return cudaErrorInvalidValue;
 #ifdef TFSM_BOUNDS_CHECK
     if (e == cudaSuccess && cudaStreamSynchronize(s) != cudaSuccess) {
@@ -1211,7 +1230,7 @@ cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, c
 
 uint32_t resident_search_warps() {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<32>, kSearchWarps * 32, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<32, kTaskMaxN>, kSearchWarps * 32, 0);
     if (per_sm <= 0) per_sm = 1;
     return (uint32_t)(num_sms() * per_sm * kSearchWarps);
 }
@@ -1223,11 +1242,13 @@ cudaError_t launch_split_round(const Graph &g, const PatDesc *descs, PatStatus *
     const SplitTask *in = splits + (size_t)(round % 2) * prm.split_cap;
     SplitTask *out = splits + (size_t)((round + 1) % 2) * prm.split_cap;
     if (round + 1 == kMaxRounds) budget = 0;  // the last possible round completes every task
+    if (prm.max_n > (uint32_t)kTaskMaxN || (prm.team_lanes == 8 && prm.max_n > 8)) return cudaErrorInvalidValue;
     cudaError_t e;
     if (prm.team_lanes == 8)
-        e = launch_split_t<8>(g, descs, st, prm, counters, round, budget, dom, found, failed, in, out, groups, s);
+        e = launch_split_t<8, 8>(g, descs, st, prm, counters, round, budget, dom, found, failed, in, out, groups, s);
     else if (prm.team_lanes == 32)
-        e = launch_split_t<32>(g, descs, st, prm, counters, round, budget, dom, found, failed, in, out, groups, s);
+        e = launch_split_t<32, kTaskMaxN>(g, descs, st, prm, counters, round, budget, dom, found, failed, in, out,
+                                          groups, s);
     else return cudaErrorInvalidValue;
 #ifdef TFSM_BOUNDS_CHECK
     if (e == cudaSuccess && cudaStreamSynchronize(s) != cudaSuccess) {

@@ -632,7 +632,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         PatDesc &D = L.hdescs[p];
         std::memset(&D, 0, sizeof(D));
         const int n = pat.size();
-        if (n > dev::kMaxN) throw EngineError(4, "pattern has more than 16 vertices");
+        if (n > dev::kMaxN) throw EngineError(4, "pattern has more than 32 vertices");
         D.n = n;
         res[p].mni.assign((size_t)n, 0);
         std::memset(D.el, dev::kNoEdge, sizeof(D.el));
@@ -650,7 +650,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
             std::map<int, int> need;
             for (auto &e : pat.vertices[u].edges) need[dense_label(pat.label(e.to))]++;
             for (auto &kv : need) {
-                if (kv.first < 0) continue;
+                if (kv.first < 0 || D.nlf_n[u] == dev::kMaxNlf) continue;
                 D.nlf_lab[u][D.nlf_n[u]] = (uint8_t)kv.first;
                 D.nlf_cnt[u][D.nlf_n[u]] = (uint8_t)std::min(kv.second, 255);
                 D.nlf_n[u]++;
@@ -851,7 +851,10 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         need_search[p] = 1;
         any_search = true;
         for (int u = 0; u < D.n; ++u)
-            if (D.rep[u] == u) gql_plan(*pats[p], s.dom_size, u, D.order[u], D.bn[u]);
+            if (D.rep[u] == u) {
+                uint32_t bn[dev::kMaxN];
+                gql_plan(*pats[p], s.dom_size, u, D.order[u], bn);
+            }
     }
     if (!any_search) return;
 
@@ -866,10 +869,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         const auto t_ord = std::chrono::steady_clock::now();
         std::mt19937_64 rng(opt.order_seed * 0x9E3779B97F4A7C15ull + times_.search_calls + 1);
         auto set_order = [](PatDesc &D, int u, const costmodel::Order &o) {
-            for (int i = 0; i < D.n; ++i) {
-                D.order[u][i] = o[(size_t)i];
-                D.bn[u][i] = costmodel::backward_mask(D, o, i);
-            }
+            for (int i = 0; i < D.n; ++i) D.order[u][i] = o[(size_t)i];
         };
         std::vector<float> X;                                       // model inputs, all candidates
         std::vector<std::pair<size_t, size_t>> span;                // per planned entry: [first, count)
@@ -936,15 +936,13 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     // lanes per search: teams of 8 when asked for, when the call has several patterns to search
     // (single-pattern calls measured faster with whole warps) and every one fits a team's state
     uint32_t team_lanes = 32;
-    if (opt.search_lanes == 8) {
-        int max_n = 0, searched = 0;
-        for (size_t p = 0; p < P; ++p)
-            if (need_search[p]) {
-                max_n = std::max(max_n, L.hdescs[p].n);
-                ++searched;
-            }
-        if (max_n <= 8 && searched > 1) team_lanes = 8;
-    }
+    int max_n = 0, searched_pats = 0;
+    for (size_t p = 0; p < P; ++p)
+        if (need_search[p]) {
+            max_n = std::max(max_n, L.hdescs[p].n);
+            ++searched_pats;
+        }
+    if (opt.search_lanes == 8 && max_n <= 8 && searched_pats > 1) team_lanes = 8;
     const uint32_t cw = std::max<uint32_t>(1, opt.chunk_words);
     std::vector<dev::ItemGroup> igroups;
     std::vector<dev::ItemEntry> ientries;
@@ -1027,7 +1025,10 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     prm.n_items = (uint32_t)n_items;
     prm.n_groups = (uint32_t)igroups.size();
     prm.chunk_words = cw;
-    prm.split = opt.split && opt.step_budget ? 1 : 0;
+    // patterns of more than kTaskMaxN vertices finish every search in place (split tasks hold
+    // prefixes of at most kTaskMaxN vertices)
+    prm.split = opt.split && opt.step_budget && max_n <= dev::kTaskMaxN ? 1 : 0;
+    prm.max_n = (uint32_t)std::max(1, max_n);
     prm.split_slice = std::max<uint32_t>(1, opt.split_slice);
     prm.hub_span = opt.hub_span;
     prm.hub_parts = std::min<uint32_t>(std::max<uint32_t>(1, opt.hub_parts), 32);

@@ -110,7 +110,7 @@ struct LevelRef {
 constexpr int kMaxPushSources = 4;
 struct PushSource {
     LevelRef at;        // where its bitmaps are
-    int8_t vertex[16];  // per candidate vertex: the sub-pattern vertex it maps to, or -1
+    int8_t vertex[32];  // per candidate vertex: the sub-pattern vertex it maps to, or -1
 };
 
 class GpuEngine {

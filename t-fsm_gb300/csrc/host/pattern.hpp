@@ -414,7 +414,8 @@ inline void extend_pattern(const Pattern &p, const ExtendContext &ctx, std::vect
         child.push(c);
         if (!check_canonical || is_canonical(child)) out.push_back(std::move(child));
     };
-    const bool grow = ctx.max_nodes == -1 || p.size() < ctx.max_nodes;
+    // unbounded growth stops at the reference's MAX_PATTERN_SIZE
+    const bool grow = (ctx.max_nodes == -1 || p.size() < ctx.max_nodes) && p.size() < kMaxPatternVertices;
     // forward from the rightmost vertex
     if (grow) {
         for (int nl : ctx.nbrs(last_label))

@@ -30,9 +30,18 @@ struct SmallGraph {
     std::vector<std::array<int, 3>> edges;  // (a, b, edge label)
 };
 
-// Isomorphism-invariant key (bytes of int32 values).  With `order`, also the vertex at each
-// position of the canonical form: for two isomorphic graphs, order_a[i] <-> order_b[i] is an
-// isomorphism.
+// Orderings a canonical key may try; a graph that needs more gets no key (see canonical_key).
+constexpr uint64_t kMaxKeyOrderings = 50000;
+
+// Isomorphism-invariant key (bytes of int32 values).  Vertices are ranked by an invariant
+// (label, degree, sorted (edge label, neighbour label) pairs), the ranks are refined by the ranks
+// of the neighbours until stable (colour refinement: ranks are assigned by sorting signatures, so
+// isomorphic graphs get the same ranks), every ordering that keeps the rank order is tried, and the
+// smallest edge list wins.  With `order`, also the vertex at each position of the canonical form:
+// for two isomorphic graphs, order_a[i] <-> order_b[i] is an isomorphism.  A graph whose classes
+// of equal rank allow more than kMaxKeyOrderings orderings (long symmetric paths or cycles) gets
+// the empty key, which callers treat as unknown; whether a graph gets one depends only on its
+// isomorphism class.
 inline std::string canonical_key(const SmallGraph &g, std::vector<int> *order_out = nullptr) {
     const int n = (int)g.label.size();
     std::vector<std::vector<int>> inv((size_t)n);
@@ -53,16 +62,57 @@ inline std::string canonical_key(const SmallGraph &g, std::vector<int> *order_ou
             inv[(size_t)v].push_back(p.second);
         }
     }
+    // initial ranks from the invariants, then refinement by (rank, sorted (edge label, neighbour rank))
+    std::vector<int> rank((size_t)n);
+    auto rank_by = [&](const std::vector<std::vector<int>> &sig) {
+        std::vector<int> idx((size_t)n);
+        for (int v = 0; v < n; ++v) idx[(size_t)v] = v;
+        std::sort(idx.begin(), idx.end(), [&](int a, int b) { return sig[(size_t)a] < sig[(size_t)b]; });
+        int r = 0;
+        for (int i = 0; i < n; ++i) {
+            if (i > 0 && sig[(size_t)idx[(size_t)i]] != sig[(size_t)idx[(size_t)i - 1]]) ++r;
+            rank[(size_t)idx[(size_t)i]] = r;
+        }
+        return n ? r + 1 : 0;
+    };
+    int classes = rank_by(inv);
+    std::vector<std::vector<std::array<int, 2>>> adj((size_t)n);
+    for (auto &e : g.edges) {
+        adj[(size_t)e[0]].push_back({e[2], e[1]});
+        adj[(size_t)e[1]].push_back({e[2], e[0]});
+    }
+    for (int round = 0; round < n; ++round) {
+        std::vector<std::vector<int>> sig((size_t)n);
+        for (int v = 0; v < n; ++v) {
+            std::vector<std::pair<int, int>> ns;
+            for (auto &a : adj[(size_t)v]) ns.push_back({a[0], rank[(size_t)a[1]]});
+            std::sort(ns.begin(), ns.end());
+            sig[(size_t)v].push_back(rank[(size_t)v]);
+            for (auto &x : ns) {
+                sig[(size_t)v].push_back(x.first);
+                sig[(size_t)v].push_back(x.second);
+            }
+        }
+        const int before = classes;
+        classes = rank_by(sig);
+        if (classes == before) break;
+    }
     std::vector<int> order((size_t)n);
     for (int v = 0; v < n; ++v) order[(size_t)v] = v;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return inv[(size_t)a] < inv[(size_t)b]; });
-    // classes of equal invariants: [begin, end) ranges of `order`
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return rank[(size_t)a] < rank[(size_t)b]; });
+    // classes of equal rank: [begin, end) ranges of `order` (ascending vertex ids inside)
     std::vector<std::pair<int, int>> cls;
+    uint64_t orderings = 1;
     for (int i = 0; i < n;) {
         int j = i + 1;
-        while (j < n && inv[(size_t)order[(size_t)j]] == inv[(size_t)order[(size_t)i]]) ++j;
+        while (j < n && rank[(size_t)order[(size_t)j]] == rank[(size_t)order[(size_t)i]]) ++j;
         cls.push_back({i, j});
+        for (int f = 2; f <= j - i && orderings <= kMaxKeyOrderings; ++f) orderings *= (uint64_t)f;
         i = j;
+    }
+    if (orderings > kMaxKeyOrderings) {
+        if (order_out) order_out->clear();
+        return std::string();
     }
     std::vector<int> pos((size_t)n);
     std::vector<std::array<int, 3>> cur, best;
@@ -105,7 +155,8 @@ inline SmallGraph small_graph(const Pattern &p) {
 }
 
 // A connected sub-pattern of P with one edge less: its key and, for every vertex of P, the
-// position of its image in the sub-pattern's canonical order (-1 for the dropped vertex).
+// position of its image in the sub-pattern's canonical order (-1 for the dropped vertex; all -1
+// when the key is unknown, i.e. empty).
 struct SubPattern {
     std::string key;
     std::vector<int> pos_of;  // by P vertex
@@ -154,11 +205,13 @@ inline void one_edge_smaller(const Pattern &p, std::vector<SubPattern> &subs) {
         SubPattern sp;
         std::vector<int> order;
         sp.key = canonical_key(s, &order);
-        std::vector<int> pos_in_s((size_t)ns);
-        for (int i = 0; i < ns; ++i) pos_in_s[(size_t)order[(size_t)i]] = i;
         sp.pos_of.assign((size_t)n, -1);
-        for (int v = 0; v < n; ++v)
-            if (remap[(size_t)v] >= 0) sp.pos_of[(size_t)v] = pos_in_s[(size_t)remap[(size_t)v]];
+        if (!sp.key.empty()) {
+            std::vector<int> pos_in_s((size_t)ns);
+            for (int i = 0; i < ns; ++i) pos_in_s[(size_t)order[(size_t)i]] = i;
+            for (int v = 0; v < n; ++v)
+                if (remap[(size_t)v] >= 0) sp.pos_of[(size_t)v] = pos_in_s[(size_t)remap[(size_t)v]];
+        }
         subs.push_back(std::move(sp));
     }
 }

@@ -380,12 +380,16 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
             //   * one evaluated and infrequent: the child is infrequent (MNI is anti-monotone);
             //   * one missing from a complete level (single edge label): infrequent as well;
             //   * the frequent ones bound the child's domains (up to kMaxPushSources of them).
+            // An unknown (empty) key, of a pattern too symmetric for the key's search, decides nothing:
+            // such a sub-pattern neither prunes nor bounds the child (isomorphic patterns are all
+            // unknown, so no frequent pattern is missed).
             std::unordered_map<std::string, size_t> evaluated;
             for (size_t i = 0; i < level.size(); ++i)
-                if (!level[i].pruned) evaluated.emplace(growth->key(i), i);
+                if (!level[i].pruned && !growth->key(i).empty()) evaluated.emplace(growth->key(i), i);
             for (size_t i = 0; i < next.size(); ++i) {
                 Node &child = next[i];
                 for (const SubPattern &sp : growth->child_subs((size_t)parent_of[i], child_no[i])) {
+                    if (sp.key.empty()) continue;
                     auto it = evaluated.find(sp.key);
                     if (it == evaluated.end()) {
                         if (prune_subpatterns) child.pruned = true;
@@ -401,9 +405,9 @@ void mine(GpuEngine &eng, const LgGraph &g, const MineOptions &opt, std::vector<
                     if (child.push.size() >= (size_t)kMaxPushSources) continue;
                     PushSource src;
                     src.at = LevelRef{sn.lvl, sn.idx};
-                    for (int u = 0; u < 16; ++u) src.vertex[u] = -1;
+                    for (int u = 0; u < (int)sizeof(src.vertex); ++u) src.vertex[u] = -1;
                     const std::vector<int> &ord = growth->order(it->second);
-                    for (int u = 0; u < child.pat.size() && u < 16; ++u)
+                    for (int u = 0; u < child.pat.size() && u < (int)sizeof(src.vertex); ++u)
                         if (sp.pos_of[(size_t)u] >= 0) src.vertex[u] = (int8_t)ord[(size_t)sp.pos_of[(size_t)u]];
                     child.push.push_back(src);
                 }

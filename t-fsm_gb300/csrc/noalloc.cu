@@ -206,6 +206,7 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
             if (!((adj[u] >> w) & 1u)) continue;
             int k = 0;
             while (k < D.nlf_n[u] && D.nlf_lab[u][k] != (uint8_t)D.lab[w]) ++k;
+            if (k == dev::kMaxNlf) continue;  // requirements beyond the first kMaxNlf labels are dropped
             if (k == D.nlf_n[u]) {
                 D.nlf_lab[u][k] = (uint8_t)D.lab[w];
                 D.nlf_cnt[u][k] = 0;
@@ -304,7 +305,10 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
         return TFSM_OK;
     }
     // ---- search ----
-    for (int u = 0; u < n; ++u) plan_from(n, adj, deg, st.dom_size, u, D.order[u], D.bn[u]);
+    for (int u = 0; u < n; ++u) {
+        uint32_t bn[dev::kMaxN];
+        plan_from(n, adj, deg, st.dom_size, u, D.order[u], bn);
+    }
     NA_CK(cudaMemcpyAsync(d_desc, &D, sizeof(D), cudaMemcpyHostToDevice, s));
     // One item group over every vertex: their runs of words interleaved round by round, as the
     // engine interleaves its items (dev::item_at decodes them on the device).
@@ -340,6 +344,7 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     prm.exact = exact ? 1 : 0;
     prm.n_items = (uint32_t)n_items;
     prm.n_groups = 1;
+    prm.max_n = (uint32_t)n;
     prm.chunk_words = kChunkWords;
     prm.split = 0;  // no hub splitting on this path (its task buffers would need more scratch)
     prm.isect_ratio = 16;

@@ -23,7 +23,7 @@ TFSM_ERR_LIMIT = 5
 TFSM_ERR_NO_DEVICE = 9
 TFSM_ERR_CUDA = 10
 TFSM_ERR_INTERNAL = 11
-MAX_PATTERN_VERTICES = 16
+MAX_PATTERN_VERTICES = 32
 MAX_LEVELS = 32
 
 FLAG_EXACT = 1

@@ -67,6 +67,9 @@ FILE_CASES = {
     "no_edges": dict(file="graphs/no_edges.lg", tau=1, max_nodes=4, mni="all"),
     "no_frequent": dict(file="graphs/no_frequent.lg", tau=50, max_nodes=4, mni="all"),
     "tau1_small": dict(file="graphs/tau1_small.lg", tau=1, max_nodes=4, mni="all"),
+    # patterns of up to 23 vertices (maxNodes unbounded): three copies of a 22-vertex path with
+    # alternating labels and a chord closing a 4-cycle
+    "long_paths": dict(file="graphs/long_paths.lg", tau=3, max_nodes=-1, mni="all"),
 }
 
 

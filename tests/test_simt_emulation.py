@@ -47,6 +47,10 @@ OPTS = {"default": [],
 # (the quirk case's many-call variants are the slowest to emulate; its other variants cover it)
 RUNS = [(c, o) for c in SMALL for o in OPTS if not (o in ("plain", "batch3") and c == "quirk_elabels")]
 RUNS += [(c, "tiny_buffers") for c in ("clique", "star_hub", "quirk_elabels")]
+# patterns of up to 23 vertices: the whole-warp search with 32-vertex state (the emulated split
+# rounds of the smaller levels are slow, so these runs do not split)
+OPTS["no_split_exact"] = ["-no-split", "-exact"]
+RUNS += [("long_paths", o) for o in ("no_split", "no_split_exact")]
 # with TFSM_SPLIT_CAPACITY=5: claims straddle the end, searches are set aside and retried by later
 # passes, the last pass finishes them in place
 OPTS["tiny_buffers"] = OPTS["split"]
