@@ -227,9 +227,14 @@ def test_invalid_patterns_are_rejected(tfsm, graphs):
     ]
     res = g.evaluate(bad)
     assert all(r.status == tfsm.TFSM_ERR_ARG for r in res)
-    big = [(0, 1, 0, 1, 0)] + [(i, i + 1, 0, 1, 0) for i in range(1, 17)]
+    # 33 vertices: more than the reference's MAX_PATTERN_SIZE (32)
+    big = [(0, 1, 0, 1, 0)] + [(i, i + 1, 0, 1, 0) for i in range(1, 32)]
     r = g.evaluate([big])[0]
     assert r.status == tfsm.TFSM_ERR_PATTERN
+    # 18 vertices are evaluated (by the search instance with 32-vertex state; lazily: proving every
+    # candidate of an 18-vertex path exactly is exponential on this graph)
+    r = g.evaluate([big[:17]])[0]
+    assert r.status == 0 and len(r.mni) == 18 and r.frequent
     # valid patterns in the same batch are still evaluated
     mixed = g.evaluate([bad[0], [(0, 1, 0, 1, 0)]])
     assert mixed[0].status == tfsm.TFSM_ERR_ARG and mixed[1].status == 0
