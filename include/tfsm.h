@@ -231,6 +231,12 @@ typedef struct {
                                probed by binary search otherwise (>= 1; the reference switches at
                                50; the autotuner tries 4, 16, 64) */
     uint32_t reserved;      /* 0 */
+    /* fields added after the first versioned layout */
+    uint32_t refine_scope;  /* vertices of the first refinement rounds: 1 (default) for a pattern that
+                               starts from its parent's domains only the two vertices of its newest
+                               edge (the others were refined against the same edges in the parent's
+                               call), 0 every vertex; distinct-label trees always refine every vertex */
+    uint32_t reserved2;     /* 0 */
 } tfsm_options;
 
 #define TFSM_OPTIONS_MIN_SIZE 64u /* the first versioned layout: struct_size .. reserved */

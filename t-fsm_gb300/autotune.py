@@ -27,6 +27,7 @@ SPACE = [
     ("step_budget", [16, 8, 32, 64]),
     ("split_slice", [64, 32, 128]),
     ("refine_rounds", [1, 2, 0]),
+    ("refine_scope", [1, 0]),
 ]
 
 

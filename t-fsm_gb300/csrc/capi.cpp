@@ -130,12 +130,14 @@ void fill_result(const tfsm::EvalResult &r, int n, tfsm_result *out) {
 }
 
 const char *const kKnobRules =
-    "split_slice, chunk_words, max_batch and isect_ratio must be >= 1; refine_rounds <= 32; hub_parts in 1..32; "
+    "split_slice, chunk_words, max_batch and isect_ratio must be >= 1; refine_rounds <= 32; refine_scope 0 or 1; "
+    "hub_parts in 1..32; "
     "time_limit_s and call_ms >= 0; search_lanes 0, 8 or 32";
 
 bool knobs_valid(const tfsm_options &o) {
     return o.split_slice >= 1 && o.chunk_words >= 1 && o.refine_rounds <= 32 && o.max_batch >= 1 &&
            o.hub_parts >= 1 && o.hub_parts <= 32 && o.isect_ratio >= 1 && o.time_limit_s >= 0 && o.call_ms >= 0 &&
+           o.refine_scope <= 1 &&
            (o.search_lanes == 0 || o.search_lanes == 8 || o.search_lanes == 32);
 }
 
@@ -152,6 +154,7 @@ void apply_knobs(const tfsm_options &o, tfsm::EngineOptions &e) {
     e.rank_window = o.rank_window;
     e.call_ms = o.call_ms;
     e.isect_ratio = o.isect_ratio;
+    e.refine_scope = o.refine_scope;
 }
 
 // The engine's knobs as a full tfsm_options.
@@ -171,6 +174,7 @@ tfsm_options knobs_of(const tfsm::EngineOptions &e) {
     o.rank_window = e.rank_window;
     o.call_ms = e.call_ms;
     o.isect_ratio = e.isect_ratio;
+    o.refine_scope = e.refine_scope;
     return o;
 }
 

@@ -294,6 +294,8 @@ struct GpuEngine::Impl {
     DevBuf<PatStatus> status;
     DevBuf<uint32_t> item_pu;
     DevBuf<uint64_t> prefix;
+    DevBuf<uint32_t> ritem_pu;  // the first refinement rounds' (pattern, vertex) items
+    DevBuf<uint64_t> rprefix;
     DevBuf<dev::ItemGroup> igroups;    // the call's search work (dev::item_at)
     DevBuf<dev::ItemEntry> ientries;
     DevBuf<dev::SourceLevel> srcs;      // the earlier calls' pools read by this call's domain init
@@ -760,6 +762,32 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     // the previous round left unchanged.
     std::vector<char> active(P, 0);
     for (size_t p = 0; p < P; ++p) active[p] = !trivial[p];
+    // the first refinement rounds: every vertex, or (scoped) for a pattern that starts from its
+    // parent's final domains only the two vertices of its newest edge (the rest were refined against
+    // the same edges in the parent's call); express patterns always refine every vertex
+    std::vector<uint32_t> ritem_pu;
+    std::vector<uint64_t> rprefix(1, 0);
+    {
+        const bool scoped = opt.refine_scope != 0;
+        for (size_t p = 0; p < P; ++p) {
+            if (!active[p]) continue;
+            const PatDesc &D = L.hdescs[p];
+            const bool has_parent = p < parent.size() && parent[p].lvl != nullptr;
+            const DfsCode &last = pats[p]->codes.back();
+            for (int u = 0; u < D.n; ++u) {
+                if (scoped && has_parent && !express[p] && u != last.from && u != last.to) continue;
+                ritem_pu.push_back(((uint32_t)p << 8) | (uint32_t)u);
+                rprefix.push_back(rprefix.back() + D.words[u]);
+            }
+        }
+        I.ritem_pu.ensure(std::max<size_t>(1, ritem_pu.size()));
+        I.rprefix.ensure(rprefix.size());
+        if (!ritem_pu.empty()) {
+            I.stage.h2d(I.ritem_pu.p, ritem_pu.data(), ritem_pu.size() * 4, I.stream);
+            I.stage.h2d(I.rprefix.p, rprefix.data(), rprefix.size() * 8, I.stream);
+            times_.h2d_bytes += ritem_pu.size() * 4 + rprefix.size() * 8;
+        }
+    }
     build_items(active);
     // refine_rounds 0: no arc consistency before the search (express patterns still run to their
     // fixpoint below: their domains are their result)
@@ -767,6 +795,8 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     if (!item_pu.empty()) {
         const uint32_t n_it = (uint32_t)item_pu.size();
         const uint64_t words = prefix.back();
+        const uint32_t n_rit = (uint32_t)ritem_pu.size();
+        const uint64_t rwords = rprefix.back();
         run_captured(I.stream, I.exec_init, [&]() {
             TFSM_CK(record_in_sequence(I.ev0, I.stream));
             TFSM_CK(dev::launch_domain_init(I.g, L.descs.p, I.status.p, I.item_pu.p, I.prefix.p, n_it, words, L.dom.p,
@@ -774,8 +804,8 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
                                             I.stream));
             TFSM_CK(record_in_sequence(I.ev_mid, I.stream));
             for (int r = 0; r < fixed_refine; ++r)
-                TFSM_CK(dev::launch_refine(I.g, L.descs.p, I.status.p, I.item_pu.p, I.prefix.p, n_it, words, L.dom.p,
-                                           total, r, tau, opt.exact, I.stream));
+                TFSM_CK(dev::launch_refine(I.g, L.descs.p, I.status.p, I.ritem_pu.p, I.rprefix.p, n_rit, rwords,
+                                           L.dom.p, total, r, tau, opt.exact, I.stream));
             TFSM_CK(record_in_sequence(I.ev1, I.stream));
         });
         read_status();
@@ -787,7 +817,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         times_.init_launches++;
         times_.init_words += words;
         times_.refine_launches += (uint64_t)fixed_refine;
-        times_.refine_words += words * (uint64_t)fixed_refine;
+        times_.refine_words += rwords * (uint64_t)fixed_refine;
     } else {
         read_status();
     }

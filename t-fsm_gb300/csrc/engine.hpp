@@ -53,6 +53,8 @@ struct EngineOptions {
     uint32_t search_lanes = 8;         // lanes per search: 32, or 8 (four searches per warp, used for
                                        //   calls with several patterns of at most 8 vertices)
     uint32_t refine_rounds = 1;        // arc-consistency passes for patterns that need search (0: none)
+    uint32_t refine_scope = 1;         // 1: a child's first refinement rounds cover its newest edge's two
+                                       //   vertices only (the rest were refined in its parent's call); 0: all
     uint32_t rank_window = 0;          // patterns per window of the vertex-major item order (0: all)
     uint32_t max_batch = 4096;         // miner: patterns per engine call
     double call_ms = 2;                // miner: engine-call time (ms) above which later calls take

@@ -1,7 +1,7 @@
 // `run`: command-line drop-in for the reference miners (parallel/run.cpp:11-82, serial/run.cpp).
 //
 //   run -file G.lg -freq TAU [-thread T] [-maxNodes N] [-plain] [-exact] [-out PATH]
-//       [-step-budget B] [-split-slice S] [-chunk-words W] [-refine-rounds R] [-max-batch M]
+//       [-step-budget B] [-split-slice S] [-chunk-words W] [-refine-rounds R] [-refine-scope 0|1] [-max-batch M]
 //       [-hub-span S] [-hub-parts K] [-isect-ratio R] [-search-lanes L] [-rank-window W] [-call-ms MS]
 //       [-no-split] [-time-limit SECONDS] [-random-orders SEED] [-no-prune]
 //
@@ -57,6 +57,7 @@ int main(int argc, char **argv) {
     if (opt(argc, argv, "-split-slice")) o.split_slice = (uint32_t)std::atoi(opt(argc, argv, "-split-slice"));
     if (opt(argc, argv, "-chunk-words")) o.chunk_words = (uint32_t)std::atoi(opt(argc, argv, "-chunk-words"));
     if (opt(argc, argv, "-refine-rounds")) o.refine_rounds = (uint32_t)std::atoi(opt(argc, argv, "-refine-rounds"));
+    if (opt(argc, argv, "-refine-scope")) o.refine_scope = (uint32_t)std::atoi(opt(argc, argv, "-refine-scope"));
     if (opt(argc, argv, "-max-batch")) o.max_batch = (uint32_t)std::atoi(opt(argc, argv, "-max-batch"));
     if (opt(argc, argv, "-hub-span")) o.hub_span = (uint32_t)std::atoi(opt(argc, argv, "-hub-span"));
     if (opt(argc, argv, "-hub-parts")) o.hub_parts = (uint32_t)std::atoi(opt(argc, argv, "-hub-parts"));

@@ -112,7 +112,8 @@ class OptionsC(C.Structure):
                 ("chunk_words", C.c_uint32), ("refine_rounds", C.c_uint32), ("max_batch", C.c_uint32),
                 ("hub_span", C.c_uint32), ("hub_parts", C.c_uint32), ("time_limit_s", C.c_double),
                 ("search_lanes", C.c_uint32), ("rank_window", C.c_uint32), ("call_ms", C.c_double),
-                ("isect_ratio", C.c_uint32), ("reserved", C.c_uint32)]
+                ("isect_ratio", C.c_uint32), ("reserved", C.c_uint32), ("refine_scope", C.c_uint32),
+                ("reserved2", C.c_uint32)]
 
     def __init__(self, **kw):
         super().__init__(**kw)
@@ -358,7 +359,7 @@ class Graph:
     def options(self) -> dict:
         o = OptionsC()
         _check(lib().tfsm_get_options(self._h, C.byref(o)))
-        return {f: getattr(o, f) for f, _ in OptionsC._fields_ if f not in ("struct_size", "reserved")}
+        return {f: getattr(o, f) for f, _ in OptionsC._fields_ if f not in ("struct_size", "reserved", "reserved2")}
 
     def set_options(self, **kw) -> None:
         cur = self.options()

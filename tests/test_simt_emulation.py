@@ -36,6 +36,7 @@ OPTS = {"default": [],
         "merge_all": ["-isect-ratio", "1000000", "-step-budget", "2"],
         "probe_all": ["-isect-ratio", "1"],
         "no_refine": ["-refine-rounds", "0"],
+        "refine_all": ["-refine-scope", "0", "-refine-rounds", "2"],
         "plain": ["-plain", "-refine-rounds", "1"], "exact": ["-exact"], "batch3": ["-max-batch", "3"],
         "random_orders": ["-random-orders", "7", "-step-budget", "2"],
         "lanes8": ["-search-lanes", "8"],
