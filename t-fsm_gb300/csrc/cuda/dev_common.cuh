@@ -76,6 +76,9 @@ struct PatDesc {
     int64_t push_off[kMaxPush][kMaxN];  // further sub-patterns (one edge less) of the previous
                                         //   growth level: source reference of their bitmaps for
                                         //   u's image, or -1
+    uint32_t filter_mask;               // bit u: domain init tests u's degree and neighbour labels (clear
+                                        //   when u's parent domain passed the same test: same degree and
+                                        //   neighbour-label requirements in the parent)
     int32_t nlf_n[kMaxN];               // neighbour-label-frequency requirements of u
     uint8_t nlf_lab[kMaxN][kMaxNlf];
     uint8_t nlf_cnt[kMaxN][kMaxNlf];

@@ -152,7 +152,8 @@ __global__ void __launch_bounds__(256) k_domain_init(Graph g, const PatDesc *__r
         if (D.parent_off[u] >= 0) pass = pass && source_bit(srcs, n_srcs, D.parent_off[u], word, lane);
         for (int k = 0; k < kMaxPush; ++k)
             if (D.push_off[k][u] >= 0) pass = pass && source_bit(srcs, n_srcs, D.push_off[k][u], word, lane);
-        if (__any_sync(0xffffffffu, pass)) {
+        // (u is the same for the whole warp, so the test is skipped or run by all lanes)
+        if (((D.filter_mask >> u) & 1u) && __any_sync(0xffffffffu, pass)) {
             const uint32_t x = D.lstart[u] + xl;
             uint32_t b = 0, e = 0;
             if (pass && !TFSM_IN(33, x, g.n)) pass = false;

@@ -685,6 +685,20 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
                 k += any ? 1 : 0;
             }
         }
+        // Domain init tests degree and neighbour labels of u unless u starts from a parent domain
+        // that passed the same test (same degree, same requirements): a child's vertices away from
+        // its newest edge.
+        D.filter_mask = 0;
+        {
+            const PatDesc *PD = p < parent.size() ? source(parent[p]) : nullptr;
+            for (int u = 0; u < n; ++u) {
+                bool same = PD && u < PD->n && D.parent_off[u] >= 0 && PD->deg[u] == D.deg[u] &&
+                            PD->nlf_n[u] == D.nlf_n[u];
+                for (int k = 0; same && k < D.nlf_n[u]; ++k)
+                    same = PD->nlf_lab[u][k] == D.nlf_lab[u][k] && PD->nlf_cnt[u][k] == D.nlf_cnt[u][k];
+                if (!same) D.filter_mask |= 1u << u;
+            }
+        }
         const std::vector<int> orb = automorphism_orbits(pat);
         for (int u = 0; u < n; ++u) {
             D.rep[u] = orb[u];

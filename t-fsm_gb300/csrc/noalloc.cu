@@ -172,6 +172,7 @@ int noalloc_evaluate(const GpuEngine &eng, const tfsm_pattern *tp, uint32_t tau,
     std::memset(D.el, dev::kNoEdge, sizeof(D.el));
     D.n = n;
     D.n_reps = n;
+    D.filter_mask = 0xffffffffu;  // no parent: every vertex is tested
     bool trivial = false, distinct = true;
     uint64_t words = 0;
     for (int u = 0; u < n; ++u) {
