@@ -78,7 +78,8 @@ struct PatDesc {
                                         //   u's image, or -1
     uint32_t filter_mask;               // bit u: domain init tests u's degree and neighbour labels (clear
                                         //   when u's parent domain passed the same test: same degree and
-                                        //   neighbour-label requirements in the parent)
+                                        //   neighbour-label requirements in the parent); the engine then
+                                        //   gives u a wide domain-init item (kWideItem)
     int32_t nlf_n[kMaxN];               // neighbour-label-frequency requirements of u
     uint8_t nlf_lab[kMaxN][kMaxNlf];
     uint8_t nlf_cnt[kMaxN][kMaxNlf];
@@ -106,6 +107,10 @@ struct PatStatus {
 };
 
 enum : uint32_t { kRunning = 0, kFrequent = 1, kInfrequent = 2 };
+
+// Domain-init items are (pattern << 8 | vertex); a wide one (this bit set) covers 32 bitmap words
+// per unit, one lane per word, for a vertex whose words are only its sources' words ANDed.
+constexpr uint32_t kWideItem = 0x80000000u;
 
 // Work item of the search kernel: a run of bitmap words of one representative's domain.
 struct SearchItem {

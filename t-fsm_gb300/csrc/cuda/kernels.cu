@@ -126,6 +126,17 @@ __device__ __forceinline__ bool source_bit(const SourceLevel *__restrict__ srcs,
     return (w >> lane) & 1u;
 }
 
+// Word `word` of a source's final domain (all ones when it cannot be read, as above).
+__device__ __forceinline__ uint32_t source_word(const SourceLevel *__restrict__ srcs, uint32_t n_srcs, int64_t ref,
+                                                uint32_t word) {
+    const uint64_t slot = (uint64_t)ref >> kSrcShift;
+    const uint64_t o = ((uint64_t)ref & kSrcMask) + word;
+    if (!TFSM_IN(32, slot, n_srcs) || slot >= n_srcs) return 0xffffffffu;
+    const SourceLevel S = srcs[slot];
+    if (!TFSM_IN(39, o, S.words) || o >= S.words) return 0xffffffffu;
+    return __ldg(S.dom + o) & ~__ldg(S.failed + o);
+}
+
 __global__ void __launch_bounds__(256) k_domain_init(Graph g, const PatDesc *__restrict__ descs,
                                                      PatStatus *__restrict__ st, const uint32_t *__restrict__ item_pu,
                                                      const uint64_t *__restrict__ prefix, uint32_t n_items,
@@ -141,8 +152,29 @@ __global__ void __launch_bounds__(256) k_domain_init(Graph g, const PatDesc *__r
     for (uint64_t gw = warp; gw < total; gw += nwarps) {
         item = find_item(prefix, n_items, gw, item);
         const uint32_t pu = item_pu[item];
-        const uint32_t p = pu >> 8, u = pu & 0xff;
+        const uint32_t p = (pu & ~kWideItem) >> 8, u = pu & 0xff;
         const PatDesc &D = descs[p];
+        if (pu & kWideItem) {
+            // u skips the degree / neighbour-label test: its words are only the sources' words
+            // ANDed, 32 words per warp, one lane per word
+            const uint32_t word = (uint32_t)(gw - prefix[item]) * 32 + lane;
+            const bool ok = word < D.words[u] && TFSM_IN(31, D.off[u] + word, chk_words);
+            uint32_t w = 0;
+            if (ok) {
+                const uint32_t first = word * 32;
+                w = D.lsize[u] - first >= 32 ? 0xffffffffu : (1u << (D.lsize[u] - first)) - 1u;
+                if (D.parent_off[u] >= 0) w &= source_word(srcs, n_srcs, D.parent_off[u], word);
+                for (int k = 0; k < kMaxPush; ++k)
+                    if (D.push_off[k][u] >= 0) w &= source_word(srcs, n_srcs, D.push_off[k][u], word);
+                const uint64_t o = D.off[u] + word;
+                dom[o] = w;
+                found[o] = 0;
+                failed[o] = 0;
+            }
+            const uint32_t cnt = __reduce_add_sync(0xffffffffu, (uint32_t)__popc(w));
+            if (lane == 0 && cnt) atomicAdd(&st[p].dom_size[u], cnt);
+            continue;
+        }
         const uint32_t word = (uint32_t)(gw - prefix[item]);
         const uint32_t xl = word * 32 + lane;
         bool pass = xl < D.lsize[u];
@@ -152,8 +184,7 @@ __global__ void __launch_bounds__(256) k_domain_init(Graph g, const PatDesc *__r
         if (D.parent_off[u] >= 0) pass = pass && source_bit(srcs, n_srcs, D.parent_off[u], word, lane);
         for (int k = 0; k < kMaxPush; ++k)
             if (D.push_off[k][u] >= 0) pass = pass && source_bit(srcs, n_srcs, D.push_off[k][u], word, lane);
-        // (u is the same for the whole warp, so the test is skipped or run by all lanes)
-        if (((D.filter_mask >> u) & 1u) && __any_sync(0xffffffffu, pass)) {
+        if (__any_sync(0xffffffffu, pass)) {
             const uint32_t x = D.lstart[u] + xl;
             uint32_t b = 0, e = 0;
             if (pass && !TFSM_IN(33, x, g.n)) pass = false;
@@ -203,7 +234,7 @@ __global__ void __launch_bounds__(256) k_refine(Graph g, const PatDesc *__restri
     for (uint64_t gw = warp; gw < total; gw += nwarps) {
         item = find_item(prefix, n_items, gw, item);
         const uint32_t pu = item_pu[item];
-        const uint32_t p = pu >> 8, u = pu & 0xff;
+        const uint32_t p = (pu & ~kWideItem) >> 8, u = pu & 0xff;
         const PatDesc &D = descs[p];
         const uint32_t word = (uint32_t)(gw - prefix[item]);
         if (!TFSM_IN(34, D.off[u] + word, chk_words)) continue;

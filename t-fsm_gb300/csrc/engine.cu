@@ -733,15 +733,17 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
     // ---- domain init over every (pattern, vertex) ----
     std::vector<uint32_t> item_pu;
     std::vector<uint64_t> prefix;
-    auto build_items = [&](const std::vector<char> &active) {
+    // `wide`: the domain-init form, where a vertex with filter_mask clear takes one unit per 32 words
+    auto build_items = [&](const std::vector<char> &active, bool wide) {
         item_pu.clear();
         prefix.assign(1, 0);
         for (size_t p = 0; p < P; ++p) {
             if (!active[p]) continue;
             const PatDesc &D = L.hdescs[p];
             for (int u = 0; u < D.n; ++u) {
-                item_pu.push_back(((uint32_t)p << 8) | (uint32_t)u);
-                prefix.push_back(prefix.back() + D.words[u]);
+                const bool w = wide && !((D.filter_mask >> u) & 1u);
+                item_pu.push_back(((uint32_t)p << 8) | (uint32_t)u | (w ? dev::kWideItem : 0u));
+                prefix.push_back(prefix.back() + (w ? (D.words[u] + 31) / 32 : D.words[u]));
             }
         }
         I.item_pu.ensure(item_pu.size());
@@ -802,7 +804,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
             times_.h2d_bytes += ritem_pu.size() * 4 + rprefix.size() * 8;
         }
     }
-    build_items(active);
+    build_items(active, true);
     // refine_rounds 0: no arc consistency before the search (express patterns still run to their
     // fixpoint below: their domains are their result)
     const int fixed_refine = (int)std::min<uint32_t>(opt.refine_rounds, 32);
@@ -829,7 +831,9 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
         TFSM_CK(cudaEventElapsedTime(&ms, I.ev_mid, I.ev1));
         times_.refine_ms += ms;
         times_.init_launches++;
-        times_.init_words += words;
+        for (size_t p = 0; p < P; ++p)
+            if (active[p])
+                for (int u = 0; u < L.hdescs[p].n; ++u) times_.init_words += L.hdescs[p].words[u];
         times_.refine_launches += (uint64_t)fixed_refine;
         times_.refine_words += rwords * (uint64_t)fixed_refine;
     } else {
@@ -852,7 +856,7 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
             active[p] = !trivial[p] && express[p] && viable(p) &&
                         (round == 0 || ((I.hstatus[p].changed >> (round - 1)) & 1u));
         if (std::find(active.begin(), active.end(), 1) == active.end()) break;
-        build_items(active);
+        build_items(active, false);
         TFSM_CK(cudaEventRecord(I.ev0, I.stream));
         TFSM_CK(dev::launch_refine(I.g, L.descs.p, I.status.p, I.item_pu.p, I.prefix.p, (uint32_t)item_pu.size(),
                                    prefix.back(), L.dom.p, total, round, tau, opt.exact, I.stream));
