@@ -45,7 +45,7 @@ GEN_CASES = {
     "cfg2_t9000": dict(gen=dict(n=100000, mean=22, gamma=2.2, max_degree=1400, labels=29, zipf=1.2, elabels=1,
                                 seed=1), tau=9000, max_nodes=5, mni="all"),
     "cfg2_t7000": dict(gen=dict(n=100000, mean=22, gamma=2.2, max_degree=1400, labels=29, zipf=1.2, elabels=1,
-                                seed=1), tau=7000, max_nodes=5, mni="none", serial=False),
+                                seed=1), tau=7000, max_nodes=5, mni="all", serial=False),
     # the batched workload: the config-2 graph at tau 5000 with up to 6 pattern vertices (the
     # 5,000-vertex graph has no label frequent at tau 5000)
     "cfg3": dict(gen=dict(n=100000, mean=22, gamma=2.2, max_degree=1400, labels=29, zipf=1.2, elabels=1,
