@@ -80,6 +80,8 @@ struct PatDesc {
                                         //   when u's parent domain passed the same test: same degree and
                                         //   neighbour-label requirements in the parent); the engine then
                                         //   gives u a wide domain-init item (kWideItem)
+    int8_t hub_shift[kMaxN];            // searches from u split a hub's first depth above
+                                        //   hub_span << shift (negative: >>); kNoHubSplit: never
     int32_t nlf_n[kMaxN];               // neighbour-label-frequency requirements of u
     uint8_t nlf_lab[kMaxN][kMaxNlf];
     uint8_t nlf_cnt[kMaxN][kMaxNlf];
@@ -111,6 +113,7 @@ enum : uint32_t { kRunning = 0, kFrequent = 1, kInfrequent = 2 };
 // Domain-init items are (pattern << 8 | vertex); a wide one (this bit set) covers 32 bitmap words
 // per unit, one lane per word, for a vertex whose words are only its sources' words ANDed.
 constexpr uint32_t kWideItem = 0x80000000u;
+constexpr int8_t kNoHubSplit = 127;  // PatDesc::hub_shift: no hub split for this start vertex
 
 // Work item of the search kernel: a run of bitmap words of one representative's domain.
 struct SearchItem {

@@ -936,6 +936,13 @@ __global__ void __launch_bounds__(SearchBlock<N>::warps * 32, SearchBlock<N>::mi
         if (!TFSM_IN(22, descs[p].n, N + 1)) continue;
         load_plan(T, P, descs[p], p, u, prm.words);
         PatStatus &ps = st[p];
+        // this start vertex's hub-split span (the cost model may move it: PatDesc::hub_shift)
+        const int shift = descs[p].hub_shift[u];
+        uint32_t u_hub_span = hub_span;
+        if (shift == kNoHubSplit) u_hub_span = 0u;
+        else if (shift > 0) u_hub_span = hub_span << (shift < 8 ? shift : 8);
+        else if (shift < 0) u_hub_span = hub_span >> (-shift < 8 ? -shift : 8);
+        if (hub_span && shift != kNoHubSplit && u_hub_span == 0) u_hub_span = 1;
         unsigned long long n_search = 0, n_steps = 0, n_bytes = 0, max_steps = 0, n_isects = 0;
         bool stop = false, stopped = false;
         for (uint32_t word = item.word_lo; word < item.word_hi && !stop; ++word) {
@@ -968,7 +975,7 @@ __global__ void __launch_bounds__(SearchBlock<N>::warps * 32, SearchBlock<N>::mi
                 int adepth = 0;
                 ++n_search;
                 const Cancel cancel{found + o, 1u << b, &ps, u, exact};
-                int r = dfs(T, g, P, S, tile, dom, found, failed, 1, false, 0, 0, budget, hub_span, prm.isect_ratio,
+                int r = dfs(T, g, P, S, tile, dom, found, failed, 1, false, 0, 0, budget, u_hub_span, prm.isect_ratio,
                             cancel, steps, adepth, bytes, isects);
                 if (r == kAbort) {
                     // The unexplored remainder becomes tasks for the split rounds, grouped so that

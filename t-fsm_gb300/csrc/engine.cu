@@ -956,7 +956,13 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
                 size_t best = 0;
                 for (size_t j = 1; j < span[k].second; ++j)
                     if (y[span[k].first + j] < y[span[k].first + best]) best = j;
-                set_order(L.hdescs[planned[k].p], planned[k].u, cands[k][best]);
+                PatDesc &D = L.hdescs[planned[k].p];
+                set_order(D, planned[k].u, cands[k][best]);
+                // The predicted cost of the chosen order also sets the hub-split span of its searches:
+                // searches predicted to take 127 chunk steps or more split a hub's first depth above a
+                // quarter of hub_span, searches predicted to take at most 3 never split it.
+                const float c = y[span[k].first + best];  // log2(1 + chunk steps per search)
+                D.hub_shift[planned[k].u] = c >= 7.f ? (int8_t)-2 : c <= 2.f ? dev::kNoHubSplit : (int8_t)0;
             }
         }
         for (auto &pl : planned) {
