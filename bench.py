@@ -429,7 +429,7 @@ def gpu_arm(args, w, world, rank):
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32", "data": "synthetic", "config": config_of(args, w),
             "path": "batched (one engine call per growth level while calls take under 2 ms, smaller calls after a "
-                    "slower one); searches split into tasks after 16 chunk steps",
+                    f"slower one); searches split into tasks after {g.options()['step_budget']} chunk steps",
             "parallelism": "replicas" if world > 1 else "single GPU",
             "graph_vertices": info["n_vertices"], "graph_edges": info["n_edges"],
             "load_s": info["load_ms"] / 1e3, "wall_clock_mine_s": step_ms / 1e3,

@@ -205,7 +205,9 @@ typedef struct {
     uint32_t step_budget;   /* 32-candidate chunks a search may evaluate before its unexplored
                                branches (at every depth) become split tasks; split tasks get twice
                                that, doubling per round up to 8x; a search whose tasks find no room
-                               is retried by a later pass with 8x the budgets (0: never split) */
+                               is retried by a later pass with 8x the budgets (0: never split;
+                               default 16, or 64 for a graph with a vertex of more than 4 * hub_span
+                               neighbours) */
     uint32_t split_slice;   /* adjacency positions per split task (>= 1) */
     uint32_t chunk_words;   /* 32-bit domain-bitmap words per search work item (>= 1) */
     uint32_t refine_rounds; /* arc-consistency passes for patterns that need a search (0..32; 0: none,

@@ -191,6 +191,8 @@ bool read_options(const tfsm_options *in, const tfsm::EngineOptions &cur, tfsm_o
 const char *const kSizeRule = "tfsm_options.struct_size must be set to sizeof(tfsm_options) (at least "
                               "TFSM_OPTIONS_MIN_SIZE, at most the library's own size)";
 
+constexpr uint32_t kHubStepBudget = 64;  // default step budget of hub graphs (finish_graph)
+
 tfsm::EngineOptions engine_options(const tfsm_graph *g, uint32_t flags) {
     tfsm::EngineOptions o = g->opt;
     o.exact = (flags & TFSM_FLAG_EXACT) != 0;
@@ -204,6 +206,11 @@ int finish_graph(std::unique_ptr<tfsm_graph> &g, int tau, std::chrono::steady_cl
     g->tau = tau;
     const auto t_prune = std::chrono::steady_clock::now();
     if (!g->eng) g->eng.reset(new tfsm::GpuEngine(g->lg, 0));
+    // Hub graphs (a vertex with more than four hub spans of neighbours) split searches later: with
+    // hubs of ~40k neighbours a 16-step budget writes ~130 M split tasks per mining run, and 64
+    // steps measured 12% faster there; graphs without such hubs keep 16 (64 measured 19% slower on
+    // one with hubs of 1.4k).
+    if (g->lg.max_degree > 4 * g->opt.hub_span) g->opt.step_budget = kHubStepBudget;
     g->load_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (std::getenv("TFSM_VERBOSE"))
         std::fprintf(stderr, "[load] %s: parse + prune %.3f ms, engine %.3f ms (%s)\n",
