@@ -132,13 +132,13 @@ void fill_result(const tfsm::EvalResult &r, int n, tfsm_result *out) {
 const char *const kKnobRules =
     "split_slice, chunk_words, max_batch and isect_ratio must be >= 1; refine_rounds <= 32; refine_scope 0 or 1; "
     "hub_parts in 1..32; "
-    "time_limit_s and call_ms >= 0; search_lanes 0, 8 or 32";
+    "time_limit_s and call_ms >= 0; search_lanes 0, 4, 8 or 32";
 
 bool knobs_valid(const tfsm_options &o) {
     return o.split_slice >= 1 && o.chunk_words >= 1 && o.refine_rounds <= 32 && o.max_batch >= 1 &&
            o.hub_parts >= 1 && o.hub_parts <= 32 && o.isect_ratio >= 1 && o.time_limit_s >= 0 && o.call_ms >= 0 &&
            o.refine_scope <= 1 &&
-           (o.search_lanes == 0 || o.search_lanes == 8 || o.search_lanes == 32);
+           (o.search_lanes == 0 || o.search_lanes == 4 || o.search_lanes == 8 || o.search_lanes == 32);
 }
 
 // The speed-only knobs of `o` (not the time limit, which belongs to the whole run).

@@ -367,13 +367,15 @@ struct Team {
     }
 };
 
-// Block shape of a search kernel whose teams hold state for patterns of up to N vertices: the
-// 32-vertex state (about 11 KB per team) fits four whole-warp teams per block in static shared
-// memory; smaller states keep kSearchWarps warps.
-template <int N>
+// Block shape of a search kernel with teams of G lanes holding state for patterns of up to N
+// vertices: the 32-vertex state (about 11 KB per team) fits four whole-warp teams per block in
+// static shared memory, and so do the 32 teams of 4 lanes of four warps; otherwise kSearchWarps
+// warps.
+template <int G, int N>
 struct SearchBlock {
-    static constexpr int warps = N > kTaskMaxN ? 4 : kSearchWarps;
-    static constexpr int min_blocks = N > kTaskMaxN ? 2 * kSearchMinBlocks : kSearchMinBlocks;
+    // 32-vertex state, or eight teams of 4 lanes per warp: four warps per block (static shared memory)
+    static constexpr int warps = N > kTaskMaxN || G == 4 ? 4 : kSearchWarps;
+    static constexpr int min_blocks = N > kTaskMaxN || G == 4 ? 2 * kSearchMinBlocks : kSearchMinBlocks;
 };
 
 template <int N>
@@ -894,10 +896,12 @@ __device__ __forceinline__ bool pattern_stops(const Team<G> &T, const PatStatus 
 // claims its own items.  Outside the last pass, a search whose remainder finds no room is set aside
 // (neither found nor failed), and a team starts no more searches once the first round's share of
 // the buffer is full: the next pass, with larger budgets, takes up what is left.
-// Instances: teams of 8 lanes for patterns of at most 8 vertices, whole warps for at most 16, and
-// whole warps for at most 32 (these searches never split: split tasks hold 16-vertex prefixes).
+// Instances: teams of 4 lanes for patterns of at most 5 vertices (a depth has at most 4 backward
+// neighbours, one per lane in setup_depth), teams of 8 lanes for at most 8, whole warps for at most
+// 16, and whole warps for at most 32 (these searches never split: split tasks hold 16-vertex
+// prefixes).
 template <int G, int N>
-__global__ void __launch_bounds__(SearchBlock<N>::warps * 32, SearchBlock<N>::min_blocks)
+__global__ void __launch_bounds__(SearchBlock<G, N>::warps * 32, SearchBlock<G, N>::min_blocks)
     k_search(Graph g, const PatDesc *__restrict__ descs,
                                                               PatStatus *__restrict__ st,
                                                               const ItemGroup *__restrict__ igroups,
@@ -908,7 +912,7 @@ __global__ void __launch_bounds__(SearchBlock<N>::warps * 32, SearchBlock<N>::mi
                                                               uint32_t *__restrict__ failed,
                                                               SplitTask *__restrict__ splits,
                                                               SplitGroup *__restrict__ groups) {
-    constexpr int kTeams = SearchBlock<N>::warps * 32 / G;
+    constexpr int kTeams = SearchBlock<G, N>::warps * 32 / G;
     constexpr bool kSplits = N <= kTaskMaxN;
     __shared__ Plan<N> plans[kTeams];
     __shared__ State<N> states[kTeams];
@@ -1043,7 +1047,7 @@ __global__ void __launch_bounds__(SearchBlock<N>::warps * 32, SearchBlock<N>::mi
 // pass, a remainder without room is set aside (the group is marked incomplete, so v stays
 // undecided for the next pass).
 template <int G, int N>
-__global__ void __launch_bounds__(SearchBlock<N>::warps * 32, SearchBlock<N>::min_blocks)
+__global__ void __launch_bounds__(SearchBlock<G, N>::warps * 32, SearchBlock<G, N>::min_blocks)
     k_split(Graph g, const PatDesc *__restrict__ descs,
                                                              PatStatus *__restrict__ st, SearchParams prm,
                                                              uint32_t *__restrict__ counters, int round,
@@ -1054,7 +1058,7 @@ __global__ void __launch_bounds__(SearchBlock<N>::warps * 32, SearchBlock<N>::mi
                                                              SplitTask *__restrict__ out,
                                                              SplitGroup *__restrict__ groups) {
     static_assert(N <= kTaskMaxN, "split tasks hold prefixes of at most kTaskMaxN vertices");
-    constexpr int kTeams = SearchBlock<N>::warps * 32 / G;
+    constexpr int kTeams = SearchBlock<G, N>::warps * 32 / G;
     __shared__ Plan<N> plans[kTeams];
     __shared__ State<N> states[kTeams];
     __shared__ Tile<G> tiles[kTeams];
@@ -1209,7 +1213,7 @@ cudaError_t launch_search_t(const Graph &g, const PatDesc *descs, PatStatus *st,
                             const ItemEntry *ientries, const SearchParams &prm, uint32_t *counters,
                             const uint32_t *dom, uint32_t *found, uint32_t *failed, SplitTask *splits,
                             SplitGroup *groups, cudaStream_t s) {
-    constexpr int kThreads = SearchBlock<N>::warps * 32;
+    constexpr int kThreads = SearchBlock<G, N>::warps * 32;
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<G, N>, kThreads, 0);
     if (per_sm <= 0) per_sm = 1;
@@ -1227,7 +1231,7 @@ cudaError_t launch_split_t(const Graph &g, const PatDesc *descs, PatStatus *st, 
                            uint32_t *counters, int round, uint32_t budget, const uint32_t *dom, uint32_t *found,
                            uint32_t *failed, const SplitTask *in, SplitTask *out, SplitGroup *groups,
                            cudaStream_t s) {
-    constexpr int kThreads = SearchBlock<N>::warps * 32;
+    constexpr int kThreads = SearchBlock<G, N>::warps * 32;
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_split<G, N>, kThreads, 0);
     if (per_sm <= 0) per_sm = 1;
@@ -1245,10 +1249,15 @@ cudaError_t launch_search(const Graph &g, const PatDesc *descs, PatStatus *st, c
     if (prm.n_groups == 0 || prm.chunk_words == 0 || !igroups || !ientries) return cudaErrorInvalidValue;
     if (prm.split && (!splits || !groups || prm.split_cap == 0 || prm.group_cap == 0 || prm.split_slice == 0))
         return cudaErrorInvalidValue;
-    if (prm.max_n > (uint32_t)kMaxN || (prm.team_lanes == 8 && prm.max_n > 8)) return cudaErrorInvalidValue;
+    if (prm.max_n > (uint32_t)kMaxN || (prm.team_lanes == 8 && prm.max_n > 8) ||
+        (prm.team_lanes == 4 && prm.max_n > 5))
+        return cudaErrorInvalidValue;
     if (prm.split && prm.max_n > (uint32_t)kTaskMaxN) return cudaErrorInvalidValue;
     cudaError_t e;
-    if (prm.team_lanes == 8)
+    if (prm.team_lanes == 4)
+        e = launch_search_t<4, 8>(g, descs, st, igroups, ientries, prm, counters, dom, found, failed, splits, groups,
+                                  s);
+    else if (prm.team_lanes == 8)
         e = launch_search_t<8, 8>(g, descs, st, igroups, ientries, prm, counters, dom, found, failed, splits, groups,
                                   s);
     else if (prm.team_lanes == 32 && prm.max_n <= (uint32_t)kTaskMaxN)
@@ -1281,9 +1290,13 @@ cudaError_t launch_split_round(const Graph &g, const PatDesc *descs, PatStatus *
     const SplitTask *in = splits + (size_t)(round % 2) * prm.split_cap;
     SplitTask *out = splits + (size_t)((round + 1) % 2) * prm.split_cap;
     if (round + 1 == kMaxRounds) budget = 0;  // the last possible round completes every task
-    if (prm.max_n > (uint32_t)kTaskMaxN || (prm.team_lanes == 8 && prm.max_n > 8)) return cudaErrorInvalidValue;
+    if (prm.max_n > (uint32_t)kTaskMaxN || (prm.team_lanes == 8 && prm.max_n > 8) ||
+        (prm.team_lanes == 4 && prm.max_n > 5))
+        return cudaErrorInvalidValue;
     cudaError_t e;
-    if (prm.team_lanes == 8)
+    if (prm.team_lanes == 4)
+        e = launch_split_t<4, 8>(g, descs, st, prm, counters, round, budget, dom, found, failed, in, out, groups, s);
+    else if (prm.team_lanes == 8)
         e = launch_split_t<8, 8>(g, descs, st, prm, counters, round, budget, dom, found, failed, in, out, groups, s);
     else if (prm.team_lanes == 32)
         e = launch_split_t<32, kTaskMaxN>(g, descs, st, prm, counters, round, budget, dom, found, failed, in, out,

@@ -997,6 +997,8 @@ void GpuEngine::evaluate(const std::vector<const Pattern *> &pats, const std::ve
             ++searched_pats;
         }
     if (opt.search_lanes == 8 && max_n <= 8 && searched_pats > 1) team_lanes = 8;
+    // teams of 4 lanes: patterns of at most 5 vertices (at most 4 backward neighbours per depth)
+    if (opt.search_lanes == 4 && searched_pats > 1) team_lanes = max_n <= 5 ? 4 : max_n <= 8 ? 8 : 32;
     const uint32_t cw = std::max<uint32_t>(1, opt.chunk_words);
     std::vector<dev::ItemGroup> igroups;
     std::vector<dev::ItemEntry> ientries;

@@ -50,8 +50,9 @@ struct EngineOptions {
                                        //   is at most this many times the step's survivors, else
                                        //   galloping search
     uint32_t chunk_words = 1;          // bitmap words per search work item (x32 candidates)
-    uint32_t search_lanes = 8;         // lanes per search: 32, or 8 (four searches per warp, used for
-                                       //   calls with several patterns of at most 8 vertices)
+    uint32_t search_lanes = 8;         // lanes per search: 32, 8 (four searches per warp, used for calls
+                                       //   with several patterns of at most 8 vertices) or 4 (eight per
+                                       //   warp, patterns of at most 5 vertices; larger ones fall back)
     uint32_t refine_rounds = 1;        // arc-consistency passes for patterns that need search (0: none)
     uint32_t refine_scope = 1;         // 1: a child's first refinement rounds cover its newest edge's two
                                        //   vertices only (the rest were refined in its parent's call); 0: all

@@ -7,7 +7,7 @@
 // __shfl_sync, __shfl_xor_sync, __reduce_add_sync) are rendezvous on a std::barrier, which also
 // orders memory like bar.warp.sync.  __shared__ variables become static storage (one block at a
 // time).  Atomics are GCC __atomic builtins; __ldcg is a relaxed atomic load.  Device memory is
-// host memory.  Masks: the full warp, or an aligned group of 8 or 16 lanes (a team of lanes that
+// host memory.  Masks: the full warp, or an aligned group of 4, 8 or 16 lanes (a team of lanes that
 // runs its own search); each group has its own rendezvous, so groups of a warp proceed independently.
 #pragma once
 
@@ -78,21 +78,23 @@ struct Barrier {
 
 struct Warp {
     Barrier bar;
-    Barrier g8[4], g16[2];  // aligned lane groups
+    Barrier g4[8], g8[4], g16[2];  // aligned lane groups
     uint64_t vals[32];
     Warp() {
+        for (auto &b : g4) b.count = 4;
         for (auto &b : g8) b.count = 8;
         for (auto &b : g16) b.count = 16;
     }
     Barrier &of(unsigned mask) {
         if (mask == 0xffffffffu) return bar;
         const unsigned base = (unsigned)__builtin_ctz(mask), size = (unsigned)__builtin_popcount(mask);
-        const bool aligned = (size == 8 || size == 16) && base % size == 0 && mask == (((1u << size) - 1) << base);
+        const bool aligned = (size == 4 || size == 8 || size == 16) && base % size == 0 &&
+                             mask == (((1u << size) - 1) << base);
         if (!aligned) {
             std::fprintf(stderr, "emulation: unsupported collective mask %08x\n", mask);
             std::abort();
         }
-        return size == 8 ? g8[base / 8] : g16[base / 16];
+        return size == 4 ? g4[base / 4] : size == 8 ? g8[base / 8] : g16[base / 16];
     }
 };
 

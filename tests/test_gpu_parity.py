@@ -297,10 +297,11 @@ def test_subpattern_pruning_keeps_results(tfsm, graphs, case, tmp_path):
         assert sa["pruned"] > 0
 
 
-@pytest.mark.parametrize("case", ["cfg1", "el3", "clique", "quirk_elabels", "cfg2_t9000"])
-@pytest.mark.parametrize("lanes", [8, 32])
+@pytest.mark.parametrize("case", ["cfg1", "el3", "clique", "quirk_elabels", "cfg2_t9000", "cfg4_m3"])
+@pytest.mark.parametrize("lanes", [4, 8, 32])
 def test_team_sizes_keep_results(tfsm, graphs, case, lanes, tmp_path):
-    """Searches run by teams of 8 lanes (four per warp) or by whole warps: the same pattern sets and
+    """Searches run by teams of 4 lanes (eight per warp; patterns of at most 5 vertices, larger
+    ones fall back to 8 or 32), of 8 lanes (four per warp) or by whole warps: the same pattern sets and
     exact supports."""
     g = graphs(case)
     saved = g.options()

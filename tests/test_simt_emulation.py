@@ -40,6 +40,8 @@ OPTS = {"default": [],
         "plain": ["-plain", "-refine-rounds", "1"], "exact": ["-exact"], "batch3": ["-max-batch", "3"],
         "random_orders": ["-random-orders", "7", "-step-budget", "2"],
         "lanes8": ["-search-lanes", "8"],
+        "lanes4": ["-search-lanes", "4"],
+        "lanes4_split": ["-search-lanes", "4", "-step-budget", "1", "-split-slice", "1"],
         "lanes8_split": ["-search-lanes", "8", "-step-budget", "1", "-split-slice", "1"],
         "lanes8_exact": ["-search-lanes", "8", "-exact", "-step-budget", "1", "-split-slice", "1"],
         "rank_window2": ["-rank-window", "2", "-step-budget", "2"],
