@@ -1,11 +1,12 @@
 """Generate the golden fixtures of the parity tests from the reference T-FSM itself.
 
 Runs only where the reference sources exist (oracle/Makefile reads them from the tree its REF
-variable names): `make -C oracle ref harness port REF=<tree>` builds
+variable names): `make -C oracle ref harness port brute REF=<tree>` builds
   oracle/_ref/serial_run    the reference serial miner   (serial/Makefile flags)
   oracle/_ref/parallel_run  the reference parallel miner (parallel/Makefile flags)
   oracle/_ref/mni_harness   exact MNI domains from the reference's GMatchEngine
   oracle/tfsm_port          the CPU restatement (used here only to list candidate patterns)
+  oracle/mni_brute          exact MNI domains from the definition by plain backtracking
 
 For every case it writes, next to this script:
   <case>.patterns.txt  frequent patterns (DFS-code keys, sorted) from the serial build; the
@@ -13,9 +14,11 @@ For every case it writes, next to this script:
   <case>.mni.txt       "<key> | c0 c1 ..." exact per-vertex MNI domain sizes from the harness, for
                        frequent and infrequent candidates alike
 and cases.json with the graph recipe (generator arguments or a committed graph file), tau,
-maxNodes and the graph checksum.
+maxNodes and the graph checksum.  For the pattern samples of MNI_SAMPLES it writes
+<sample>.mni.txt (the harness) and <sample>.brute.txt (oracle/mni_brute) for the patterns that
+<sample>.keys.txt lists.
 
-usage: python tests/golden/make_golden.py [case ...]
+usage: python tests/golden/make_golden.py [case or sample ...]
 """
 from __future__ import annotations
 
@@ -33,6 +36,7 @@ ROOT = HERE.parent.parent
 REF = ROOT / "oracle" / "_ref"
 GEN = ROOT / "t-fsm_gb300" / "bin" / "gen_lg"
 PORT = ROOT / "oracle" / "tfsm_port"
+BRUTE = ROOT / "oracle" / "mni_brute"
 sys.path.insert(0, str(ROOT / "tests"))
 from golden_io import read_parallel_stdout, read_results, graph_checksum  # noqa: E402
 
@@ -58,6 +62,15 @@ GEN_CASES = {
     "cfg4_m3": dict(gen=dict(n=2000000, mean=20, gamma=2.05, max_degree=50000, labels=50, zipf=1.1, elabels=3,
                              seed=2), tau=20000, max_nodes=3, mni="none", serial=False, threads=0),
 }
+
+# Exact MNI of listed patterns on a case's graph, without a mining run: <name>.keys.txt holds the
+# patterns (DFS-code keys), the harness writes <name>.mni.txt.  cfg4_sample: 4- and 5-vertex
+# patterns of the 2M-vertex hub graph, beyond what the reference's miners finish here (maxNodes 4
+# and 5); its keys are every 190th frequent 4-vertex tree, every 90th 4-vertex cycle and every
+# 8000th 5-vertex pattern of the GPU miner's maxNodes-5 output on that graph (output order), plus
+# every 400th 4-vertex tree from the 8th with its last vertex relabelled to the rarest frequent
+# label (infrequent candidates).  The reference's engine decides every one of them.
+MNI_SAMPLES = {"cfg4_sample": dict(graph_case="cfg4_m3")}
 
 # Small hand-made graphs for edge cases, written by make_small_graphs().
 FILE_CASES = {
@@ -143,15 +156,60 @@ def run(cmd, cwd=None, timeout=None) -> subprocess.CompletedProcess:
     return r
 
 
+def make_mni_sample(name: str) -> None:
+    """<name>.mni.txt: the harness on every pattern of <name>.keys.txt, the keys split over all
+    cores (one harness process each, every process loads the graph); <name>.brute.txt: the
+    definition checker on the same patterns."""
+    spec = GEN_CASES[MNI_SAMPLES[name]["graph_case"]]
+    keys = [k for k in (HERE / f"{name}.keys.txt").read_text().splitlines() if k.strip()]
+    with tempfile.TemporaryDirectory() as tmp:
+        tmp = Path(tmp)
+        graph = tmp / "g.lg"
+        run([GEN, "--out", graph, *gen_args(spec["gen"])])
+        parts = min(len(keys), os.cpu_count() or 4)
+        procs = []
+        for i in range(parts):
+            plist = tmp / f"pats{i}.txt"
+            plist.write_text("".join(k + "\n" for k in keys[i::parts]))
+            procs.append(subprocess.Popen([str(REF / "mni_harness"), "-file", str(graph), "-freq", str(spec["tau"]),
+                                           "-patterns", str(plist)], stdout=subprocess.PIPE, text=True))
+        got = {}
+        for p in procs:
+            out, _ = p.communicate(timeout=7200)
+            if p.returncode != 0:
+                sys.exit(f"{name}: mni_harness failed")
+            for ln in out.splitlines():
+                if " | " in ln:
+                    got[ln.split(" | ")[0]] = ln
+        missing = [k for k in keys if k not in got]
+        if missing:
+            sys.exit(f"{name}: no result for {len(missing)} patterns, e.g. {missing[0]}")
+        (HERE / f"{name}.mni.txt").write_text("".join(got[k] + "\n" for k in keys))
+        # the same patterns through the definition checker (oracle/mni_brute.cpp)
+        plist = tmp / "all.txt"
+        plist.write_text("".join(k + "\n" for k in keys))
+        b = run([BRUTE, "-file", graph, "-freq", spec["tau"], "-patterns", plist], timeout=7200)
+        brute = {ln.split(" | ")[0]: ln for ln in b.stdout.splitlines() if " | " in ln}
+        if [k for k in keys if k not in brute]:
+            sys.exit(f"{name}: the definition checker skipped patterns")
+        (HERE / f"{name}.brute.txt").write_text("".join(brute[k] + "\n" for k in keys))
+    differ = [k for k in keys if got[k] != brute[k]]
+    print(name, len(keys), "patterns;", len(differ), "where the reference engine differs from the definition",
+          flush=True)
+
+
 def main(names: list[str]) -> None:
-    for tool in (REF / "serial_run", REF / "parallel_run", REF / "mni_harness", PORT, GEN):
+    for tool in (REF / "serial_run", REF / "parallel_run", REF / "mni_harness", PORT, BRUTE, GEN):
         if not tool.exists():
-            sys.exit(f"missing {tool}: run `make -C oracle ref harness port REF=<tree>` and t-fsm_gb300/build.py first")
+            sys.exit(f"missing {tool}: run `make -C oracle ref harness port brute REF=<tree>` and "
+                     "t-fsm_gb300/build.py first")
     make_small_graphs()
     cases_path = HERE / "cases.json"
     cases = json.loads(cases_path.read_text()) if cases_path.exists() else {}
     todo = {**GEN_CASES, **FILE_CASES}
-    for name in names or list(todo):
+    for name in [n for n in names or list(MNI_SAMPLES) if n in MNI_SAMPLES]:
+        make_mni_sample(name)
+    for name in [n for n in names if n not in MNI_SAMPLES] if names else list(todo):
         spec = todo[name]
         with tempfile.TemporaryDirectory() as tmp:
             tmp = Path(tmp)
