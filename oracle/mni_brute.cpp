@@ -48,7 +48,7 @@ bool parse_pattern(const std::string &line, Pat &p) {
     }
     int n = 0;
     for (auto &c : codes) n = std::max(n, std::max(c[0], c[1]) + 1);
-    if (n == 0 || n > 16) return false;
+    if (n == 0 || n > 32) return false;
     p.n = n;
     p.lab.assign(n, -1);
     p.adj.assign(n, {});

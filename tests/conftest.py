@@ -58,6 +58,14 @@ def port(built):
     return ROOT / "oracle" / "tfsm_port"
 
 
+@pytest.fixture(scope="session")
+def brute():
+    """The definition checker (oracle/mni_brute), built from source."""
+    r = subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "brute"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return ROOT / "oracle" / "mni_brute"
+
+
 CASES = json.loads((GOLDEN / "cases.json").read_text())
 
 

@@ -1,4 +1,5 @@
-"""The CPU oracle (oracle/tfsm_port) pinned against the reference's own outputs.
+"""The CPU oracle (oracle/tfsm_port) and the definition checker (oracle/mni_brute) pinned against
+the reference's own outputs.
 
 tests/golden/ holds, per case, the frequent-pattern set of the reference serial and parallel builds
 and exact per-vertex MNI domain sizes from the reference's matching engine (made by
@@ -11,7 +12,7 @@ import subprocess
 
 import pytest
 
-from conftest import CASES, golden_mni, golden_pattern_set
+from conftest import CASES, GOLDEN, golden_mni, golden_pattern_set
 from golden_io import read_mni, read_results
 
 SMALL = [n for n, c in CASES.items() if "file" in c or c["gen"]["n"] <= 5000]
@@ -62,3 +63,33 @@ def test_oracle_lazy_supports_are_consistent(port, case_graph, tmp_path):
         if k in exact and min(exact[k]) >= tau:
             assert min(v) >= tau
             assert all(a <= b for a, b in zip(v, exact[k]))
+
+
+def run_brute(brute, graph, tau, keys, tmp_path):
+    plist = tmp_path / "patterns.txt"
+    plist.write_text("".join(k + "\n" for k in keys))
+    out = tmp_path / "brute.txt"
+    r = subprocess.run([str(brute), "-file", str(graph), "-freq", str(tau), "-patterns", str(plist)],
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out.write_text(r.stdout)
+    return read_mni(out)
+
+
+@pytest.mark.parametrize("case", [n for n in CASES if golden_mni(n)])
+def test_definition_checker_matches_reference_engine(case, brute, case_graph, tmp_path):
+    """oracle/mni_brute (exact MNI from the definition by plain backtracking) equals the reference
+    engine's exact MNI on every golden whose searches stay below the engine's timeout."""
+    want = golden_mni(case)
+    assert run_brute(brute, case_graph(case), CASES[case]["tau"], list(want), tmp_path) == want
+
+
+def test_definition_checker_reproduces_hub_graph_sample(brute, case_graph, tmp_path):
+    """The definition checker's fixture for the config-4 sample (tests/golden/cfg4_sample.brute.txt)
+    is what the checker computes; it agrees with the reference engine's run on at least 28 of the
+    31 patterns (the others hit the engine's resumed-search deviation)."""
+    want = read_mni(GOLDEN / "cfg4_sample.brute.txt")
+    got = run_brute(brute, case_graph("cfg4_m3"), CASES["cfg4_m3"]["tau"], list(want), tmp_path)
+    assert got == want
+    ref = golden_mni("cfg4_sample")
+    assert sum(ref[k] == want[k] for k in want) >= 28
