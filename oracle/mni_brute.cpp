@@ -53,8 +53,11 @@ bool parse_pattern(const std::string &line, Pat &p) {
     p.lab.assign(n, -1);
     p.adj.assign(n, {});
     for (auto &c : codes) {
-        p.lab[c[0]] = c[2];
-        p.lab[c[1]] = c[4];
+        for (int k : {0, 1}) {  // a vertex keeps one label across its codes
+            const int x = c[k], l = c[k == 0 ? 2 : 4];
+            if (p.lab[x] >= 0 && p.lab[x] != l) return false;
+            p.lab[x] = l;
+        }
         p.adj[c[0]].push_back({c[1], c[3]});
         p.adj[c[1]].push_back({c[0], c[3]});
     }

@@ -15,8 +15,8 @@ For every case it writes, next to this script:
                        frequent and infrequent candidates alike
 and cases.json with the graph recipe (generator arguments or a committed graph file), tau,
 maxNodes and the graph checksum.  For the pattern samples of MNI_SAMPLES it writes
-<sample>.mni.txt (the harness) and <sample>.brute.txt (oracle/mni_brute) for the patterns that
-<sample>.keys.txt lists.
+<sample>.brute.txt (oracle/mni_brute) and, where the sample asks for it, <sample>.mni.txt (the
+harness) for the patterns that <sample>.keys.txt lists.
 
 usage: python tests/golden/make_golden.py [case or sample ...]
 """
@@ -70,7 +70,13 @@ GEN_CASES = {
 # 8000th 5-vertex pattern of the GPU miner's maxNodes-5 output on that graph (output order), plus
 # every 400th 4-vertex tree from the 8th with its last vertex relabelled to the rarest frequent
 # label (infrequent candidates).  The reference's engine decides every one of them.
-MNI_SAMPLES = {"cfg4_sample": dict(graph_case="cfg4_m3")}
+# cfg4_wide: 392 more patterns of the same graph, for the definition checker only (the reference's
+# engine needs minutes per pattern there): every 10th frequent 4-vertex pattern from the 4th and
+# every 1500th 5-vertex pattern from the 6th of the same outputs, and every 50th 4-vertex pattern
+# from the 12th whose last code is a forward edge, its new vertex relabelled to label 8, 7 or 6
+# (the first that gives no frequent pattern's code), none of them in cfg4_sample.
+MNI_SAMPLES = {"cfg4_sample": dict(graph_case="cfg4_m3", reference=True),
+               "cfg4_wide": dict(graph_case="cfg4_m3", reference=False)}
 
 # Small hand-made graphs for edge cases, written by make_small_graphs().
 FILE_CASES = {
@@ -157,16 +163,16 @@ def run(cmd, cwd=None, timeout=None) -> subprocess.CompletedProcess:
 
 
 def make_mni_sample(name: str) -> None:
-    """<name>.mni.txt: the harness on every pattern of <name>.keys.txt, the keys split over all
-    cores (one harness process each, every process loads the graph); <name>.brute.txt: the
-    definition checker on the same patterns."""
+    """<name>.mni.txt (samples marked `reference`): the harness on every pattern of
+    <name>.keys.txt, the keys split over all cores (one harness process each, every process loads
+    the graph); <name>.brute.txt: the definition checker on the same patterns."""
     spec = GEN_CASES[MNI_SAMPLES[name]["graph_case"]]
     keys = [k for k in (HERE / f"{name}.keys.txt").read_text().splitlines() if k.strip()]
     with tempfile.TemporaryDirectory() as tmp:
         tmp = Path(tmp)
         graph = tmp / "g.lg"
         run([GEN, "--out", graph, *gen_args(spec["gen"])])
-        parts = min(len(keys), os.cpu_count() or 4)
+        parts = min(len(keys), os.cpu_count() or 4) if MNI_SAMPLES[name]["reference"] else 0
         procs = []
         for i in range(parts):
             plist = tmp / f"pats{i}.txt"
@@ -182,9 +188,10 @@ def make_mni_sample(name: str) -> None:
                 if " | " in ln:
                     got[ln.split(" | ")[0]] = ln
         missing = [k for k in keys if k not in got]
-        if missing:
+        if parts and missing:
             sys.exit(f"{name}: no result for {len(missing)} patterns, e.g. {missing[0]}")
-        (HERE / f"{name}.mni.txt").write_text("".join(got[k] + "\n" for k in keys))
+        if parts:
+            (HERE / f"{name}.mni.txt").write_text("".join(got[k] + "\n" for k in keys))
         # the same patterns through the definition checker (oracle/mni_brute.cpp)
         plist = tmp / "all.txt"
         plist.write_text("".join(k + "\n" for k in keys))
@@ -193,7 +200,7 @@ def make_mni_sample(name: str) -> None:
         if [k for k in keys if k not in brute]:
             sys.exit(f"{name}: the definition checker skipped patterns")
         (HERE / f"{name}.brute.txt").write_text("".join(brute[k] + "\n" for k in keys))
-    differ = [k for k in keys if got[k] != brute[k]]
+    differ = [k for k in keys if k in got and got[k] != brute[k]]
     print(name, len(keys), "patterns;", len(differ), "where the reference engine differs from the definition",
           flush=True)
 

@@ -171,6 +171,25 @@ def test_hub_graph_sample_matches_reference_engine(tfsm, graphs, opts):
     assert any(min(v) < tau for v in want.values()) and any(min(v) >= tau for v in want.values())
 
 
+def test_hub_graph_wide_sample_matches_definition(tfsm, graphs):
+    """392 more 4- and 5-vertex patterns of the 2M-vertex hub graph, frequent and infrequent: exact
+    MNI equals the definition checker's (tests/golden/cfg4_wide.brute.txt; the checker itself is
+    pinned to every exact-MNI golden of the reference's engine), and lazy decisions equal exact
+    support >= tau."""
+    want = read_mni(GOLDEN / "cfg4_wide.brute.txt")
+    keys = list(want)
+    assert len(keys) == 392
+    tau = CASES["cfg4_m3"]["tau"]
+    g = graphs("cfg4_m3")
+    pats = [tfsm.parse_key(k) for k in keys]
+    res = g.evaluate(pats, flags=tfsm.FLAG_EXACT)
+    bad = [(k, want[k], r.mni) for k, r in zip(keys, res) if r.status != 0 or r.mni != want[k]]
+    assert not bad, f"{len(bad)} of {len(keys)} differ, e.g. {bad[:3]}"
+    lazy = g.evaluate(pats)
+    assert [r.frequent for r in lazy] == [min(want[k]) >= tau for k in keys]
+    assert sum(min(v) < tau for v in want.values()) >= 20
+
+
 @pytest.mark.parametrize("case", ["cfg1", "el3", "quirk_elabels", "cfg2_t9000"])
 def test_lazy_decision_matches_exact_support(tfsm, graphs, case):
     want = golden_mni(case)

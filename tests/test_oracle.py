@@ -93,3 +93,13 @@ def test_definition_checker_reproduces_hub_graph_sample(brute, case_graph, tmp_p
     assert got == want
     ref = golden_mni("cfg4_sample")
     assert sum(ref[k] == want[k] for k in want) >= 28
+
+
+def test_definition_checker_rejects_inconsistent_labels(brute, tmp_path):
+    """A key whose codes give one vertex two labels is not a pattern: the checker stops (exit 2)
+    instead of evaluating a relabelled one."""
+    plist = tmp_path / "bad.txt"
+    plist.write_text("0,1,0,1,0 1,2,0,1,0 2,3,0,1,2 3,0,2,3,8\n")
+    r = subprocess.run([str(brute), "-file", str(GOLDEN / "graphs" / "clique.lg"), "-freq", "3", "-patterns",
+                        str(plist)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "bad pattern" in r.stderr
