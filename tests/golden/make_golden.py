@@ -75,8 +75,11 @@ GEN_CASES = {
 # every 1500th 5-vertex pattern from the 6th of the same outputs, and every 50th 4-vertex pattern
 # from the 12th whose last code is a forward edge, its new vertex relabelled to label 8, 7 or 6
 # (the first that gives no frequent pattern's code), none of them in cfg4_sample.
+# cfg4_m4: every pattern the GPU miner reports on that graph at maxNodes 4 (3 412; its
+# grami_results.txt keys, sorted), for the definition checker: each must have support >= tau.
 MNI_SAMPLES = {"cfg4_sample": dict(graph_case="cfg4_m3", reference=True),
-               "cfg4_wide": dict(graph_case="cfg4_m3", reference=False)}
+               "cfg4_wide": dict(graph_case="cfg4_m3", reference=False),
+               "cfg4_m4": dict(graph_case="cfg4_m3", reference=False)}
 
 # Small hand-made graphs for edge cases, written by make_small_graphs().
 FILE_CASES = {
