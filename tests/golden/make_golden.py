@@ -79,7 +79,10 @@ GEN_CASES = {
 # grami_results.txt keys, sorted), for the definition checker: each must have support >= tau.
 MNI_SAMPLES = {"cfg4_sample": dict(graph_case="cfg4_m3", reference=True),
                "cfg4_wide": dict(graph_case="cfg4_m3", reference=False),
-               "cfg4_m4": dict(graph_case="cfg4_m3", reference=False)}
+               "cfg4_m4": dict(graph_case="cfg4_m3", reference=False),
+               # every 100th (from the first) of the sorted 5-vertex keys the GPU miner reports
+               # there at maxNodes 5 (423 of 42 277)
+               "cfg4_m5_sample": dict(graph_case="cfg4_m3", reference=False)}
 
 # Small hand-made graphs for edge cases, written by make_small_graphs().
 FILE_CASES = {

@@ -209,6 +209,24 @@ def test_hub_graph_maxnodes4_set_is_frequent_by_definition(tfsm, graphs, tmp_pat
     assert small == golden_pattern_set("cfg4_m3")
 
 
+def test_hub_graph_maxnodes5_sample_is_frequent_by_definition(tfsm, graphs):
+    """Every 100th of the 5-vertex patterns the GPU miner reports on the 2M-vertex hub graph at
+    maxNodes 5 (the target configuration; 423 of 42 277, tests/golden/cfg4_m5_sample.brute.txt):
+    each has exact support >= tau by the definition checker, the lazy evaluation decides every one
+    frequent, and exact evaluation of every 5th equals the checker's domain sizes."""
+    want = read_mni(GOLDEN / "cfg4_m5_sample.brute.txt")
+    tau = CASES["cfg4_m3"]["tau"]
+    keys = list(want)
+    assert len(keys) == 423 and all(min(v) >= tau for v in want.values())
+    g = graphs("cfg4_m3")
+    lazy = g.evaluate([tfsm.parse_key(k) for k in keys])
+    assert all(r.status == 0 and r.frequent and r.support >= tau for r in lazy)
+    some = keys[::5]
+    res = g.evaluate([tfsm.parse_key(k) for k in some], flags=tfsm.FLAG_EXACT)
+    bad = [(k, want[k], r.mni) for k, r in zip(some, res) if r.status != 0 or r.mni != want[k]]
+    assert not bad, f"{len(bad)} of {len(some)} differ, e.g. {bad[:3]}"
+
+
 @pytest.mark.parametrize("case", ["cfg1", "el3", "quirk_elabels", "cfg2_t9000"])
 def test_lazy_decision_matches_exact_support(tfsm, graphs, case):
     want = golden_mni(case)
