@@ -193,9 +193,10 @@ def test_hub_graph_wide_sample_matches_definition(tfsm, graphs):
 def test_hub_graph_maxnodes4_set_is_frequent_by_definition(tfsm, graphs, tmp_path):
     """Mining the 2M-vertex hub graph to 4 pattern vertices (the benchmark workload; the reference's
     miners do not finish it here) reports the 3 412 patterns of tests/golden/cfg4_m4.brute.txt, each
-    with exact support >= tau by the definition checker, and its patterns of at most 3 vertices are
-    the reference's maxNodes-3 set.  (Soundness of every reported pattern; completeness rests on
-    the candidate generation pinned by the smaller goldens.)"""
+    with exact support >= tau by the definition checker, its patterns of at most 3 vertices are
+    the reference's maxNodes-3 set, and the exact MNI of every one equals the checker's.
+    (Soundness of every reported pattern; completeness rests on the candidate generation pinned by
+    the smaller goldens.)"""
     want = read_mni(GOLDEN / "cfg4_m4.brute.txt")
     tau = CASES["cfg4_m3"]["tau"]
     assert len(want) == 3412 and all(min(v) >= tau for v in want.values())
@@ -207,6 +208,10 @@ def test_hub_graph_maxnodes4_set_is_frequent_by_definition(tfsm, graphs, tmp_pat
     assert set(pats) == set(want)
     small = {k for k in pats if len({x for c in k.split() for x in c.split(",")[:2]}) <= 3}
     assert small == golden_pattern_set("cfg4_m3")
+    keys = list(want)  # exact MNI of every one equals the checker's (about 5 s)
+    res = g.evaluate([tfsm.parse_key(k) for k in keys], flags=tfsm.FLAG_EXACT)
+    bad = [(k, want[k], r.mni) for k, r in zip(keys, res) if r.status != 0 or r.mni != want[k]]
+    assert not bad, f"{len(bad)} of {len(keys)} differ, e.g. {bad[:3]}"
 
 
 def test_hub_graph_maxnodes5_sample_is_frequent_by_definition(tfsm, graphs):
