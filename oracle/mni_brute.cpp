@@ -12,8 +12,10 @@
 // vertex numbering as the reference).  Every found embedding adds all its vertices to their
 // pattern vertices' domains; the remaining candidates are searched exhaustively, in parallel.
 //
-// usage: mni_brute -file G.lg -freq TAU -patterns P.txt [-threads T]
-//   P.txt and the output use the format of mni_harness: "<codes> | c0 c1 ... c(n-1)".
+// usage: mni_brute -file G.lg -freq TAU -patterns P.txt [-threads T] [-decide 1]
+//   P.txt and the output use the format of mni_harness: "<codes> | c0 c1 ... c(n-1)".  With
+//   -decide 1 the counts are lower bounds that reach TAU everywhere exactly when the pattern is
+//   frequent (the search stops early both ways).
 #include <algorithm>
 #include <array>
 #include <atomic>
@@ -134,14 +136,16 @@ struct Search {
 int main(int argc, char **argv) {
     const char *file = nullptr, *pats = nullptr;
     int tau = -1, threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    bool decide = false;
     for (int i = 1; i + 1 < argc; i += 2) {
         if (!strcmp(argv[i], "-file")) file = argv[i + 1];
         else if (!strcmp(argv[i], "-freq")) tau = atoi(argv[i + 1]);
         else if (!strcmp(argv[i], "-patterns")) pats = argv[i + 1];
         else if (!strcmp(argv[i], "-threads")) threads = std::max(1, atoi(argv[i + 1]));
+        else if (!strcmp(argv[i], "-decide")) decide = atoi(argv[i + 1]) != 0;
     }
     if (!file || !pats || tau < 0) {
-        std::cerr << "usage: mni_brute -file G.lg -freq TAU -patterns P.txt [-threads T]" << std::endl;
+        std::cerr << "usage: mni_brute -file G.lg -freq TAU -patterns P.txt [-threads T] [-decide 1]" << std::endl;
         return 2;
     }
     const tfsm::LgGraph g = tfsm::load_lg(file, tau);
@@ -160,24 +164,39 @@ int main(int argc, char **argv) {
             std::vector<std::atomic<uint8_t>> z(g.n);
             f.swap(z);
         }
+        // -decide: stop a vertex once tau of its candidates are found, and the pattern once a
+        // vertex cannot reach tau; the counts printed are then lower bounds, and the pattern is
+        // frequent exactly when every count reaches tau
+        std::vector<std::atomic<uint64_t>> nfound(p.n);
         for (int u = 0; u < p.n; ++u) {
+            uint64_t cands = 0;
+            for (uint32_t v = 0; v < g.n; ++v) cands += g.vlabel[v] == p.lab[u];
             std::atomic<uint32_t> next{0};
+            std::atomic<uint64_t> nfail{0};
+            auto settled = [&] {
+                return decide && (nfound[u].load() >= (uint64_t)tau || cands - nfail.load() < (uint64_t)tau);
+            };
             std::vector<std::thread> th;
             for (int t = 0; t < threads; ++t)
                 th.emplace_back([&, u] {
                     Search s(g, p, u);
                     for (;;) {
                         const uint32_t v0 = next.fetch_add(64);
-                        if (v0 >= g.n) break;
+                        if (v0 >= g.n || settled()) break;
                         for (uint32_t v = v0; v < std::min<uint32_t>(g.n, v0 + 64); ++v) {
                             if (g.vlabel[v] != p.lab[u] || found[u][v].load()) continue;
                             s.emb[u] = v;
-                            if (s.dfs(1))
-                                for (int w = 0; w < p.n; ++w) found[w][s.emb[w]].store(1);
+                            if (s.dfs(1)) {
+                                for (int w = 0; w < p.n; ++w)
+                                    if (found[w][s.emb[w]].exchange(1) == 0) nfound[w].fetch_add(1);
+                            } else {
+                                nfail.fetch_add(1);
+                            }
                         }
                     }
                 });
             for (auto &t : th) t.join();
+            if (decide && cands - nfail.load() < (uint64_t)tau) break;  // infrequent
         }
         std::cout << line << " |";
         for (int u = 0; u < p.n; ++u) {
