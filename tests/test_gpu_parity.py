@@ -192,8 +192,9 @@ def test_hub_graph_wide_sample_matches_definition(tfsm, graphs):
 
 def test_hub_graph_maxnodes4_set_is_frequent_by_definition(tfsm, graphs, tmp_path):
     """Mining the 2M-vertex hub graph to 4 pattern vertices (the benchmark workload; the reference's
-    miners do not finish it here) reports the 3 412 patterns of tests/golden/cfg4_m4.brute.txt, each
-    with exact support >= tau by the definition checker, its patterns of at most 3 vertices are
+    miners do not finish it here) reports the 3 412 patterns of tests/golden/cfg4_m4.brute.txt (the
+    set the CPU restatement of the reference's algorithm reports too), each with exact support
+    >= tau by the definition checker, its patterns of at most 3 vertices are
     the reference's maxNodes-3 set, and the exact MNI of every one equals the checker's.
     (Soundness of every reported pattern; completeness rests on the candidate generation pinned by
     the smaller goldens.)"""
