@@ -41,17 +41,28 @@ def canon(labels: tuple, edges: frozenset) -> tuple:
 
 
 def to_codes(key: tuple) -> str:
-    """Any connected edge order as DFS-code-like tokens "a,b,la,el,lb" (the checker's input)."""
+    """The pattern as a valid DFS code sequence "a,b,la,el,lb ..." (not necessarily the minimal one):
+    the first code is (0,1), every later one either adds the next vertex id (forward) or joins two
+    vertices already numbered (backward), as tfsm_evaluate_support and the checkers accept."""
     labels, edges = key
-    order, seen, rest = [], {edges[0][0]}, list(edges)
+    a0, b0, el0 = edges[0]
+    num = {a0: 0, b0: 1}
+    codes = [(0, 1, labels[a0], el0, labels[b0])]
+    rest = list(edges[1:])
     while rest:
         for e in rest:
-            if e[0] in seen or e[1] in seen:
-                order.append(e)
-                seen |= {e[0], e[1]}
-                rest.remove(e)
-                break
-    return " ".join(f"{a},{b},{labels[a]},{el},{labels[b]}" for a, b, el in order)
+            x, y, el = e
+            if x in num and y in num:
+                codes.append((num[x], num[y], labels[x], el, labels[y]))
+            elif x in num or y in num:
+                old, new = (x, y) if x in num else (y, x)
+                num[new] = len(num)
+                codes.append((num[old], num[new], labels[old], el, labels[new]))
+            else:
+                continue
+            rest.remove(e)
+            break
+    return " ".join(f"{a},{b},{la},{el},{lb}" for a, b, la, el, lb in codes)
 
 
 def from_results(path: Path) -> set:

@@ -83,7 +83,11 @@ MNI_SAMPLES = {"cfg4_sample": dict(graph_case="cfg4_m3", reference=True),
                "cfg4_m4": dict(graph_case="cfg4_m3", reference=False),
                # every 100th (from the first) of the sorted 5-vertex keys the GPU miner reports
                # there at maxNodes 5 (423 of 42 277)
-               "cfg4_m5_sample": dict(graph_case="cfg4_m3", reference=False)}
+               "cfg4_m5_sample": dict(graph_case="cfg4_m3", reference=False),
+               # the 358 patterns of at most 4 vertices frequent there by the definition
+               # (oracle/enumerate_frequent.py) that the reference's growth never produces (the
+               # cfg4_m4 set lacks them), in oracle/enumerate_frequent.py's key order
+               "cfg4_unreached": dict(graph_case="cfg4_m3", reference=False)}
 
 # Small hand-made graphs for edge cases, written by make_small_graphs().
 FILE_CASES = {

@@ -233,6 +233,25 @@ def test_hub_graph_maxnodes5_sample_is_frequent_by_definition(tfsm, graphs):
     assert not bad, f"{len(bad)} of {len(some)} differ, e.g. {bad[:3]}"
 
 
+def test_hub_graph_patterns_outside_the_reference_growth(tfsm, graphs):
+    """The 358 patterns of at most 4 vertices that are frequent on the 2M-vertex hub graph by the
+    definition but that the reference's growth never produces (tests/golden/cfg4_unreached.*): the
+    drop-in's evaluation, called on them directly, decides every one frequent and its exact MNI
+    equals the definition checker's."""
+    want = read_mni(GOLDEN / "cfg4_unreached.brute.txt")
+    tau = CASES["cfg4_m3"]["tau"]
+    keys = list(want)
+    assert len(keys) == 358 and all(min(v) >= tau for v in want.values())
+    g = graphs("cfg4_m3")
+    pats = [tfsm.parse_key(k) for k in keys]
+    lazy = g.evaluate(pats)
+    bad = [(k, r.status, r.frequent, r.support) for k, r in zip(keys, lazy) if r.status != 0 or not r.frequent]
+    assert not bad, f"{len(bad)} of {len(keys)}, e.g. {bad[:3]}"
+    res = g.evaluate(pats, flags=tfsm.FLAG_EXACT)
+    bad = [(k, want[k], r.mni) for k, r in zip(keys, res) if r.status != 0 or r.mni != want[k]]
+    assert not bad, f"{len(bad)} of {len(keys)} differ, e.g. {bad[:3]}"
+
+
 @pytest.mark.parametrize("case", ["cfg1", "el3", "quirk_elabels", "cfg2_t9000"])
 def test_lazy_decision_matches_exact_support(tfsm, graphs, case):
     want = golden_mni(case)
